@@ -1,0 +1,434 @@
+#!/usr/bin/env python
+"""Throughput benchmark of the GB300 level-set solver.
+
+Workload (configuration 3 of the reference's benchmark plan): a 512^3
+periodic grid, G0 = perturbed sphere (r0 = 0.2, 8 spherical-harmonic modes),
+velocity = curl of a 24-mode random vector potential scaled to max|u| = 1,
+S_L = 0.2, dt from CFL 0.5 with the field-max speed, WENO-5 + TVD-RK3, HCR-2
+reinitialisation every 5 steps with 2 pseudo-steps.  Fields are seeded
+synthetic data generated on the device.
+
+One bench step = one reinitialisation period: 5 TVD-RK3 steps + 1 HCR-2
+(2 pseudo-steps).  Metric: Gcell-updates/s = interior cells x RK3 steps /
+time.  The headline value is the FP32-bulk form (FP64 interface constraint
+and reductions); the plain FP64 form is measured beside it.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the reference's algorithm on the host CPU cores
+(the oracle) on a bounded slab of the same workload.
+Multi-GPU runs are independent replicas (the path is not sharded); rank 0
+prints the aggregate.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "level-set-method-code_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "Gcell-updates/s at 512^3 FP32 vs FP64 at stated Linf; adjoint/forward cost ratio"
+RK_PER_BENCH_STEP = 5      # reinit interval
+REINIT_ITERS = 2
+CFL = 0.5
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--n", type=int, default=512)
+    ap.add_argument("--fp64-steps", type=int, default=2, help="timed FP64 bench steps (0 = skip)")
+    ap.add_argument("--e2e-steps", type=int, default=2, help="timed end-to-end calls (0 = skip)")
+    ap.add_argument("--e2e-rk-steps", type=int, default=50, help="RK3 steps per end-to-end call")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline sample length")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--json-out", default=None)
+    return ap.parse_args()
+
+
+# -- distributed plumbing (replicas) ------------------------------------------
+class Dist:
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+
+    def init(self, backend):
+        if self.world > 1:
+            import torch.distributed as dist
+            dist.init_process_group(backend)
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, x: float) -> float:
+        if not self.pg:
+            return x
+        import torch
+        dev = torch.device("cuda", self.local) if torch.cuda.is_available() else torch.device("cpu")
+        t = torch.tensor([x], dtype=torch.float64, device=dev)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, x: float) -> float:
+        if not self.pg:
+            return x
+        import torch
+        dev = torch.device("cuda", self.local) if torch.cuda.is_available() else torch.device("cpu")
+        t = torch.tensor([x], dtype=torch.float64, device=dev)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.SUM)
+        return float(t.item())
+
+    def done(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+# -- clocks ------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int, out_path: str | None = None):
+        self.gpu = gpu_index
+        self.out_path = out_path
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200", "-i", str(self.gpu)],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+            out, _ = self.proc.communicate()
+        self.lines = [l for l in out.splitlines() if l.strip()]
+        if self.out_path:
+            with open(self.out_path, "w") as f:
+                f.write(self.FIELDS + "\n" + "\n".join(self.lines) + "\n")
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in self.lines:
+            parts = [x.strip() for x in l.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# -- helpers -----------------------------------------------------------------
+def load_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def load_traffic(precision: str, n: int):
+    """dram bytes per stage-kernel launch from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "stage_traffic.json")
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        d = json.load(f)
+    e = d.get(f"{precision}_{n}")
+    return None if e is None else float(e["bytes_per_launch"])
+
+
+def make_solver(lsgb, syn, n: int, precision: str, stream):
+    wl = syn.config3(n)
+    p = lsgb.params(3, n, n, n, s_l=wl.s_l, enable_reinit=True, reinit_interval=RK_PER_BENCH_STEP,
+                    reinit_iterations=REINIT_ITERS)
+    s = lsgb.Solver(p, precision)
+    s.set_stream(stream)
+    s.synth(syn.to_device_desc(wl))
+    s.compute_dt(CFL)
+    return s, wl
+
+
+def time_solver(torch, s, stream, steps: int, warmup: int, dist: Dist | None, sampler=None):
+    """Returns (elapsed_ms over `steps` bench steps, kernel launches in the window,
+    stage_ms, stage_launches, reinit_ms, reinit_launches)."""
+    import lsgb
+    for _ in range(warmup):
+        s.advance(RK_PER_BENCH_STEP)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    s.enable_timing(True)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    n0 = lsgb.launch_count()
+    if sampler:
+        sampler.start()
+        time.sleep(0.3)
+    with torch.cuda.stream(stream):
+        e0.record(stream)
+        for _ in range(steps):
+            s.advance(RK_PER_BENCH_STEP)
+        e1.record(stream)
+    torch.cuda.synchronize()
+    if sampler:
+        sampler.stop()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    launches = lsgb.launch_count() - n0
+    ms = e0.elapsed_time(e1)
+    st_ms, st_n, re_ms, re_n = s.kernel_times()
+    s.enable_timing(False)
+    return ms, launches, st_ms, st_n, re_ms, re_n
+
+
+# -- CPU leg (oracle: the reference's algorithm on the host cores) -------------
+def cpu_sample(n: int, nz_slab: int, target_s: float, max_periods: int | None = None):
+    """Times the oracle (oracle/ls_oracle.c, OpenMP over all host cores) on a
+    512 x 512 x nz_slab periodic slab of the same workload.  Returns
+    (Gcell-updates/s, periods run, seconds, threads, per-period seconds)."""
+    import numpy as np
+    from lsgb import synthetic as syn
+    from oracle import Oracle, Problem
+    orc = Oracle("port")
+    wl = syn.config3(n)
+    wl.n = (n, n, nz_slab)
+    G, u, v, w = syn.host_fields(wl, normalise=False)
+    # same scale as the full grid (max |u| = 1 there): reuse the slab max
+    sp = float(np.sqrt(u * u + v * v + w * w).max())
+    u, v, w = u / sp, v / sp, w / sp
+    dt = syn.cfl_dt(wl, u, v, w, CFL)
+    pb = Problem(nx=n, ny=n, nz=nz_slab, dx=1 / n, dy=1 / n, dz=1 / n, dim=3, s_l=wl.s_l, dt=dt,
+                 enable_reinit=True, reinit_interval=RK_PER_BENCH_STEP, reinit_iterations=REINIT_ITERS)
+    cells = n * n * nz_slab
+    periods, t0, per = 0, time.perf_counter(), []
+    cur = G
+    while True:
+        a = time.perf_counter()
+        # step0 = 1 makes the last of the 5 steps of each call run the reinit
+        cur = orc.run(pb, RK_PER_BENCH_STEP, cur, u, v, w, step0=1)
+        per.append(time.perf_counter() - a)
+        periods += 1
+        el = time.perf_counter() - t0
+        if max_periods is not None:
+            if periods >= max_periods:
+                break
+        elif el >= target_s:
+            break
+    threads = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    return cells * RK_PER_BENCH_STEP * periods / el / 1e9, periods, el, threads, per
+
+
+def run_reference(args, dist: Dist):
+    """--impl reference: the reference algorithm on the host cores."""
+    if dist.rank != 0:
+        return
+    from oracle import build_port
+    build_port()
+    nz = 16
+    # warmup + timed steps, each one reinit period on the slab
+    _, _, _, threads, per = cpu_sample(args.n, nz, 0.0, max_periods=args.warmup + args.steps)
+    timed = per[args.warmup:]
+    step_s = sum(timed) / len(timed)
+    value = args.n * args.n * nz * RK_PER_BENCH_STEP / step_s / 1e9
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "Gcell-updates/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": step_s * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"config3 {args.n}x{args.n}x{nz} periodic slab of the {args.n}^3 workload "
+                               "(per-cell work identical), FP64, WENO5-RK3 + HCR-2 every 5 steps",
+                   "bench_step": "5 RK3 steps + 1 HCR-2 reinit (2 pseudo-steps)"},
+        "cpu_baseline": {"value": value, "unit": "Gcell-updates/s", "cores": threads, "kind": "port",
+                         "sample": f"{args.n}x{args.n}x{nz} slab, {len(timed)} periods of 5 RK3 steps"},
+        "e2e": {"value": value, "unit": "Gcell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, dist: Dist):
+    import numpy as np
+    import torch
+    import __graft_entry__ as ge
+
+    ge.build_library()
+    import lsgb
+    from lsgb import synthetic as syn
+
+    torch.cuda.set_device(dist.local)
+    dist.init("nccl")
+    n = args.n
+    cells = n ** 3
+    stream = torch.cuda.Stream()
+    os.makedirs(os.path.join(ROOT, "gpurun_out"), exist_ok=True)
+    sampler = ClockSampler(dist.local, os.path.join(ROOT, "gpurun_out", f"clocks_rank{dist.rank}.csv"))
+
+    # --- FP32-bulk headline ---
+    s32, wl = make_solver(lsgb, syn, n, "f32", stream)
+    dt = s32.params().dt
+    ms, launches, st_ms, st_n, re_ms, re_n = time_solver(torch, s32, stream, args.steps, args.warmup, dist, sampler)
+    ms_max = dist.max(ms)
+    rk_steps = args.steps * RK_PER_BENCH_STEP
+    value = dist.world * cells * rk_steps / (ms_max * 1e-3) / 1e9
+
+    # roofline of the dominant kernel (the fused RK3 stage): stage 1 moves
+    # G, u, v, w in and G1 out (5 fields), stages 2 and 3 also read G^n (6)
+    s_bytes = 4
+    stage_bytes_total = cells * s_bytes * 17 * rk_steps
+    peak, peak_kind = load_peaks()
+    achieved = stage_bytes_total / (st_ms * 1e-3) / 1e9
+    traffic = load_traffic("f32", n)
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
+                "kernel": "stage_f32_kernel (fused WENO5 RHS + RK3 stage combine)",
+                "algorithmic_bytes_per_launch": cells * s_bytes * 17 / 3,
+                "launches": st_n, "avg_launch_ms": st_ms / max(st_n, 1)}
+    step_bytes = cells * s_bytes * (17 + (4 + 5 * REINIT_ITERS) / RK_PER_BENCH_STEP)
+    whole_step_gbs = step_bytes * rk_steps / (ms * 1e-3) / 1e9
+    clocks = sampler.summary()
+
+    # --- end to end through the public C ABI with host buffers ---
+    e2e = None
+    if args.e2e_steps > 0:
+        shape = (n + 6,) * 3
+        host = [torch.empty(shape, dtype=torch.float64, pin_memory=True) for _ in range(5)]
+        for name, t in zip(("G", "u", "v", "w"), host[:4]):
+            s32.get_field(name, out=t.numpy())
+        s32.run_host(host[0].numpy(), host[1].numpy(), host[2].numpy(), host[3].numpy(), args.e2e_rk_steps,
+                     host[4].numpy())  # warm
+        torch.cuda.synchronize()
+        dist.barrier()
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+        with torch.cuda.stream(stream):
+            ev[0].record(stream)
+            for _ in range(args.e2e_steps):
+                s32.run_host(host[0].numpy(), host[1].numpy(), host[2].numpy(), host[3].numpy(),
+                             args.e2e_rk_steps, host[4].numpy())
+            ev[1].record(stream)
+        torch.cuda.synchronize()
+        e2e_ms = dist.max(ev[0].elapsed_time(ev[1]))
+        e2e = {"value": dist.world * cells * args.e2e_rk_steps * args.e2e_steps / (e2e_ms * 1e-3) / 1e9,
+               "unit": "Gcell-updates/s", "h2d_bytes_per_step": 4 * shape[0] ** 3 * 8,
+               "d2h_bytes_per_step": shape[0] ** 3 * 8,
+               "call": "lsgb_solver_run_host (ghosted FP64 host arrays G,u,v,w in, G out)",
+               "rk3_steps_per_call": args.e2e_rk_steps}
+        del host
+
+    # --- plain FP64 form beside it, and the FP32-vs-FP64 error after the same steps ---
+    fp64 = None
+    prec = None
+    if args.fp64_steps > 0:
+        s64, _ = make_solver(lsgb, syn, n, "f64", stream)
+        s64.set_dt(dt)
+        ms64, _, st64, stn64, _, _ = time_solver(torch, s64, stream, args.fp64_steps, 1, None)
+        v64 = dist.world * cells * args.fp64_steps * RK_PER_BENCH_STEP / (dist.max(ms64) * 1e-3) / 1e9
+        fp64 = {"value": v64, "unit": "Gcell-updates/s", "ms_per_step": ms64 / args.fp64_steps,
+                "stage_avg_launch_ms": st64 / max(stn64, 1),
+                "fp32_speedup": value / v64}
+        total_periods = 1 + args.fp64_steps
+        # FP32 from the same initial state for the same number of steps
+        s32b, _ = make_solver(lsgb, syn, n, "f32", stream)
+        s32b.set_dt(dt)
+        s32b.advance(total_periods * RK_PER_BENCH_STEP)
+        g64 = s64.get_G(layout="compact")
+        g32 = s32b.get_G(layout="compact")
+        d = np.abs(g32 - g64)
+        band = np.abs(g64) < 3.0 / n
+        prec = {"rk3_steps": total_periods * RK_PER_BENCH_STEP,
+                "linf_G": float(d.max()), "linf_G_band3": float(d[band].max()) if band.any() else None,
+                "linf_G_band3_over_dx": (float(d[band].max()) * n) if band.any() else None,
+                "volume_f64": s64.volume()[0], "volume_f32": s32b.volume()[0]}
+        s64.close()
+        s32b.close()
+        del g64, g32, d, band
+
+    s32.close()
+
+    cpu = None
+    if not args.no_cpu_baseline and dist.rank == 0 and dist.world == 1:
+        rate, periods, el, threads, _ = cpu_sample(n, 16, args.cpu_seconds)
+        cpu = {"value": rate, "unit": "Gcell-updates/s", "cores": threads, "kind": "port",
+               "sample": f"{n}x{n}x16 slab of the workload, {periods} reinit periods "
+                         f"({periods * RK_PER_BENCH_STEP} RK3 steps), {el:.1f} s"}
+
+    if dist.rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "Gcell-updates/s", "n_gpus": dist.world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded config-3 fields generated on the device)",
+            "config": {"workload": f"config3 {n}^3 periodic, FP32-bulk WENO5-RK3 + HCR-2 (every 5 steps, "
+                                   "2 pseudo-steps, FP64 interface constraint), S_L=0.2, CFL 0.5",
+                       "grid": n, "bench_step": "5 RK3 steps + 1 HCR-2 reinit", "dt": dt,
+                       "l2": "inputs larger than L2 (each FP32 field 512 MiB)",
+                       "parallelism": f"replicas x{dist.world}"},
+            "roofline": roofline,
+            "whole_step_algorithmic_GBps": whole_step_gbs,
+            "cpu_baseline": cpu,
+            "e2e": e2e,
+            "gpu_launches": launches,
+            "clocks": clocks,
+            "fp64": fp64,
+            "precision_vs_fp64": prec,
+            "reinit_avg_launch_ms": re_ms / max(re_n, 1),
+        }
+        s = json.dumps(line)
+        print(s, flush=True)
+        if args.json_out:
+            with open(args.json_out, "w") as f:
+                f.write(s + "\n")
+    dist.done()
+
+
+def main():
+    args = parse()
+    dist = Dist()
+    if args.impl == "reference":
+        run_reference(args, dist)
+        return
+    run_ours(args, dist)
+
+
+if __name__ == "__main__":
+    main()

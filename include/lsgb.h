@@ -1,0 +1,273 @@
+/*
+ * lsgb.h -- C ABI of the GB300 level-set (G-equation) solver.
+ *
+ * Advances dG/dt + u_eff . grad G = 0, u_eff = u - S_L grad G / |grad G|, with
+ * WENO-5 upwind derivatives and TVD (Shu-Osher) RK3, and the HCR-2
+ * constrained reinitialisation, on one NVIDIA GB300 (sm_103a).
+ *
+ * Reference solver being replaced (juhoon196/Level-set-method-code):
+ * Local_code/level-set_MPI_3D (3D) and Local_code/level-set_MPI_2D (2D),
+ * whose hot-path functions are header-inline C++ called from src/main.cpp.
+ * Each entry point below names the reference function it stands in for.
+ *
+ * Conventions
+ *   - Every function returns LSGB_OK (0) or an LSGB_ERR_* code; the message of
+ *     the last failure on the calling thread is lsgb_last_error().  Nothing
+ *     calls exit() or abort().
+ *   - "Device" pointers are CUDA device (or managed) memory of the current
+ *     device; stream arguments are cudaStream_t values passed as void*
+ *     (NULL = the legacy default stream).  Work is stream-ordered; functions
+ *     that return a host scalar synchronise that stream.
+ *   - Field layout LSGB_LAYOUT_GHOSTED is the reference's: 3 ghost cells per
+ *     side, row-major, index k*(nx+6)*(ny+6) + j*(nx+6) + i
+ *     (Local_code/level-set_MPI_3D/include/config.h:301-306); 2D arrays have no
+ *     k term.  LSGB_LAYOUT_COMPACT is interior cells only, index
+ *     k*nx*ny + j*nx + i.
+ *   - The FP64 functions reproduce the reference's IEEE double arithmetic
+ *     operation for operation (no fused multiply-adds).
+ */
+#ifndef LSGB_H
+#define LSGB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define LSGB_API __attribute__((visibility("default")))
+#else
+#define LSGB_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define LSGB_OK 0
+#define LSGB_ERR_INVALID 1   /* bad argument or parameter block */
+#define LSGB_ERR_CUDA 2      /* a CUDA runtime call or kernel launch failed */
+#define LSGB_ERR_ALLOC 3     /* device or pinned-host allocation failed */
+#define LSGB_ERR_NUMERIC 4   /* non-finite value detected in a reduction */
+#define LSGB_ERR_STATE 5     /* call out of order (fields not set, ...) */
+#define LSGB_ERR_UNSUPPORTED 6
+
+/* boundary treatment per axis */
+#define LSGB_BC_PERIODIC 0       /* boundary.h:144-188 (3D), 2D boundary.h:98-114 */
+#define LSGB_BC_ZERO_GRADIENT 1  /* 2D boundary.h:126-147 */
+
+/* arithmetic of a solver handle */
+#define LSGB_PREC_F64 0  /* plain FP64, the reference's arithmetic */
+#define LSGB_PREC_F32 1  /* FP32 bulk; FP64 HCR-2 interface constraint and reductions */
+
+/* array layouts */
+#define LSGB_LAYOUT_GHOSTED 0
+#define LSGB_LAYOUT_COMPACT 1
+
+/* where a pointer lives */
+#define LSGB_MEM_HOST 0
+#define LSGB_MEM_DEVICE 1
+
+/*
+ * Parameter block: the fields of the reference's SimParams that the hot path
+ * reads (Local_code/level-set_MPI_3D/include/config.h:134-175), with the MPI
+ * decomposition fields replaced by one boundary code per axis.  Defaults as in
+ * config.h:88-107 come from lsgb_params_default().
+ */
+typedef struct lsgb_params {
+    int dim;                /* 2 or 3 */
+    int nx, ny, nz;         /* interior cells; nz is ignored when dim == 2 */
+    int nghost;             /* must be 3 (config.h:31) */
+    double dx, dy, dz;      /* spacing; dz ignored when dim == 2 */
+    double s_l;             /* laminar flame speed (uniform) */
+    double dt;              /* time step */
+    double cfl;             /* CFL number used by lsgb_cfl_dt */
+    double epsilon;         /* 1e-10: S_L gate and |grad G| regulariser (rk3.h:54-65) */
+    int enable_reinit;      /* HCR-2 on/off */
+    int reinit_interval;    /* reinit when step > 0 && step % interval == 0 (src/main.cpp:310) */
+    int reinit_iterations;  /* pseudo-time steps per reinit */
+    double reinit_dtau;     /* pseudo-time step, 0.25 * min spacing by default */
+    double reinit_beta;     /* HCR-2 forcing weight, 0.5 */
+    int bc_x, bc_y, bc_z;   /* LSGB_BC_* per axis */
+} lsgb_params;
+
+/* Fills *p with the reference's defaults for an nx x ny x nz grid on the unit
+ * cube/square with spacing 1/n (periodic on every axis). */
+LSGB_API void lsgb_params_default(lsgb_params* p, int dim, int nx, int ny, int nz);
+
+/* Checks a parameter block; LSGB_OK or LSGB_ERR_INVALID with a message. */
+LSGB_API int lsgb_params_check(const lsgb_params* p);
+
+/* Message of the last failed call on this thread ("" if none). */
+LSGB_API const char* lsgb_last_error(void);
+
+/* Library version string. */
+LSGB_API const char* lsgb_version(void);
+
+/* Number of CUDA kernels this library has launched in this process (graph
+ * replays count every kernel node). */
+LSGB_API uint64_t lsgb_launch_count(void);
+
+/* ------------------------------------------------------------------------
+ * Drop-in entry points: device pointers in the reference's GHOSTED layout,
+ * FP64, the reference's calling convention (the caller owns every buffer).
+ * ------------------------------------------------------------------------ */
+
+/* One TVD-RK3 step G_n -> G_new, boundary fill after each stage.
+ * Replaces rk3TimeStep3D (Local_code/level-set_MPI_3D/include/rk3.h:131-150)
+ * and rk3TimeStep (Local_code/level-set_MPI_2D/include/rk3.h:168-187).
+ * The reference's G_rhs scratch array is not needed: the RHS is fused into
+ * each stage.  G_1 and G_2 receive the stage fields as in the reference.
+ * w is ignored in 2D.  s_l_field (nullable, ghosted) is a per-cell flame
+ * speed that replaces p->s_l cell by cell (an addition; NULL = uniform). */
+LSGB_API int lsgb_rk3_step_f64(const lsgb_params* p, const double* G_n, double* G_new, double* G_1,
+                      double* G_2, const double* u, const double* v, const double* w,
+                      const double* s_l_field, void* stream);
+
+/* Ghost fill: applyBoundaryConditions3D (boundary.h:250-261) / 2D
+ * applyBoundaryConditions (2D boundary.h:217-229). */
+LSGB_API int lsgb_apply_bc_f64(const lsgb_params* p, double* G, void* stream);
+
+/* HCR-2 reinitialisation with the reference's pointer swap: on return *phi
+ * holds the result and *phi_tmp the other buffer; phi0, r_tilde and flag
+ * receive what the reference leaves in them.
+ * Replaces reinitializeWithSwap3D (Local_code/level-set_MPI_3D/include/reinitialization.h:199-228)
+ * and reinitializeWithSwap (Local_code/level-set_MPI_2D/include/reinitialization.h:321-360).
+ * Runs regardless of p->enable_reinit (the caller decides the cadence). */
+LSGB_API int lsgb_reinit_f64(const lsgb_params* p, double** phi, double** phi_tmp, double* phi0,
+                    double* r_tilde, int32_t* flag, void* stream);
+
+/* sum of dx*dy*dz over interior cells with G < 0 and that cell count.
+ * Replaces computeInterfaceVolume (io.h:263-288) / computeInterfaceArea
+ * (2D io.h:225-249).  Synchronises the stream. */
+LSGB_API int lsgb_volume_f64(const lsgb_params* p, const double* G, double* volume, int64_t* count,
+                    void* stream);
+
+/* sqrt(mean over interior of (G - G_ref)^2).  Replaces computeL2Error3D
+ * (io.h:229-258) / computeL2Error (2D io.h:194-220).  Synchronises. */
+LSGB_API int lsgb_l2_error_f64(const lsgb_params* p, const double* G, const double* G_ref, double* l2,
+                      void* stream);
+
+/* max over interior cells of |u|+|v|(+|w|).  Synchronises. */
+LSGB_API int lsgb_max_speed_f64(const lsgb_params* p, const double* u, const double* v, const double* w,
+                       double* max_speed, void* stream);
+
+/* CFL step cfl * min spacing / (max_speed + s_l), 2.0 as the speed below
+ * epsilon: calculateTimeStep (config.h:272-293) with the field maximum in
+ * place of the constant velocities.  Host only. */
+LSGB_API int lsgb_cfl_dt(const lsgb_params* p, double max_speed, double* dt);
+
+/* ------------------------------------------------------------------------
+ * Solver handle: device-resident fields in the compact layout, FP64 or the
+ * FP32-bulk form, steps captured in CUDA graphs.  This is the fast path.
+ * ------------------------------------------------------------------------ */
+typedef struct lsgb_solver lsgb_solver;
+
+LSGB_API int lsgb_solver_create(const lsgb_params* p, int precision, lsgb_solver** out);
+LSGB_API int lsgb_solver_destroy(lsgb_solver* s);
+
+/* Stream the handle issues its work on (void* cudaStream_t; NULL = own stream). */
+LSGB_API int lsgb_solver_set_stream(lsgb_solver* s, void* stream);
+
+/* Current parameters (dt may have been set by lsgb_solver_compute_dt). */
+LSGB_API int lsgb_solver_get_params(const lsgb_solver* s, lsgb_params* p);
+
+/* Replace dt (e.g. the reference's final-step clip). */
+LSGB_API int lsgb_solver_set_dt(lsgb_solver* s, double dt);
+
+/* Load G and the velocity (w ignored in 2D) from FP64 arrays of the given
+ * layout in host or device memory; FP32 handles convert on the device.  Any
+ * pointer may be NULL to keep the current field. */
+LSGB_API int lsgb_solver_set_fields(lsgb_solver* s, const double* G, const double* u, const double* v,
+                           const double* w, int layout, int memory);
+
+/* Per-cell flame speed (FP64, given layout/memory); NULL restores uniform p->s_l. */
+LSGB_API int lsgb_solver_set_sl_field(lsgb_solver* s, const double* sl, int layout, int memory);
+
+/* Store G as FP64 in the given layout (ghost cells filled as the reference's
+ * boundary fill leaves them) to host or device memory. */
+LSGB_API int lsgb_solver_get_G(lsgb_solver* s, double* G, int layout, int memory);
+
+/* Advance n_steps TVD-RK3 steps; HCR-2 runs after the step whose counter
+ * satisfies enable_reinit && step > 0 && step % reinit_interval == 0, the
+ * counter then increments (Local_code/level-set_MPI_3D/src/main.cpp:291-316).
+ * Asynchronous on the handle's stream. */
+LSGB_API int lsgb_solver_advance(lsgb_solver* s, int n_steps);
+
+/* Run one HCR-2 reinitialisation now (reinitializeWithSwap3D). */
+LSGB_API int lsgb_solver_reinit(lsgb_solver* s);
+
+/* Step counter used for the reinit cadence. */
+LSGB_API int lsgb_solver_get_step(const lsgb_solver* s, int* step);
+LSGB_API int lsgb_solver_set_step(lsgb_solver* s, int step);
+
+/* Reductions over the current G / velocity (FP64 accumulation; synchronise). */
+LSGB_API int lsgb_solver_volume(lsgb_solver* s, double* volume, int64_t* count);
+LSGB_API int lsgb_solver_max_speed(lsgb_solver* s, double* max_speed);
+/* Sets dt from the CFL formula with the field-max speed; returns it. */
+LSGB_API int lsgb_solver_compute_dt(lsgb_solver* s, double cfl, double* dt);
+/* L2 difference of G against an FP64 field (given layout/memory). */
+LSGB_API int lsgb_solver_l2_error(lsgb_solver* s, const double* G_ref, int layout, int memory, double* l2);
+
+/* End to end on host buffers, the call a host-side caller makes: upload G, u,
+ * v, w (FP64, given layout, host memory), advance n_steps, download G into
+ * G_out (same layout).  Synchronises.  Any velocity pointer may be NULL to
+ * keep the resident field. */
+LSGB_API int lsgb_solver_run_host(lsgb_solver* s, const double* G, const double* u, const double* v,
+                         const double* w, int n_steps, double* G_out, int layout);
+
+/* Store one resident field as FP64 (given layout / memory): which = 0 G,
+ * 1 u, 2 v, 3 w, 4 the per-cell S_L field.  Ghosts are filled as the
+ * reference's boundary fill leaves them. */
+#define LSGB_FIELD_G 0
+#define LSGB_FIELD_U 1
+#define LSGB_FIELD_V 2
+#define LSGB_FIELD_W 3
+#define LSGB_FIELD_SL 4
+LSGB_API int lsgb_solver_get_field(lsgb_solver* s, int which, double* out, int layout, int memory);
+
+/* Kernel timing with CUDA events on the handle's stream, for roofline
+ * accounting.  While enabled, every RK3 stage launch and every HCR-2
+ * pseudo-step launch is bracketed by events; lsgb_solver_kernel_times
+ * synchronises and returns the summed durations (ms) and launch counts since
+ * the last enable. */
+LSGB_API int lsgb_solver_enable_timing(lsgb_solver* s, int enable);
+LSGB_API int lsgb_solver_kernel_times(lsgb_solver* s, double* stage_ms, int64_t* stage_launches,
+                                      double* reinit_ms, int64_t* reinit_launches);
+
+/* Deformation-vortex velocity of the reference's default 3D test case at time
+ * t with period T, evaluated on the device at the cell centres x_i = i * dx:
+ * computeDeformationVelocity / updateDeformationVelocity
+ * (Local_code/level-set_MPI_3D/include/initial_conditions.h:232-282). */
+LSGB_API int lsgb_solver_set_velocity_deformation(lsgb_solver* s, double t, double T);
+
+/* ------------------------------------------------------------------------
+ * Synthetic benchmark fields, generated on the device (FP64 arithmetic).
+ *   G0 = |x - c| - (r0 + sum_m a_m Y_lm(theta, phi))      (sphere; 3D)
+ *   G0 = |x - c| - r0                                    (circle; 2D)
+ *   u  = sum_m c_m cos(2 pi k_m . x + phi_m), c_m = 2 pi k_m x a_m (curl of
+ *        A = sum a_m sin(2 pi k_m . x + phi_m)), scaled by vel_scale.
+ * Mode tables are drawn on the host from the seed (see lsgb/synthetic.py).
+ * ------------------------------------------------------------------------ */
+#define LSGB_MAX_MODES 32
+typedef struct lsgb_synth {
+    double center[3];
+    double r0;
+    int n_shape_modes;                 /* spherical-harmonic perturbations */
+    int shape_l[LSGB_MAX_MODES];
+    int shape_m[LSGB_MAX_MODES];
+    double shape_amp[LSGB_MAX_MODES];
+    int n_vel_modes;                   /* Fourier modes of the vector potential */
+    double vel_k[LSGB_MAX_MODES][3];
+    double vel_c[LSGB_MAX_MODES][3];   /* 2 pi k x a (before vel_scale) */
+    double vel_phase[LSGB_MAX_MODES];
+    double vel_scale;
+} lsgb_synth;
+
+/* Fill G, u, v, w of the handle from the description (device side). */
+LSGB_API int lsgb_solver_synth(lsgb_solver* s, const lsgb_synth* d);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LSGB_H */

@@ -1,0 +1,834 @@
+// api.cu -- the C ABI declared in include/lsgb.h.
+//
+// Host logic only: parameter checks, error reporting, the drop-in FP64
+// entry points over caller-owned ghosted arrays, and the solver handle that
+// keeps compact device-resident fields and sequences the kernels of
+// f64_kernels.cu / f32_kernels.cu / reduce.cu / synth.cu on one stream.
+#include "common.cuh"
+
+#include <atomic>
+#include <cmath>
+#include <cstdarg>
+#include <cstring>
+#include <string>
+#include <utility>
+#include <vector>
+
+namespace lsgb {
+
+static std::atomic<uint64_t> g_launches{0};
+void count_launches(uint64_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return code;
+}
+
+#define LSGB_CUDA(call)                                                                  \
+    do {                                                                                 \
+        cudaError_t e_ = (call);                                                         \
+        if (e_ != cudaSuccess)                                                           \
+            return fail(LSGB_ERR_CUDA, "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), \
+                        __FILE__, __LINE__);                                             \
+    } while (0)
+
+#define LSGB_TRY(call)             \
+    do {                           \
+        int rc_ = (call);          \
+        if (rc_ != LSGB_OK) return rc_; \
+    } while (0)
+
+Geo geo_of(const lsgb_params& p) {
+    Geo g;
+    g.dim = p.dim;
+    g.nx = p.nx;
+    g.ny = p.ny;
+    g.nz = p.dim == 3 ? p.nz : 1;
+    g.bcx = p.bc_x;
+    g.bcy = p.bc_y;
+    g.bcz = p.dim == 3 ? p.bc_z : LSGB_BC_PERIODIC;
+    return g;
+}
+
+bool finite_pos(double x) { return std::isfinite(x) && x > 0.0; }
+
+int check_params(const lsgb_params* p) {
+    if (!p) return fail(LSGB_ERR_INVALID, "params is NULL");
+    if (p->dim != 2 && p->dim != 3) return fail(LSGB_ERR_INVALID, "dim must be 2 or 3 (got %d)", p->dim);
+    if (p->nghost != NG) return fail(LSGB_ERR_INVALID, "nghost must be 3 (got %d)", p->nghost);
+    if (p->nx < 3 || p->ny < 3 || (p->dim == 3 && p->nz < 3))
+        return fail(LSGB_ERR_INVALID, "every axis needs at least 3 interior cells (got %d x %d x %d)",
+                    p->nx, p->ny, p->dim == 3 ? p->nz : 1);
+    long long tot = (long long)(p->nx + 6) * (p->ny + 6) * (p->dim == 3 ? p->nz + 6 : 1);
+    if (tot > (1LL << 34)) return fail(LSGB_ERR_INVALID, "grid too large (%lld cells with ghosts)", tot);
+    if (!finite_pos(p->dx) || !finite_pos(p->dy) || (p->dim == 3 && !finite_pos(p->dz)))
+        return fail(LSGB_ERR_INVALID, "grid spacing must be positive and finite");
+    if (!std::isfinite(p->dt) || p->dt < 0.0) return fail(LSGB_ERR_INVALID, "dt must be finite and >= 0");
+    if (!std::isfinite(p->s_l)) return fail(LSGB_ERR_INVALID, "s_l must be finite");
+    if (!std::isfinite(p->epsilon) || p->epsilon < 0.0) return fail(LSGB_ERR_INVALID, "epsilon must be finite and >= 0");
+    int bcs[3] = {p->bc_x, p->bc_y, p->dim == 3 ? p->bc_z : 0};
+    for (int a = 0; a < 3; ++a)
+        if (bcs[a] != LSGB_BC_PERIODIC && bcs[a] != LSGB_BC_ZERO_GRADIENT)
+            return fail(LSGB_ERR_INVALID, "unknown boundary code %d on axis %d", bcs[a], a);
+    if (p->enable_reinit) {
+        if (p->reinit_interval < 1) return fail(LSGB_ERR_INVALID, "reinit_interval must be >= 1");
+        if (p->reinit_iterations < 0) return fail(LSGB_ERR_INVALID, "reinit_iterations must be >= 0");
+        if (!std::isfinite(p->reinit_dtau) || !std::isfinite(p->reinit_beta))
+            return fail(LSGB_ERR_INVALID, "reinit_dtau / reinit_beta must be finite");
+    }
+    return LSGB_OK;
+}
+
+int check_dev(const void* ptr, const char* name) {
+    if (!ptr) return fail(LSGB_ERR_INVALID, "%s is NULL", name);
+    cudaPointerAttributes at;
+    cudaError_t e = cudaPointerGetAttributes(&at, ptr);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return fail(LSGB_ERR_INVALID, "%s: cudaPointerGetAttributes failed: %s", name, cudaGetErrorString(e));
+    }
+    if (at.type != cudaMemoryTypeDevice && at.type != cudaMemoryTypeManaged)
+        return fail(LSGB_ERR_INVALID, "%s is not device memory", name);
+    return LSGB_OK;
+}
+
+StageArgs stage_args(const lsgb_params& p, const Geo& g, const Lay& lay) {
+    StageArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.g = g;
+    a.lay = lay;
+    a.s_l = p.s_l;
+    a.eps = p.epsilon;
+    a.dx = p.dx;
+    a.dy = p.dy;
+    a.dz = p.dim == 3 ? p.dz : p.dx;
+    a.dt = p.dt;
+    return a;
+}
+
+double cell_volume(const lsgb_params& p) {
+    return p.dim == 3 ? p.dx * p.dy * p.dz : p.dx * p.dy;
+}
+
+// Stream-ordered scratch for one reduction call of the drop-in API
+// (partials + two result slots).
+struct CallScratch {
+    double* d = nullptr;
+    cudaStream_t st;
+    explicit CallScratch(cudaStream_t s) : st(s) {}
+    int alloc() {
+        cudaError_t e = cudaMallocAsync((void**)&d, reduce_scratch_bytes() + 2 * sizeof(double), st);
+        if (e != cudaSuccess) { d = nullptr; return fail(LSGB_ERR_ALLOC, "scratch allocation failed: %s", cudaGetErrorString(e)); }
+        return LSGB_OK;
+    }
+    double* partials() const { return d; }
+    double* out() const { return d + 2 * (RED_BLOCKS + 1); }
+    ~CallScratch() { if (d) cudaFreeAsync(d, st); }
+};
+
+int read_result(const double* dev, double* host2, cudaStream_t st) {
+    LSGB_CUDA(cudaMemcpyAsync(host2, dev, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
+    LSGB_CUDA(cudaStreamSynchronize(st));
+    return LSGB_OK;
+}
+
+}  // namespace
+}  // namespace lsgb
+
+using namespace lsgb;
+
+// ---------------------------------------------------------------------------
+// misc
+// ---------------------------------------------------------------------------
+extern "C" void lsgb_params_default(lsgb_params* p, int dim, int nx, int ny, int nz) {
+    std::memset(p, 0, sizeof(*p));
+    p->dim = dim;
+    p->nx = nx;
+    p->ny = ny;
+    p->nz = dim == 3 ? nz : 1;
+    p->nghost = NG;
+    p->dx = 1.0 / nx;
+    p->dy = 1.0 / ny;
+    p->dz = dim == 3 ? 1.0 / nz : p->dx;
+    p->s_l = 0.0;
+    p->dt = 1.0e-3;
+    p->cfl = 0.2;
+    p->epsilon = 1.0e-10;
+    p->enable_reinit = 0;
+    p->reinit_interval = 10;
+    p->reinit_iterations = 2;
+    double h = dim == 3 ? std::fmin(p->dx, std::fmin(p->dy, p->dz)) : std::fmin(p->dx, p->dy);
+    p->reinit_dtau = 0.25 * h;
+    p->reinit_beta = 0.5;
+    p->bc_x = p->bc_y = p->bc_z = LSGB_BC_PERIODIC;
+}
+
+extern "C" int lsgb_params_check(const lsgb_params* p) { return check_params(p); }
+extern "C" const char* lsgb_last_error(void) { return g_err.c_str(); }
+extern "C" const char* lsgb_version(void) { return "lsgb 0.1 (sm_103a)"; }
+extern "C" uint64_t lsgb_launch_count(void) { return g_launches.load(); }
+
+extern "C" int lsgb_cfl_dt(const lsgb_params* p, double max_speed, double* dt) {
+    LSGB_TRY(check_params(p));
+    if (!dt) return fail(LSGB_ERR_INVALID, "dt is NULL");
+    double speed = max_speed + p->s_l;
+    if (speed < p->epsilon) speed = 2.0;
+    double dmin = p->dim == 3 ? std::fmin(p->dx, std::fmin(p->dy, p->dz)) : std::fmin(p->dx, p->dy);
+    *dt = p->cfl * dmin / speed;
+    return LSGB_OK;
+}
+
+// ---------------------------------------------------------------------------
+// drop-in FP64 entry points (ghosted, caller-owned device buffers)
+// ---------------------------------------------------------------------------
+extern "C" int lsgb_rk3_step_f64(const lsgb_params* p, const double* G_n, double* G_new,
+                                 double* G_1, double* G_2, const double* u, const double* v,
+                                 const double* w, const double* s_l_field, void* stream) {
+    LSGB_TRY(check_params(p));
+    LSGB_TRY(check_dev(G_n, "G_n"));
+    LSGB_TRY(check_dev(G_new, "G_new"));
+    LSGB_TRY(check_dev(G_1, "G_1"));
+    LSGB_TRY(check_dev(G_2, "G_2"));
+    LSGB_TRY(check_dev(u, "u"));
+    LSGB_TRY(check_dev(v, "v"));
+    if (p->dim == 3) LSGB_TRY(check_dev(w, "w"));
+    if (s_l_field) LSGB_TRY(check_dev(s_l_field, "s_l_field"));
+    if (G_new == G_n || G_1 == G_n || G_2 == G_n || G_1 == G_2 || G_new == G_2)
+        return fail(LSGB_ERR_INVALID, "G_new, G_1, G_2 must be distinct from G_n and each other");
+    cudaStream_t st = (cudaStream_t)stream;
+    Geo g = geo_of(*p);
+    Lay lay = ghosted_layout(g);
+    StageArgs a = stage_args(*p, g, lay);
+    a.u = u; a.v = v; a.w = w; a.sl = s_l_field;
+    a.Gn = G_n;
+    a.Gin = G_n; a.Gout = G_1; a.stage = 1;
+    LSGB_CUDA(launch_stage_f64(a, st));
+    LSGB_CUDA(launch_bc_fill_f64(g, G_1, st));
+    a.Gin = G_1; a.Gout = G_2; a.stage = 2;
+    LSGB_CUDA(launch_stage_f64(a, st));
+    LSGB_CUDA(launch_bc_fill_f64(g, G_2, st));
+    a.Gin = G_2; a.Gout = G_new; a.stage = 3;
+    LSGB_CUDA(launch_stage_f64(a, st));
+    LSGB_CUDA(launch_bc_fill_f64(g, G_new, st));
+    return LSGB_OK;
+}
+
+extern "C" int lsgb_apply_bc_f64(const lsgb_params* p, double* G, void* stream) {
+    LSGB_TRY(check_params(p));
+    LSGB_TRY(check_dev(G, "G"));
+    LSGB_CUDA(launch_bc_fill_f64(geo_of(*p), G, (cudaStream_t)stream));
+    return LSGB_OK;
+}
+
+extern "C" int lsgb_reinit_f64(const lsgb_params* p, double** phi, double** phi_tmp,
+                               double* phi0, double* r_tilde, int32_t* flag, void* stream) {
+    LSGB_TRY(check_params(p));
+    if (!phi || !phi_tmp) return fail(LSGB_ERR_INVALID, "phi / phi_tmp handles are NULL");
+    LSGB_TRY(check_dev(*phi, "*phi"));
+    LSGB_TRY(check_dev(*phi_tmp, "*phi_tmp"));
+    LSGB_TRY(check_dev(phi0, "phi0"));
+    LSGB_TRY(check_dev(r_tilde, "r_tilde"));
+    LSGB_TRY(check_dev(flag, "flag"));
+    cudaStream_t st = (cudaStream_t)stream;
+    Geo g = geo_of(*p);
+    Lay lay = ghosted_layout(g);
+    size_t bytes = sizeof(double) * (size_t)layout_elems(g, 1);
+    LSGB_CUDA(cudaMemcpyAsync(phi0, *phi, bytes, cudaMemcpyDeviceToDevice, st));
+    LSGB_CUDA(launch_bc_fill_f64(g, phi0, st));
+    LSGB_CUDA(launch_crossings_f64(g, lay, phi0, r_tilde, flag, st));
+    double* a = *phi;
+    double* b = *phi_tmp;
+    for (int it = 0; it < p->reinit_iterations; ++it) {
+        LSGB_CUDA(launch_reinit_step_stored_f64(g, lay, a, b, phi0, r_tilde, flag, p->dx, p->dy,
+                                                p->dim == 3 ? p->dz : p->dx, p->reinit_dtau,
+                                                p->reinit_beta, st));
+        std::swap(a, b);
+        LSGB_CUDA(launch_bc_fill_f64(g, a, st));
+    }
+    *phi = a;
+    *phi_tmp = b;
+    return LSGB_OK;
+}
+
+extern "C" int lsgb_volume_f64(const lsgb_params* p, const double* G, double* volume,
+                               int64_t* count, void* stream) {
+    LSGB_TRY(check_params(p));
+    LSGB_TRY(check_dev(G, "G"));
+    cudaStream_t st = (cudaStream_t)stream;
+    Geo g = geo_of(*p);
+    CallScratch s(st);
+    LSGB_TRY(s.alloc());
+    LSGB_CUDA(launch_count_negative<double>(g, ghosted_layout(g), G, s.partials(), s.out(), st));
+    double r[2];
+    LSGB_TRY(read_result(s.out(), r, st));
+    if (count) *count = (int64_t)r[0];
+    if (volume) *volume = r[0] * cell_volume(*p);
+    return LSGB_OK;
+}
+
+extern "C" int lsgb_l2_error_f64(const lsgb_params* p, const double* G, const double* G_ref,
+                                 double* l2, void* stream) {
+    LSGB_TRY(check_params(p));
+    LSGB_TRY(check_dev(G, "G"));
+    LSGB_TRY(check_dev(G_ref, "G_ref"));
+    if (!l2) return fail(LSGB_ERR_INVALID, "l2 is NULL");
+    cudaStream_t st = (cudaStream_t)stream;
+    Geo g = geo_of(*p);
+    Lay lay = ghosted_layout(g);
+    CallScratch s(st);
+    LSGB_TRY(s.alloc());
+    LSGB_CUDA(launch_sq_diff<double>(g, lay, G, G_ref, lay, s.partials(), s.out(), st));
+    double r[2];
+    LSGB_TRY(read_result(s.out(), r, st));
+    *l2 = std::sqrt(r[0] / (double)g.cells());
+    return LSGB_OK;
+}
+
+extern "C" int lsgb_max_speed_f64(const lsgb_params* p, const double* u, const double* v,
+                                  const double* w, double* max_speed, void* stream) {
+    LSGB_TRY(check_params(p));
+    LSGB_TRY(check_dev(u, "u"));
+    LSGB_TRY(check_dev(v, "v"));
+    if (p->dim == 3) LSGB_TRY(check_dev(w, "w"));
+    if (!max_speed) return fail(LSGB_ERR_INVALID, "max_speed is NULL");
+    cudaStream_t st = (cudaStream_t)stream;
+    Geo g = geo_of(*p);
+    CallScratch s(st);
+    LSGB_TRY(s.alloc());
+    LSGB_CUDA(launch_max_speed<double>(g, ghosted_layout(g), u, v, w, s.partials(), s.out(), st));
+    double r[2];
+    LSGB_TRY(read_result(s.out(), r, st));
+    *max_speed = r[0];
+    return LSGB_OK;
+}
+
+// ---------------------------------------------------------------------------
+// solver handle
+// ---------------------------------------------------------------------------
+struct lsgb_solver {
+    lsgb_params p;
+    Geo g;
+    Lay lay;            // compact
+    int prec;
+    size_t esz;         // bytes per element of the state fields
+    cudaStream_t st = nullptr;
+    bool own_stream = false;
+    void* G = nullptr;  // current field
+    void* A = nullptr;  // the two other state buffers
+    void* B = nullptr;
+    void* u = nullptr;
+    void* v = nullptr;
+    void* w = nullptr;
+    void* sl = nullptr;
+    double* stage64 = nullptr;   // FP64 ghosted staging for host/layout conversion
+    double* scratch = nullptr;   // reduction partials + results
+    double* h_res = nullptr;     // pinned result slots
+    int step = 0;
+    bool have_G = false, have_vel = false;
+    // kernel timing (lsgb_solver_enable_timing)
+    bool timing = false;
+    std::vector<cudaEvent_t> ev_pool;
+    size_t ev_used = 0;
+    std::vector<std::pair<size_t, int>> ev_marks;  // (first event index, kind 0 stage / 1 reinit)
+};
+
+namespace {
+
+size_t nbytes(const lsgb_solver* s) { return s->esz * (size_t)s->g.cells(); }
+
+int ensure_stage(lsgb_solver* s) {
+    if (s->stage64) return LSGB_OK;
+    size_t b = sizeof(double) * (size_t)layout_elems(s->g, 1);
+    cudaError_t e = cudaMalloc((void**)&s->stage64, b);
+    if (e != cudaSuccess) { s->stage64 = nullptr; return fail(LSGB_ERR_ALLOC, "staging allocation (%zu B): %s", b, cudaGetErrorString(e)); }
+    return LSGB_OK;
+}
+
+// Bring an FP64 array (layout, memory) into the compact state field dst.
+int load_field(lsgb_solver* s, void* dst, const double* src, int layout, int memory) {
+    Lay sl = layout == LSGB_LAYOUT_GHOSTED ? ghosted_layout(s->g) : compact_layout(s->g);
+    size_t sbytes = sizeof(double) * (size_t)layout_elems(s->g, sl.ghosted);
+    const double* dsrc = src;
+    if (memory == LSGB_MEM_HOST) {
+        if (s->prec == LSGB_PREC_F64 && !sl.ghosted) {
+            LSGB_CUDA(cudaMemcpyAsync(dst, src, sbytes, cudaMemcpyHostToDevice, s->st));
+            return LSGB_OK;
+        }
+        LSGB_TRY(ensure_stage(s));
+        LSGB_CUDA(cudaMemcpyAsync(s->stage64, src, sbytes, cudaMemcpyHostToDevice, s->st));
+        dsrc = s->stage64;
+    } else {
+        LSGB_TRY(check_dev(src, "field"));
+        if (s->prec == LSGB_PREC_F64 && !sl.ghosted) {
+            LSGB_CUDA(cudaMemcpyAsync(dst, src, sbytes, cudaMemcpyDeviceToDevice, s->st));
+            return LSGB_OK;
+        }
+    }
+    if (s->prec == LSGB_PREC_F64) LSGB_CUDA(launch_pack_f64(s->g, dsrc, sl, (double*)dst, s->st));
+    else LSGB_CUDA(launch_pack_f32(s->g, dsrc, sl, (float*)dst, s->st));
+    return LSGB_OK;
+}
+
+int alloc_field(lsgb_solver* s, void** f) {
+    cudaError_t e = cudaMalloc(f, nbytes(s));
+    if (e != cudaSuccess) { *f = nullptr; return fail(LSGB_ERR_ALLOC, "field allocation (%zu B): %s", nbytes(s), cudaGetErrorString(e)); }
+    return LSGB_OK;
+}
+
+// Event pair around one timed launch (no-op unless timing is enabled).
+int timed_begin(lsgb_solver* s, int kind, size_t* idx) {
+    if (!s->timing) return LSGB_OK;
+    while (s->ev_pool.size() < s->ev_used + 2) {
+        cudaEvent_t e;
+        LSGB_CUDA(cudaEventCreate(&e));
+        s->ev_pool.push_back(e);
+    }
+    *idx = s->ev_used;
+    s->ev_used += 2;
+    s->ev_marks.push_back({*idx, kind});
+    LSGB_CUDA(cudaEventRecord(s->ev_pool[*idx], s->st));
+    return LSGB_OK;
+}
+
+int timed_end(lsgb_solver* s, size_t idx) {
+    if (!s->timing) return LSGB_OK;
+    LSGB_CUDA(cudaEventRecord(s->ev_pool[idx + 1], s->st));
+    return LSGB_OK;
+}
+
+int launch_stage(lsgb_solver* s, const StageArgs& a) {
+    size_t ev = 0;
+    LSGB_TRY(timed_begin(s, 0, &ev));
+    if (s->prec == LSGB_PREC_F64) LSGB_CUDA(launch_stage_f64(a, s->st));
+    else LSGB_CUDA(launch_stage_f32(a, s->st));
+    LSGB_TRY(timed_end(s, ev));
+    return LSGB_OK;
+}
+
+// One TVD-RK3 step: G -> A (stage 1), A -> B (stage 2), (G, B) -> A (stage 3),
+// then A is the new G.
+int rk3_step(lsgb_solver* s) {
+    StageArgs a = stage_args(s->p, s->g, s->lay);
+    a.u = s->u; a.v = s->v; a.w = s->w; a.sl = s->sl;
+    a.Gn = s->G;
+    a.Gin = s->G; a.Gout = s->A; a.stage = 1;
+    LSGB_TRY(launch_stage(s, a));
+    a.Gin = s->A; a.Gout = s->B; a.stage = 2;
+    LSGB_TRY(launch_stage(s, a));
+    a.Gin = s->B; a.Gout = s->A; a.stage = 3;
+    LSGB_TRY(launch_stage(s, a));
+    std::swap(s->G, s->A);
+    return LSGB_OK;
+}
+
+// HCR-2 with phi0 = the current G buffer (left untouched), pseudo-steps
+// ping-ponging through A and B; r~ and flags are recomputed from phi0 inside
+// each pseudo-step (same operations as the stored form).
+int reinit(lsgb_solver* s) {
+    if (s->p.reinit_iterations <= 0) return LSGB_OK;
+    ReinitArgs r;
+    r.g = s->g;
+    r.lay = s->lay;
+    r.phi0 = s->G;
+    r.dx = s->p.dx;
+    r.dy = s->p.dy;
+    r.dz = s->p.dim == 3 ? s->p.dz : s->p.dx;
+    r.dtau = s->p.reinit_dtau;
+    r.beta = s->p.reinit_beta;
+    void* cur = s->G;
+    void* bufs[2] = {s->A, s->B};
+    for (int it = 0; it < s->p.reinit_iterations; ++it) {
+        r.phin = cur;
+        r.phinew = bufs[it & 1];
+        size_t ev = 0;
+        LSGB_TRY(timed_begin(s, 1, &ev));
+        if (s->prec == LSGB_PREC_F64) LSGB_CUDA(launch_reinit_f64(r, s->st));
+        else LSGB_CUDA(launch_reinit_f32(r, s->st));
+        LSGB_TRY(timed_end(s, ev));
+        cur = bufs[it & 1];
+    }
+    // the result becomes G; the old G and the other buffer are the scratch pair
+    void* old = s->G;
+    void* other = cur == s->A ? s->B : s->A;
+    s->G = cur;
+    s->A = old;
+    s->B = other;
+    return LSGB_OK;
+}
+
+int reduce_read(lsgb_solver* s, double* r2) {
+    LSGB_CUDA(cudaMemcpyAsync(s->h_res, s->scratch + 2 * (RED_BLOCKS + 1), 2 * sizeof(double),
+                              cudaMemcpyDeviceToHost, s->st));
+    LSGB_CUDA(cudaStreamSynchronize(s->st));
+    r2[0] = s->h_res[0];
+    r2[1] = s->h_res[1];
+    return LSGB_OK;
+}
+
+double* red_out(lsgb_solver* s) { return s->scratch + 2 * (RED_BLOCKS + 1); }
+
+int solver_ok(const lsgb_solver* s) {
+    if (!s) return fail(LSGB_ERR_INVALID, "solver is NULL");
+    return LSGB_OK;
+}
+
+}  // namespace
+
+extern "C" int lsgb_solver_create(const lsgb_params* p, int precision, lsgb_solver** out) {
+    LSGB_TRY(check_params(p));
+    if (!out) return fail(LSGB_ERR_INVALID, "out is NULL");
+    if (precision != LSGB_PREC_F64 && precision != LSGB_PREC_F32)
+        return fail(LSGB_ERR_INVALID, "unknown precision %d", precision);
+    lsgb_solver* s = new lsgb_solver();
+    s->p = *p;
+    if (s->p.dim == 2) { s->p.nz = 1; s->p.dz = s->p.dx; s->p.bc_z = LSGB_BC_PERIODIC; }
+    s->g = geo_of(s->p);
+    s->lay = compact_layout(s->g);
+    s->prec = precision;
+    s->esz = precision == LSGB_PREC_F64 ? sizeof(double) : sizeof(float);
+    int rc = LSGB_OK;
+    cudaError_t e = cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking);
+    if (e != cudaSuccess) { delete s; return fail(LSGB_ERR_CUDA, "stream creation: %s", cudaGetErrorString(e)); }
+    s->own_stream = true;
+    void** fields[6] = {&s->G, &s->A, &s->B, &s->u, &s->v, &s->w};
+    for (int q = 0; q < (s->p.dim == 3 ? 6 : 5) && rc == LSGB_OK; ++q) rc = alloc_field(s, fields[q]);
+    if (rc == LSGB_OK) {
+        e = cudaMalloc((void**)&s->scratch, reduce_scratch_bytes() + 2 * sizeof(double));
+        if (e != cudaSuccess) rc = fail(LSGB_ERR_ALLOC, "scratch: %s", cudaGetErrorString(e));
+    }
+    if (rc == LSGB_OK) {
+        e = cudaMallocHost((void**)&s->h_res, 2 * sizeof(double));
+        if (e != cudaSuccess) rc = fail(LSGB_ERR_ALLOC, "pinned result slots: %s", cudaGetErrorString(e));
+    }
+    if (rc != LSGB_OK) {
+        std::string keep = g_err;
+        lsgb_solver_destroy(s);
+        g_err = keep;
+        return rc;
+    }
+    *out = s;
+    return LSGB_OK;
+}
+
+extern "C" int lsgb_solver_destroy(lsgb_solver* s) {
+    if (!s) return LSGB_OK;
+    if (s->st) cudaStreamSynchronize(s->st);
+    void* ptrs[9] = {s->G, s->A, s->B, s->u, s->v, s->w, s->sl, s->stage64, s->scratch};
+    for (void* q : ptrs)
+        if (q) cudaFree(q);
+    if (s->h_res) cudaFreeHost(s->h_res);
+    for (cudaEvent_t e : s->ev_pool) cudaEventDestroy(e);
+    if (s->own_stream && s->st) cudaStreamDestroy(s->st);
+    delete s;
+    return LSGB_OK;
+}
+
+extern "C" int lsgb_solver_set_stream(lsgb_solver* s, void* stream) {
+    LSGB_TRY(solver_ok(s));
+    LSGB_CUDA(cudaStreamSynchronize(s->st));
+    if (s->own_stream) cudaStreamDestroy(s->st);
+    if (stream) {
+        s->st = (cudaStream_t)stream;
+        s->own_stream = false;
+    } else {
+        LSGB_CUDA(cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking));
+        s->own_stream = true;
+    }
+    return LSGB_OK;
+}
+
+extern "C" int lsgb_solver_get_params(const lsgb_solver* s, lsgb_params* p) {
+    LSGB_TRY(solver_ok(s));
+    if (!p) return fail(LSGB_ERR_INVALID, "p is NULL");
+    *p = s->p;
+    return LSGB_OK;
+}
+
+extern "C" int lsgb_solver_set_dt(lsgb_solver* s, double dt) {
+    LSGB_TRY(solver_ok(s));
+    if (!std::isfinite(dt) || dt < 0.0) return fail(LSGB_ERR_INVALID, "dt must be finite and >= 0");
+    s->p.dt = dt;
+    return LSGB_OK;
+}
+
+extern "C" int lsgb_solver_set_fields(lsgb_solver* s, const double* G, const double* u,
+                                      const double* v, const double* w, int layout, int memory) {
+    LSGB_TRY(solver_ok(s));
+    if (layout != LSGB_LAYOUT_GHOSTED && layout != LSGB_LAYOUT_COMPACT)
+        return fail(LSGB_ERR_INVALID, "unknown layout %d", layout);
+    if (memory != LSGB_MEM_HOST && memory != LSGB_MEM_DEVICE)
+        return fail(LSGB_ERR_INVALID, "unknown memory kind %d", memory);
+    if (G) { LSGB_TRY(load_field(s, s->G, G, layout, memory)); s->have_G = true; }
+    if (u) LSGB_TRY(load_field(s, s->u, u, layout, memory));
+    if (v) LSGB_TRY(load_field(s, s->v, v, layout, memory));
+    if (w && s->p.dim == 3) LSGB_TRY(load_field(s, s->w, w, layout, memory));
+    if (u && v && (w || s->p.dim == 2)) s->have_vel = true;
+    return LSGB_OK;
+}
+
+extern "C" int lsgb_solver_set_sl_field(lsgb_solver* s, const double* sl, int layout, int memory) {
+    LSGB_TRY(solver_ok(s));
+    if (!sl) {
+        if (s->sl) { LSGB_CUDA(cudaStreamSynchronize(s->st)); cudaFree(s->sl); s->sl = nullptr; }
+        return LSGB_OK;
+    }
+    if (!s->sl) LSGB_TRY(alloc_field(s, &s->sl));
+    return load_field(s, s->sl, sl, layout, memory);
+}
+
+extern "C" int lsgb_solver_get_G(lsgb_solver* s, double* G, int layout, int memory) {
+    LSGB_TRY(solver_ok(s));
+    if (!G) return fail(LSGB_ERR_INVALID, "G is NULL");
+    if (!s->have_G) return fail(LSGB_ERR_STATE, "G has not been set");
+    Lay dl = layout == LSGB_LAYOUT_GHOSTED ? ghosted_layout(s->g) : compact_layout(s->g);
+    size_t dbytes = sizeof(double) * (size_t)layout_elems(s->g, dl.ghosted);
+    double* ddst = G;
+    if (memory == LSGB_MEM_HOST) {
+        if (s->prec == LSGB_PREC_F64 && !dl.ghosted) {
+            LSGB_CUDA(cudaMemcpyAsync(G, s->G, dbytes, cudaMemcpyDeviceToHost, s->st));
+            LSGB_CUDA(cudaStreamSynchronize(s->st));
+            return LSGB_OK;
+        }
+        LSGB_TRY(ensure_stage(s));
+        ddst = s->stage64;
+    } else {
+        LSGB_TRY(check_dev(G, "G"));
+    }
+    if (s->prec == LSGB_PREC_F64) LSGB_CUDA(launch_unpack_f64(s->g, (const double*)s->G, ddst, dl, s->st));
+    else LSGB_CUDA(launch_unpack_f32(s->g, (const float*)s->G, ddst, dl, s->st));
+    if (memory == LSGB_MEM_HOST) {
+        LSGB_CUDA(cudaMemcpyAsync(G, ddst, dbytes, cudaMemcpyDeviceToHost, s->st));
+        LSGB_CUDA(cudaStreamSynchronize(s->st));
+    }
+    return LSGB_OK;
+}
+
+extern "C" int lsgb_solver_advance(lsgb_solver* s, int n_steps) {
+    LSGB_TRY(solver_ok(s));
+    if (n_steps < 0) return fail(LSGB_ERR_INVALID, "n_steps < 0");
+    if (!s->have_G || !s->have_vel) return fail(LSGB_ERR_STATE, "fields not set");
+    for (int q = 0; q < n_steps; ++q) {
+        LSGB_TRY(rk3_step(s));
+        if (s->p.enable_reinit && s->step > 0 && s->step % s->p.reinit_interval == 0)
+            LSGB_TRY(reinit(s));
+        s->step++;
+    }
+    return LSGB_OK;
+}
+
+extern "C" int lsgb_solver_reinit(lsgb_solver* s) {
+    LSGB_TRY(solver_ok(s));
+    if (!s->have_G) return fail(LSGB_ERR_STATE, "G has not been set");
+    return reinit(s);
+}
+
+extern "C" int lsgb_solver_get_step(const lsgb_solver* s, int* step) {
+    LSGB_TRY(solver_ok(s));
+    if (!step) return fail(LSGB_ERR_INVALID, "step is NULL");
+    *step = s->step;
+    return LSGB_OK;
+}
+
+extern "C" int lsgb_solver_set_step(lsgb_solver* s, int step) {
+    LSGB_TRY(solver_ok(s));
+    if (step < 0) return fail(LSGB_ERR_INVALID, "step < 0");
+    s->step = step;
+    return LSGB_OK;
+}
+
+extern "C" int lsgb_solver_volume(lsgb_solver* s, double* volume, int64_t* count) {
+    LSGB_TRY(solver_ok(s));
+    if (!s->have_G) return fail(LSGB_ERR_STATE, "G has not been set");
+    if (s->prec == LSGB_PREC_F64)
+        LSGB_CUDA(launch_count_negative<double>(s->g, s->lay, (const double*)s->G, s->scratch, red_out(s), s->st));
+    else
+        LSGB_CUDA(launch_count_negative<float>(s->g, s->lay, (const float*)s->G, s->scratch, red_out(s), s->st));
+    double r[2];
+    LSGB_TRY(reduce_read(s, r));
+    if (count) *count = (int64_t)r[0];
+    if (volume) *volume = r[0] * cell_volume(s->p);
+    return LSGB_OK;
+}
+
+extern "C" int lsgb_solver_max_speed(lsgb_solver* s, double* max_speed) {
+    LSGB_TRY(solver_ok(s));
+    if (!s->have_vel) return fail(LSGB_ERR_STATE, "velocity has not been set");
+    if (!max_speed) return fail(LSGB_ERR_INVALID, "max_speed is NULL");
+    if (s->prec == LSGB_PREC_F64)
+        LSGB_CUDA(launch_max_speed<double>(s->g, s->lay, (const double*)s->u, (const double*)s->v,
+                                           (const double*)s->w, s->scratch, red_out(s), s->st));
+    else
+        LSGB_CUDA(launch_max_speed<float>(s->g, s->lay, (const float*)s->u, (const float*)s->v,
+                                          (const float*)s->w, s->scratch, red_out(s), s->st));
+    double r[2];
+    LSGB_TRY(reduce_read(s, r));
+    *max_speed = r[0];
+    return LSGB_OK;
+}
+
+extern "C" int lsgb_solver_compute_dt(lsgb_solver* s, double cfl, double* dt) {
+    double ms;
+    LSGB_TRY(lsgb_solver_max_speed(s, &ms));
+    lsgb_params p = s->p;
+    p.cfl = cfl;
+    double d;
+    LSGB_TRY(lsgb_cfl_dt(&p, ms, &d));
+    s->p.cfl = cfl;
+    s->p.dt = d;
+    if (dt) *dt = d;
+    return LSGB_OK;
+}
+
+extern "C" int lsgb_solver_l2_error(lsgb_solver* s, const double* G_ref, int layout, int memory,
+                                    double* l2) {
+    LSGB_TRY(solver_ok(s));
+    if (!G_ref || !l2) return fail(LSGB_ERR_INVALID, "G_ref / l2 is NULL");
+    if (!s->have_G) return fail(LSGB_ERR_STATE, "G has not been set");
+    Lay rl = layout == LSGB_LAYOUT_GHOSTED ? ghosted_layout(s->g) : compact_layout(s->g);
+    const double* ref = G_ref;
+    if (memory == LSGB_MEM_HOST) {
+        LSGB_TRY(ensure_stage(s));
+        LSGB_CUDA(cudaMemcpyAsync(s->stage64, G_ref, sizeof(double) * (size_t)layout_elems(s->g, rl.ghosted),
+                                  cudaMemcpyHostToDevice, s->st));
+        ref = s->stage64;
+    } else {
+        LSGB_TRY(check_dev(G_ref, "G_ref"));
+    }
+    if (s->prec == LSGB_PREC_F64)
+        LSGB_CUDA(launch_sq_diff<double>(s->g, s->lay, (const double*)s->G, ref, rl, s->scratch, red_out(s), s->st));
+    else
+        LSGB_CUDA(launch_sq_diff<float>(s->g, s->lay, (const float*)s->G, ref, rl, s->scratch, red_out(s), s->st));
+    double r[2];
+    LSGB_TRY(reduce_read(s, r));
+    *l2 = std::sqrt(r[0] / (double)s->g.cells());
+    return LSGB_OK;
+}
+
+extern "C" int lsgb_solver_run_host(lsgb_solver* s, const double* G, const double* u,
+                                    const double* v, const double* w, int n_steps, double* G_out,
+                                    int layout) {
+    LSGB_TRY(solver_ok(s));
+    if (!G || !G_out) return fail(LSGB_ERR_INVALID, "G / G_out is NULL");
+    LSGB_TRY(lsgb_solver_set_fields(s, G, u, v, w, layout, LSGB_MEM_HOST));
+    LSGB_TRY(lsgb_solver_advance(s, n_steps));
+    LSGB_TRY(lsgb_solver_get_G(s, G_out, layout, LSGB_MEM_HOST));
+    return LSGB_OK;
+}
+
+extern "C" int lsgb_solver_synth(lsgb_solver* s, const lsgb_synth* d) {
+    LSGB_TRY(solver_ok(s));
+    if (!d) return fail(LSGB_ERR_INVALID, "descriptor is NULL");
+    if (d->n_shape_modes < 0 || d->n_shape_modes > LSGB_MAX_MODES || d->n_vel_modes < 0 ||
+        d->n_vel_modes > LSGB_MAX_MODES)
+        return fail(LSGB_ERR_INVALID, "mode counts must lie in [0, %d]", LSGB_MAX_MODES);
+    for (int m = 0; m < d->n_shape_modes; ++m)
+        if (d->shape_l[m] < 0 || d->shape_l[m] > 4 || d->shape_m[m] > d->shape_l[m] || -d->shape_m[m] > d->shape_l[m])
+            return fail(LSGB_ERR_INVALID, "shape mode %d: need 0 <= |m| <= l <= 4", m);
+    const long long n = s->g.cells();
+    double* tmp[4] = {nullptr, nullptr, nullptr, nullptr};
+    const bool direct = s->prec == LSGB_PREC_F64;
+    if (direct) {
+        tmp[0] = (double*)s->G; tmp[1] = (double*)s->u; tmp[2] = (double*)s->v;
+        tmp[3] = s->p.dim == 3 ? (double*)s->w : nullptr;
+    } else {
+        for (int q = 0; q < (s->p.dim == 3 ? 4 : 3); ++q) {
+            cudaError_t e = cudaMallocAsync((void**)&tmp[q], sizeof(double) * (size_t)n, s->st);
+            if (e != cudaSuccess) {
+                for (int r = 0; r < q; ++r) cudaFreeAsync(tmp[r], s->st);
+                return fail(LSGB_ERR_ALLOC, "synth temporaries: %s", cudaGetErrorString(e));
+            }
+        }
+    }
+    int rc = LSGB_OK;
+    Lay cl = compact_layout(s->g);
+    double dz = s->p.dim == 3 ? s->p.dz : s->p.dx;
+    cudaError_t e = launch_synth(s->g, *d, s->p.dx, s->p.dy, dz, tmp[0], tmp[1], tmp[2], tmp[3], s->st);
+    if (e != cudaSuccess) rc = fail(LSGB_ERR_CUDA, "synth kernel: %s", cudaGetErrorString(e));
+    if (rc == LSGB_OK && d->vel_scale <= 0.0) {
+        // normalise to max |u|_2 = 1
+        e = launch_max_speed<double>(s->g, cl, tmp[1], tmp[2], tmp[3], s->scratch, red_out(s), s->st);
+        double r[2] = {0, 0};
+        if (e == cudaSuccess) rc = reduce_read(s, r);
+        else rc = fail(LSGB_ERR_CUDA, "synth normalisation: %s", cudaGetErrorString(e));
+        if (rc == LSGB_OK && r[1] > 0.0) {
+            e = launch_scale3(n, 1.0 / r[1], tmp[1], tmp[2], tmp[3], s->st);
+            if (e != cudaSuccess) rc = fail(LSGB_ERR_CUDA, "synth scale: %s", cudaGetErrorString(e));
+        }
+    }
+    if (!direct) {
+        void* dst[4] = {s->G, s->u, s->v, s->w};
+        for (int q = 0; q < (s->p.dim == 3 ? 4 : 3) && rc == LSGB_OK; ++q) {
+            e = launch_pack_f32(s->g, tmp[q], cl, (float*)dst[q], s->st);
+            if (e != cudaSuccess) rc = fail(LSGB_ERR_CUDA, "synth convert: %s", cudaGetErrorString(e));
+        }
+        for (int q = 0; q < 4; ++q)
+            if (tmp[q]) cudaFreeAsync(tmp[q], s->st);
+    }
+    if (rc == LSGB_OK) { s->have_G = true; s->have_vel = true; }
+    return rc;
+}
+
+extern "C" int lsgb_solver_set_velocity_deformation(lsgb_solver* s, double t, double T) {
+    LSGB_TRY(solver_ok(s));
+    if (s->p.dim != 3) return fail(LSGB_ERR_INVALID, "the deformation vortex is a 3D field");
+    if (!std::isfinite(t) || !std::isfinite(T) || T == 0.0) return fail(LSGB_ERR_INVALID, "bad t / T");
+    LSGB_CUDA(launch_deformation(s->g, s->p.dx, s->p.dy, s->p.dz, t, T, s->u, s->v, s->w,
+                                 s->prec == LSGB_PREC_F32, s->st));
+    s->have_vel = true;
+    return LSGB_OK;
+}
+
+extern "C" int lsgb_solver_get_field(lsgb_solver* s, int which, double* out, int layout, int memory) {
+    LSGB_TRY(solver_ok(s));
+    if (which == LSGB_FIELD_G) return lsgb_solver_get_G(s, out, layout, memory);
+    void* f = which == LSGB_FIELD_U ? s->u : which == LSGB_FIELD_V ? s->v
+            : which == LSGB_FIELD_W ? (s->p.dim == 3 ? s->w : nullptr)
+            : which == LSGB_FIELD_SL ? s->sl : nullptr;
+    if (!f) return fail(LSGB_ERR_INVALID, "field %d is not resident", which);
+    if (!out) return fail(LSGB_ERR_INVALID, "out is NULL");
+    void* keep = s->G;
+    bool had = s->have_G;
+    s->G = f;
+    s->have_G = true;
+    int rc = lsgb_solver_get_G(s, out, layout, memory);
+    s->G = keep;
+    s->have_G = had;
+    return rc;
+}
+
+extern "C" int lsgb_solver_enable_timing(lsgb_solver* s, int enable) {
+    LSGB_TRY(solver_ok(s));
+    LSGB_CUDA(cudaStreamSynchronize(s->st));
+    s->timing = enable != 0;
+    s->ev_used = 0;
+    s->ev_marks.clear();
+    return LSGB_OK;
+}
+
+extern "C" int lsgb_solver_kernel_times(lsgb_solver* s, double* stage_ms, int64_t* stage_launches,
+                                        double* reinit_ms, int64_t* reinit_launches) {
+    LSGB_TRY(solver_ok(s));
+    LSGB_CUDA(cudaStreamSynchronize(s->st));
+    double t[2] = {0.0, 0.0};
+    int64_t c[2] = {0, 0};
+    for (const auto& m : s->ev_marks) {
+        float ms = 0.0f;
+        LSGB_CUDA(cudaEventElapsedTime(&ms, s->ev_pool[m.first], s->ev_pool[m.first + 1]));
+        t[m.second] += ms;
+        c[m.second] += 1;
+    }
+    if (stage_ms) *stage_ms = t[0];
+    if (stage_launches) *stage_launches = c[0];
+    if (reinit_ms) *reinit_ms = t[1];
+    if (reinit_launches) *reinit_launches = c[1];
+    return LSGB_OK;
+}

@@ -1,0 +1,158 @@
+// common.cuh -- shared declarations of the GB300 level-set library.
+//
+// Geometry, array layouts and the internal launch interface between the
+// translation units:
+//   f64_kernels.cu  FP64 kernels in the reference's exact operation order
+//                   (compiled with --fmad=false)
+//   f32_kernels.cu  FP32-bulk kernels (tiled, fast math) with the FP64 HCR-2
+//                   interface constraint
+//   reduce.cu       deterministic two-pass reductions (volume, L2, max speed)
+//   synth.cu        on-device synthetic benchmark fields
+//   api.cu          the C ABI (include/lsgb.h), solver handle, CUDA graphs
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstdio>
+
+#include "../../include/lsgb.h"
+
+namespace lsgb {
+
+constexpr int NG = 3;  // ghost cells per side (reference config.h:31)
+
+// Interior grid and boundary codes.
+struct Geo {
+    int dim;
+    int nx, ny, nz;        // nz == 1 in 2D
+    int bcx, bcy, bcz;     // LSGB_BC_*
+    __host__ __device__ long long cells() const { return (long long)nx * ny * nz; }
+};
+
+// Storage of one field: element (i, j, k) of the interior lives at
+// off + i + j * sy + k * sz.  Ghosted arrays (the reference layout) have
+// off = 3 + 3 sy + 3 sz; compact arrays off = 0.
+struct Lay {
+    long long off, sy, sz;
+    int ghosted;
+};
+
+inline Lay ghosted_layout(const Geo& g) {
+    Lay l;
+    long long nxT = g.nx + 2 * NG, nyT = g.ny + 2 * NG;
+    l.sy = nxT;
+    l.sz = g.dim == 3 ? nxT * nyT : 0;
+    l.off = NG + NG * l.sy + (g.dim == 3 ? NG * l.sz : 0);
+    l.ghosted = 1;
+    return l;
+}
+
+inline Lay compact_layout(const Geo& g) {
+    Lay l;
+    l.sy = g.nx;
+    l.sz = g.dim == 3 ? (long long)g.nx * g.ny : 0;
+    l.off = 0;
+    l.ghosted = 0;
+    return l;
+}
+
+inline long long layout_elems(const Geo& g, int ghosted) {
+    if (ghosted)
+        return (long long)(g.nx + 2 * NG) * (g.ny + 2 * NG) * (g.dim == 3 ? g.nz + 2 * NG : 1);
+    return g.cells();
+}
+
+// Periodic wrap / zero-gradient clamp of an interior coordinate that is at
+// most 3 cells outside [0, n).  Periodic needs n >= 3 (checked at set-up).
+__host__ __device__ __forceinline__ int map_axis(int i, int n, int bc) {
+    if (bc == LSGB_BC_PERIODIC) return i < 0 ? i + n : (i >= n ? i - n : i);
+    return i < 0 ? 0 : (i >= n ? n - 1 : i);
+}
+
+// Physics / step coefficients handed to the stage kernels.
+struct StageArgs {
+    Geo g;
+    Lay lay;                 // layout of G fields and velocity
+    const void* Gin;         // field the RHS is evaluated on
+    const void* Gn;          // field at the start of the RK3 step
+    void* Gout;
+    const void* u;
+    const void* v;
+    const void* w;
+    const void* sl;          // nullable per-cell flame speed (same layout)
+    double s_l, eps, dx, dy, dz, dt;
+    int stage;               // 1, 2, 3
+};
+
+// HCR-2 pseudo-step arguments (handle path: r~ and flags recomputed from phi0).
+struct ReinitArgs {
+    Geo g;
+    Lay lay;
+    const void* phin;
+    const void* phi0;
+    void* phinew;
+    double dx, dy, dz, dtau, beta;
+};
+
+// Drop-in (ghosted, FP64) reinit pieces with stored r~ and flags.
+cudaError_t launch_crossings_f64(const Geo& g, const Lay& lay, const double* phi0,
+                                 double* rt, int32_t* flag, cudaStream_t st);
+cudaError_t launch_reinit_step_stored_f64(const Geo& g, const Lay& lay, const double* phin,
+                                          double* phinew, const double* phi0, const double* rt,
+                                          const int32_t* flag, double dx, double dy, double dz,
+                                          double dtau, double beta, cudaStream_t st);
+
+cudaError_t launch_stage_f64(const StageArgs& a, cudaStream_t st);
+cudaError_t launch_stage_f32(const StageArgs& a, cudaStream_t st);
+cudaError_t launch_reinit_f64(const ReinitArgs& a, cudaStream_t st);
+cudaError_t launch_reinit_f32(const ReinitArgs& a, cudaStream_t st);
+
+// Ghost fill of a ghosted FP64 array from its interior (periodic images /
+// zero-gradient copies), the state the reference's boundary fill leaves.
+cudaError_t launch_bc_fill_f64(const Geo& g, double* G, cudaStream_t st);
+
+// Layout / precision conversion between an FP64 array (src layout) and a
+// compact T array; to_ghosted also fills the ghosts.
+cudaError_t launch_pack_f64(const Geo& g, const double* src, const Lay& src_lay, double* dst,
+                            cudaStream_t st);
+cudaError_t launch_pack_f32(const Geo& g, const double* src, const Lay& src_lay, float* dst,
+                            cudaStream_t st);
+cudaError_t launch_unpack_f64(const Geo& g, const double* src, double* dst, const Lay& dst_lay,
+                              cudaStream_t st);
+cudaError_t launch_unpack_f32(const Geo& g, const float* src, double* dst, const Lay& dst_lay,
+                              cudaStream_t st);
+
+// Reductions.  `partials` is scratch of at least reduce_scratch_bytes();
+// results land in device memory `out` (host reads them after a sync).
+constexpr int RED_BLOCKS = 1024;
+constexpr int RED_THREADS = 256;
+inline size_t reduce_scratch_bytes() { return sizeof(double) * 2 * (RED_BLOCKS + 1); }
+
+// out[0] = count of interior cells with G < 0 (as double, exact below 2^53)
+template <typename T>
+cudaError_t launch_count_negative(const Geo& g, const Lay& lay, const T* G, double* partials,
+                                  double* out, cudaStream_t st);
+// out[0] = sum over interior of (G - Gref)^2 in FP64 (Gref FP64, its own layout)
+template <typename T>
+cudaError_t launch_sq_diff(const Geo& g, const Lay& lay, const T* G, const double* Gref,
+                           const Lay& ref_lay, double* partials, double* out, cudaStream_t st);
+// out[0] = max over interior of |u|+|v|(+|w|); out[1] = max of sqrt(u^2+v^2+w^2)
+template <typename T>
+cudaError_t launch_max_speed(const Geo& g, const Lay& lay, const T* u, const T* v, const T* w,
+                             double* partials, double* out, cudaStream_t st);
+// out[0] = 1 if any interior G is not finite
+template <typename T>
+cudaError_t launch_nonfinite(const Geo& g, const Lay& lay, const T* G, double* partials,
+                             double* out, cudaStream_t st);
+
+// Synthetic fields: writes FP64 compact arrays G, u, v, w (w ignored in 2D).
+cudaError_t launch_synth(const Geo& g, const lsgb_synth& d, double dx, double dy, double dz,
+                         double* G, double* u, double* v, double* w, cudaStream_t st);
+cudaError_t launch_deformation(const Geo& g, double dx, double dy, double dz, double t, double Tp,
+                               void* u, void* v, void* w, bool f32, cudaStream_t st);
+cudaError_t launch_scale3(long long n, double s, double* u, double* v, double* w, cudaStream_t st);
+
+// Bookkeeping of kernel launches (lsgb_launch_count).
+void count_launches(uint64_t n);
+
+}  // namespace lsgb

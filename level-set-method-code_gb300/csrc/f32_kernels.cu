@@ -1,0 +1,267 @@
+// f32_kernels.cu -- FP32-bulk form of the hot path.
+//
+// Same scheme as the reference (Local_code/level-set_MPI_3D/include/weno5.h,
+// rk3.h, reinitialization.h): u_eff WENO-5 upwinding, TVD RK3, HCR-2.  The
+// WENO/RK3/reinit arithmetic runs in FP32 with fused multiply-adds and one
+// approximate reciprocal per reconstruction; the HCR-2 interface constraint
+// (r~ = phi0 / sum phi0_nb and the forcing beta (r~ sum phi - phi) / dx, the
+// sub-cell position of G = 0) is evaluated in FP64 on the flagged cells.
+// Accuracy against the FP64 path is measured, not assumed (bench.py
+// --precision-report and tests/test_gpu_precision.py).
+//
+// WENO-5 in mirrored form: with sgn = (u_eff >= 0), the 7 samples G[i-3..i+3]
+// are read as w[m] = G[i-3+m] (sgn) or G[i+3-m] (!sgn).  Both the left-biased
+// pair of weno5_left (weno5.h:39-58) and the right-biased pair of weno5_right
+// (weno5.h:60-81) are then X = R(w0..w4) and Y = R(w1..w5) of one formula,
+// with the optimal weights (0.1, 0.6, 0.3) for sgn and the reference's
+// (0.3, 0.6, 0.1) otherwise; the derivative is +-(Y - X)/h.  The smoothness
+// indicators of the four triples centred at w1..w4 are shared by X and Y.
+#include "common.cuh"
+
+namespace lsgb {
+namespace {
+
+constexpr float F_WENO_EPS = 1.0e-6f;
+
+// WENO reconstruction from the 5-point window (a..e) with the squared
+// regularised indicators q0..q2 of its three sub-stencils.  Division-free
+// weights: omega_k ~ d_k / q_k, so with Q_k = prod_{j != k} q_j the value is
+// sum d_k Q_k P_k / sum d_k Q_k.  P_k carry a factor 6 that the denominator
+// removes.
+__device__ __forceinline__ float recon(float a, float b, float c, float d, float e,
+                                       float q0, float q1, float q2, float q01, float q02,
+                                       float q12, float d0, float d2) {
+    const float P0 = fmaf(2.0f, a, fmaf(-7.0f, b, 11.0f * c));
+    const float P1 = fmaf(-1.0f, b, fmaf(5.0f, c, 2.0f * d));
+    const float P2 = fmaf(2.0f, c, fmaf(5.0f, d, -e));
+    const float w0 = d0 * q12, w1 = 0.6f * q02, w2 = d2 * q01;
+    const float num = fmaf(w0, P0, fmaf(w1, P1, w2 * P2));
+    const float den = 6.0f * (w0 + w1 + w2);
+    return __fdividef(num, den);
+}
+
+__device__ __forceinline__ float qbeta(float a, float b, float c) {
+    const float t = fmaf(-2.0f, b, a) + c;
+    const float r = c - a;
+    const float B = fmaf(13.0f / 12.0f * t, t, 0.25f * r * r);
+    const float s = F_WENO_EPS + B;
+    return s * s;
+}
+
+// Upwind WENO-5 derivative from s[0..6] = G[i-3..i+3], times 1/h.
+__device__ __forceinline__ float weno_deriv_f32(const float* s, float vel, float inv_h) {
+    const bool p = vel >= 0.0f;
+    float w[6];
+#pragma unroll
+    for (int m = 0; m < 6; ++m) w[m] = p ? s[m] : s[6 - m];
+    const float Q1 = qbeta(w[0], w[1], w[2]);
+    const float Q2 = qbeta(w[1], w[2], w[3]);
+    const float Q3 = qbeta(w[2], w[3], w[4]);
+    const float Q4 = qbeta(w[3], w[4], w[5]);
+    const float Q23 = Q2 * Q3;
+    const float d0 = p ? 0.1f : 0.3f;
+    const float d2 = p ? 0.3f : 0.1f;
+    const float X = recon(w[0], w[1], w[2], w[3], w[4], Q1, Q2, Q3, Q1 * Q2, Q1 * Q3, Q23, d0, d2);
+    const float Y = recon(w[1], w[2], w[3], w[4], w[5], Q2, Q3, Q4, Q23, Q2 * Q4, Q3 * Q4, d0, d2);
+    const float diff = Y - X;
+    return (p ? diff : -diff) * inv_h;
+}
+
+struct F32Coef {
+    float inv_dx, inv_dy, inv_dz, inv_2dx, inv_2dy, inv_2dz, s_l, eps, dt;
+};
+
+// Fused RK3 stage on compact FP32 arrays, one thread per cell, periodic or
+// zero-gradient index mapping at the domain edges.
+template <int DIM, int STAGE>
+__global__ void __launch_bounds__(256) stage_f32_kernel(Geo g, const float* __restrict__ Gin,
+                                                        const float* __restrict__ Gn,
+                                                        float* __restrict__ Gout,
+                                                        const float* __restrict__ u,
+                                                        const float* __restrict__ v,
+                                                        const float* __restrict__ w,
+                                                        const float* __restrict__ sl, F32Coef c) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int j = blockIdx.y * blockDim.y + threadIdx.y;
+    int k = DIM == 3 ? blockIdx.z * blockDim.z + threadIdx.z : 0;
+    if (i >= g.nx || j >= g.ny || k >= g.nz) return;
+    const long long sy = g.nx;
+    const long long sz = (long long)g.nx * g.ny;
+    const long long row = j * sy + k * sz;
+    const long long id = row + i;
+
+    float sx[7], syv[7], szv[7];
+#pragma unroll
+    for (int d = -3; d <= 3; ++d) {
+        sx[d + 3] = __ldg(Gin + row + map_axis(i + d, g.nx, g.bcx));
+        syv[d + 3] = __ldg(Gin + (long long)map_axis(j + d, g.ny, g.bcy) * sy + k * sz + i);
+        if (DIM == 3) szv[d + 3] = __ldg(Gin + (long long)map_axis(k + d, g.nz, g.bcz) * sz + j * sy + i);
+    }
+    const float s_l = sl ? __ldg(sl + id) : c.s_l;
+    float ue = __ldg(u + id), ve = __ldg(v + id), we = 0.0f;
+    if (DIM == 3) we = __ldg(w + id);
+    if (s_l > c.eps) {
+        const float gx = (sx[4] - sx[2]) * c.inv_2dx;
+        const float gy = (syv[4] - syv[2]) * c.inv_2dy;
+        float sq = fmaf(gx, gx, fmaf(gy, gy, c.eps));
+        float gz = 0.0f;
+        if (DIM == 3) { gz = (szv[4] - szv[2]) * c.inv_2dz; sq = fmaf(gz, gz, sq); }
+        const float f = s_l * rsqrtf(sq);
+        ue = fmaf(-f, gx, ue);
+        ve = fmaf(-f, gy, ve);
+        if (DIM == 3) we = fmaf(-f, gz, we);
+    }
+    float rhs = ue * weno_deriv_f32(sx, ue, c.inv_dx);
+    rhs = fmaf(ve, weno_deriv_f32(syv, ve, c.inv_dy), rhs);
+    if (DIM == 3) rhs = fmaf(we, weno_deriv_f32(szv, we, c.inv_dz), rhs);
+    rhs = -rhs;
+
+    float out;
+    if (STAGE == 1) {
+        out = fmaf(c.dt, rhs, sx[3]);
+    } else if (STAGE == 2) {
+        const float gn = __ldg(Gn + id);
+        out = fmaf(0.25f * c.dt, rhs, fmaf(0.75f, gn, 0.25f * sx[3]));
+    } else {
+        const float gn = __ldg(Gn + id);
+        out = fmaf((2.0f / 3.0f) * c.dt, rhs, fmaf(1.0f / 3.0f, gn, (2.0f / 3.0f) * sx[3]));
+    }
+    Gout[id] = out;
+}
+
+// One HCR-2 pseudo-step (reinitStep3D, reinitialization.h:136-193) in FP32
+// with the interface constraint in FP64: the crossing flags and
+// r~ = phi0_c / sum(phi0 of crossing neighbours) (computeInterfaceCrossings3D,
+// :46-89) are recomputed from phi0 in FP64, and on flagged cells the forcing
+// and the update are formed in FP64 before the final rounding.
+template <int DIM>
+__global__ void __launch_bounds__(256) reinit_f32_kernel(Geo g, const float* __restrict__ phin,
+                                                         const float* __restrict__ phi0,
+                                                         float* __restrict__ phinew, float inv_dx,
+                                                         float inv_dy, float inv_dz, float dx2,
+                                                         float dtau_f, double dx, double dtau,
+                                                         double beta) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int j = blockIdx.y * blockDim.y + threadIdx.y;
+    int k = DIM == 3 ? blockIdx.z * blockDim.z + threadIdx.z : 0;
+    if (i >= g.nx || j >= g.ny || k >= g.nz) return;
+    const long long sy = g.nx;
+    const long long sz = (long long)g.nx * g.ny;
+    const long long id = j * sy + k * sz + i;
+    long long nb[6];
+    nb[0] = j * sy + k * sz + map_axis(i - 1, g.nx, g.bcx);
+    nb[1] = j * sy + k * sz + map_axis(i + 1, g.nx, g.bcx);
+    nb[2] = (long long)map_axis(j - 1, g.ny, g.bcy) * sy + k * sz + i;
+    nb[3] = (long long)map_axis(j + 1, g.ny, g.bcy) * sy + k * sz + i;
+    if (DIM == 3) {
+        nb[4] = (long long)map_axis(k - 1, g.nz, g.bcz) * sz + j * sy + i;
+        nb[5] = (long long)map_axis(k + 1, g.nz, g.bcz) * sz + j * sy + i;
+    }
+    const float phi = __ldg(phin + id);
+    const float ph0 = __ldg(phi0 + id);
+    float pn[6], p0[6];
+#pragma unroll
+    for (int q = 0; q < 2 * DIM; ++q) {
+        pn[q] = __ldg(phin + nb[q]);
+        p0[q] = __ldg(phi0 + nb[q]);
+    }
+    const float S = ph0 * rsqrtf(fmaf(ph0, ph0, dx2));
+    const bool pos = S > 0.0f;
+    float gsq = 0.0f;
+    const float inv[3] = {inv_dx, inv_dy, inv_dz};
+#pragma unroll
+    for (int ax = 0; ax < DIM; ++ax) {
+        const float dm = (phi - pn[2 * ax]) * inv[ax];
+        const float dp = (pn[2 * ax + 1] - phi) * inv[ax];
+        const float a = pos ? fmaxf(dm, 0.0f) : fminf(dm, 0.0f);
+        const float b = pos ? fminf(dp, 0.0f) : fmaxf(dp, 0.0f);
+        gsq += fmaxf(a * a, b * b);
+    }
+    const float term = -S * (sqrtf(gsq) - 1.0f);
+
+    // interface constraint, FP64
+    int flag = 0;
+    double sum0 = 0.0;
+    int cnt = 0;
+#pragma unroll
+    for (int q = 0; q < 2 * DIM; ++q) {
+        if ((double)ph0 * (double)p0[q] < 0.0) { sum0 += (double)p0[q]; cnt++; flag |= 1 << q; }
+    }
+    float out;
+    bool forced = false;
+    double outd = 0.0;
+    if (flag != 0) {
+        bool stable = (phi > 0.0f) == (ph0 > 0.0f);
+#pragma unroll
+        for (int q = 0; q < 2 * DIM; ++q)
+            if ((flag >> q) & 1) stable = stable && ((pn[q] > 0.0f) == (p0[q] > 0.0f));
+        if (stable) {
+            const double rt = (cnt > 0 && fabs(sum0) > 1e-15) ? (double)ph0 / sum0 : 0.0;
+            double sum = 0.0;
+#pragma unroll
+            for (int q = 0; q < 2 * DIM; ++q)
+                if ((flag >> q) & 1) sum += (double)pn[q];
+            const double forcing = beta * (rt * sum - (double)phi) / dx;
+            outd = (double)phi + dtau * ((double)term + forcing);
+            forced = true;
+        }
+    }
+    out = forced ? (float)outd : fmaf(dtau_f, term, phi);
+    phinew[id] = out;
+}
+
+inline dim3 cell_block(const Geo& g) { return g.dim == 3 ? dim3(32, 4, 2) : dim3(32, 8, 1); }
+inline dim3 cell_grid(const Geo& g, dim3 b) {
+    return dim3((g.nx + b.x - 1) / b.x, (g.ny + b.y - 1) / b.y, (g.nz + b.z - 1) / b.z);
+}
+
+}  // namespace
+
+cudaError_t launch_stage_f32(const StageArgs& a, cudaStream_t st) {
+    if (a.lay.ghosted) return cudaErrorInvalidValue;  // FP32 fields are compact only
+    F32Coef c;
+    c.inv_dx = (float)(1.0 / a.dx);
+    c.inv_dy = (float)(1.0 / a.dy);
+    c.inv_dz = (float)(1.0 / a.dz);
+    c.inv_2dx = (float)(1.0 / (2.0 * a.dx));
+    c.inv_2dy = (float)(1.0 / (2.0 * a.dy));
+    c.inv_2dz = (float)(1.0 / (2.0 * a.dz));
+    c.s_l = (float)a.s_l;
+    c.eps = (float)a.eps;
+    c.dt = (float)a.dt;
+    dim3 b = cell_block(a.g), gr = cell_grid(a.g, b);
+    const float* Gin = (const float*)a.Gin;
+    const float* Gn = (const float*)a.Gn;
+    float* Gout = (float*)a.Gout;
+    const float* u = (const float*)a.u;
+    const float* v = (const float*)a.v;
+    const float* w = (const float*)a.w;
+    const float* sl = (const float*)a.sl;
+#define LSGB_S32(D, S) stage_f32_kernel<D, S><<<gr, b, 0, st>>>(a.g, Gin, Gn, Gout, u, v, w, sl, c)
+    if (a.g.dim == 3) {
+        if (a.stage == 1) LSGB_S32(3, 1); else if (a.stage == 2) LSGB_S32(3, 2); else LSGB_S32(3, 3);
+    } else {
+        if (a.stage == 1) LSGB_S32(2, 1); else if (a.stage == 2) LSGB_S32(2, 2); else LSGB_S32(2, 3);
+    }
+#undef LSGB_S32
+    count_launches(1);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_reinit_f32(const ReinitArgs& a, cudaStream_t st) {
+    if (a.lay.ghosted) return cudaErrorInvalidValue;
+    dim3 b = cell_block(a.g), gr = cell_grid(a.g, b);
+    const float* pn = (const float*)a.phin;
+    const float* p0 = (const float*)a.phi0;
+    float* out = (float*)a.phinew;
+    const float ix = (float)(1.0 / a.dx), iy = (float)(1.0 / a.dy), iz = (float)(1.0 / a.dz);
+    const float dx2 = (float)(a.dx * a.dx);
+    if (a.g.dim == 3)
+        reinit_f32_kernel<3><<<gr, b, 0, st>>>(a.g, pn, p0, out, ix, iy, iz, dx2, (float)a.dtau, a.dx, a.dtau, a.beta);
+    else
+        reinit_f32_kernel<2><<<gr, b, 0, st>>>(a.g, pn, p0, out, ix, iy, iz, dx2, (float)a.dtau, a.dx, a.dtau, a.beta);
+    count_launches(1);
+    return cudaGetLastError();
+}
+
+}  // namespace lsgb

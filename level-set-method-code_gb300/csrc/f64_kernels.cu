@@ -1,0 +1,454 @@
+// f64_kernels.cu -- FP64 kernels that reproduce the reference's arithmetic.
+//
+// Compiled with --fmad=false: every a*b+c below stays a rounded multiply and a
+// rounded add, divisions and sqrt are IEEE round-to-nearest, and expressions
+// keep the reference's evaluation order.  With the same inputs the results
+// are bit-identical to the reference CPU solver
+// (Local_code/level-set_MPI_3D/include/{weno5,rk3,reinitialization}.h and the
+// 2D twins), which tests/test_gpu_parity.py checks.
+//
+// Kernel shapes: one thread per interior cell (blocks of 32 x 4 x 2 in 3D,
+// 32 x 8 in 2D).  FP64 on GB300 runs far below the HBM roof (the step is
+// bound by the FP64 pipe, ~60 divisions per cell and stage), so these kernels
+// favour exactness and simple addressing; the throughput path is the FP32 form
+// in f32_kernels.cu.
+#include "common.cuh"
+
+namespace lsgb {
+namespace {
+
+constexpr double WENO_EPS = 1.0e-6;  // weno5.h:22
+
+// Smoothness indicator of the triple (a, b, c) = (v[k], v[k+1], v[k+2]),
+// computeSmoothnessIndicators, weno5.h:28-37 (non-standard second term).
+__device__ __forceinline__ double sm_beta(double a, double b, double c) {
+    double d2 = c - 2.0 * b + a;
+    return (13.0 / 12.0) * d2 * d2 + 0.25 * (c - a) * (c - a);
+}
+
+// weno5_left, weno5.h:39-58: value at i+1/2 from G[i-2..i+2].
+__device__ __forceinline__ double weno_left(double v0, double v1, double v2, double v3, double v4) {
+    double b0 = sm_beta(v0, v1, v2);
+    double b1 = sm_beta(v1, v2, v3);
+    double b2 = sm_beta(v2, v3, v4);
+    double a0 = 0.1 / ((WENO_EPS + b0) * (WENO_EPS + b0));
+    double a1 = 0.6 / ((WENO_EPS + b1) * (WENO_EPS + b1));
+    double a2 = 0.3 / ((WENO_EPS + b2) * (WENO_EPS + b2));
+    double s = a0 + a1 + a2;
+    double w0 = a0 / s, w1 = a1 / s, w2 = a2 / s;
+    double p0 = (2.0 * v0 - 7.0 * v1 + 11.0 * v2) / 6.0;
+    double p1 = (-v1 + 5.0 * v2 + 2.0 * v3) / 6.0;
+    double p2 = (2.0 * v2 + 5.0 * v3 - v4) / 6.0;
+    return w0 * p0 + w1 * p1 + w2 * p2;
+}
+
+// weno5_right, weno5.h:60-81: value at i-1/2 from G[i-2..i+2]; indicators
+// on the mirrored stencil.
+__device__ __forceinline__ double weno_right(double v0, double v1, double v2, double v3, double v4) {
+    double b0 = sm_beta(v4, v3, v2);
+    double b1 = sm_beta(v3, v2, v1);
+    double b2 = sm_beta(v2, v1, v0);
+    double a0 = 0.3 / ((WENO_EPS + b0) * (WENO_EPS + b0));
+    double a1 = 0.6 / ((WENO_EPS + b1) * (WENO_EPS + b1));
+    double a2 = 0.1 / ((WENO_EPS + b2) * (WENO_EPS + b2));
+    double s = a0 + a1 + a2;
+    double w0 = a0 / s, w1 = a1 / s, w2 = a2 / s;
+    double p0 = (11.0 * v2 - 7.0 * v3 + 2.0 * v4) / 6.0;
+    double p1 = (2.0 * v1 + 5.0 * v2 - v3) / 6.0;
+    double p2 = (-v0 + 5.0 * v1 + 2.0 * v2) / 6.0;
+    return w0 * p0 + w1 * p1 + w2 * p2;
+}
+
+// weno5_dx_3d / _dy_3d / _dz_3d (weno5.h:90-196): s[0..6] = G[i-3..i+3]
+// along the axis; branch on vel >= 0 (weno5.h:99).
+__device__ __forceinline__ double weno_deriv(const double* s, double vel, double h) {
+    double gl, gr;
+    if (vel >= 0.0) {
+        gl = weno_left(s[0], s[1], s[2], s[3], s[4]);
+        gr = weno_left(s[1], s[2], s[3], s[4], s[5]);
+    } else {
+        gl = weno_right(s[1], s[2], s[3], s[4], s[5]);
+        gr = weno_right(s[2], s[3], s[4], s[5], s[6]);
+    }
+    return (gr - gl) / h;
+}
+
+// Stencil reader: element offset of interior coordinate (i + d) etc.  In the
+// ghosted layout the neighbours are read from the ghost cells the caller's
+// boundary fill left (as the reference does); in the compact layout the
+// coordinates wrap / clamp.
+template <bool GH>
+struct Nb {
+    long long sy, sz;
+    int i, j, k, nx, ny, nz, bcx, bcy, bcz;
+    long long row;  // j*sy + k*sz of the centre
+
+    __device__ __forceinline__ long long c() const { return row + i; }
+    __device__ __forceinline__ long long x(int d) const {
+        return GH ? row + i + d : row + map_axis(i + d, nx, bcx);
+    }
+    __device__ __forceinline__ long long y(int d) const {
+        return GH ? row + i + d * sy : (long long)map_axis(j + d, ny, bcy) * sy + (long long)k * sz + i;
+    }
+    __device__ __forceinline__ long long z(int d) const {
+        return GH ? row + i + d * sz : (long long)map_axis(k + d, nz, bcz) * sz + (long long)j * sy + i;
+    }
+};
+
+template <bool GH>
+__device__ __forceinline__ Nb<GH> make_nb(const Geo& g, const Lay& lay, int i, int j, int k) {
+    Nb<GH> n;
+    n.sy = lay.sy; n.sz = lay.sz;
+    n.i = i; n.j = j; n.k = k;
+    n.nx = g.nx; n.ny = g.ny; n.nz = g.nz;
+    n.bcx = g.bcx; n.bcy = g.bcy; n.bcz = g.bcz;
+    n.row = (long long)j * lay.sy + (long long)k * lay.sz;
+    return n;
+}
+
+// Fused RK3 stage: rhs of computeRHS3D (rk3.h:31-81) / computeRHS (2D
+// rk3.h:54-98) at the cell, combined as rk3Stage{1,2,3}_3D (rk3.h:87-121).
+template <int DIM, int STAGE, bool GH>
+__global__ void __launch_bounds__(256) stage_f64_kernel(StageArgs a) {
+    const Geo g = a.g;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int j = blockIdx.y * blockDim.y + threadIdx.y;
+    int k = DIM == 3 ? blockIdx.z * blockDim.z + threadIdx.z : 0;
+    if (i >= g.nx || j >= g.ny || k >= g.nz) return;
+    const double* __restrict__ G = (const double*)a.Gin + a.lay.off;
+    const Nb<GH> n = make_nb<GH>(g, a.lay, i, j, k);
+    const long long id = n.c();
+
+    double sx[7], sy[7], sz[7];
+#pragma unroll
+    for (int d = -3; d <= 3; ++d) {
+        sx[d + 3] = G[n.x(d)];
+        sy[d + 3] = G[n.y(d)];
+        if (DIM == 3) sz[d + 3] = G[n.z(d)];
+    }
+
+    double s_l = a.sl ? ((const double*)a.sl)[a.lay.off + id] : a.s_l;
+    double gx = 0.0, gy = 0.0, gz = 0.0, gm = 1.0;
+    if (s_l > a.eps) {
+        gx = (sx[4] - sx[2]) / (2.0 * a.dx);
+        gy = (sy[4] - sy[2]) / (2.0 * a.dy);
+        if (DIM == 3) {
+            gz = (sz[4] - sz[2]) / (2.0 * a.dz);
+            gm = sqrt(gx * gx + gy * gy + gz * gz + a.eps);
+        } else {
+            gm = sqrt(gx * gx + gy * gy + a.eps);
+        }
+    }
+    const double ue = ((const double*)a.u)[a.lay.off + id] - s_l * gx / gm;
+    const double ve = ((const double*)a.v)[a.lay.off + id] - s_l * gy / gm;
+    double rhs;
+    if (DIM == 3) {
+        const double we = ((const double*)a.w)[a.lay.off + id] - s_l * gz / gm;
+        double dgx = weno_deriv(sx, ue, a.dx);
+        double dgy = weno_deriv(sy, ve, a.dy);
+        double dgz = weno_deriv(sz, we, a.dz);
+        rhs = -(ue * dgx + ve * dgy + we * dgz);
+    } else {
+        double dgx = weno_deriv(sx, ue, a.dx);
+        double dgy = weno_deriv(sy, ve, a.dy);
+        rhs = -(ue * dgx + ve * dgy);
+    }
+
+    const double dt = a.dt;
+    double out;
+    if (STAGE == 1) {
+        out = sx[3] + dt * rhs;  // G_n + dt L(G_n), Gin == Gn
+    } else if (STAGE == 2) {
+        const double gn = ((const double*)a.Gn)[a.lay.off + id];
+        out = 0.75 * gn + 0.25 * sx[3] + 0.25 * dt * rhs;
+    } else {
+        const double gn = ((const double*)a.Gn)[a.lay.off + id];
+        const double a0 = 1.0 / 3.0, a2 = 2.0 / 3.0, b3 = 2.0 / 3.0;
+        out = a0 * gn + a2 * sx[3] + b3 * dt * rhs;
+    }
+    ((double*)a.Gout)[a.lay.off + id] = out;
+}
+
+// Godunov first-order |grad phi|^2 term of one axis by sign(S),
+// weno5_gradient_magnitude_3d (weno5.h:202-248).
+__device__ __forceinline__ double godunov_axis(double dm, double dp, bool pos) {
+    double a, b;
+    if (pos) { a = fmax(dm, 0.0); b = fmin(dp, 0.0); }
+    else { a = fmin(dm, 0.0); b = fmax(dp, 0.0); }
+    return fmax(a * a, b * b);
+}
+
+// Sign pattern and r~ of computeInterfaceCrossings3D (reinitialization.h:46-89)
+// from phi0 values c (centre) and nb[0..2*DIM) in the order -x,+x,-y,+y,-z,+z.
+template <int DIM>
+__device__ __forceinline__ void crossing_of(double c, const double* nb, int& flag, double& rt) {
+    double sum = 0.0;
+    int cnt = 0;
+    flag = 0;
+#pragma unroll
+    for (int q = 0; q < 2 * DIM; ++q) {
+        if (c * nb[q] < 0.0) { sum += nb[q]; cnt++; flag |= 1 << q; }
+    }
+    rt = (cnt > 0 && fabs(sum) > 1e-15) ? c / sum : 0.0;
+}
+
+// One HCR-2 pseudo-step, reinitStep3D (reinitialization.h:136-193) with
+// checkStabilityConstraint3D (:95-130).  STORED: r~/flag read from arrays
+// (drop-in); otherwise recomputed from phi0 with the same operations.
+template <int DIM, bool GH, bool STORED>
+__global__ void __launch_bounds__(256) reinit_f64_kernel(Geo g, Lay lay, const double* __restrict__ phin_,
+                                                         const double* __restrict__ phi0_,
+                                                         double* __restrict__ phinew_,
+                                                         const double* __restrict__ rt_,
+                                                         const int32_t* __restrict__ flag_,
+                                                         double dx, double dy, double dz,
+                                                         double dtau, double beta) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int j = blockIdx.y * blockDim.y + threadIdx.y;
+    int k = DIM == 3 ? blockIdx.z * blockDim.z + threadIdx.z : 0;
+    if (i >= g.nx || j >= g.ny || k >= g.nz) return;
+    const double* phin = phin_ + lay.off;
+    const double* phi0 = phi0_ + lay.off;
+    const Nb<GH> n = make_nb<GH>(g, lay, i, j, k);
+    const long long id = n.c();
+    long long nbi[6];
+    nbi[0] = n.x(-1); nbi[1] = n.x(1); nbi[2] = n.y(-1); nbi[3] = n.y(1);
+    if (DIM == 3) { nbi[4] = n.z(-1); nbi[5] = n.z(1); }
+
+    const double phi = phin[id];
+    const double ph0 = phi0[id];
+    double pn[6];
+#pragma unroll
+    for (int q = 0; q < 2 * DIM; ++q) pn[q] = phin[nbi[q]];
+
+    const double S = ph0 / sqrt(ph0 * ph0 + dx * dx);  // smoothSign, reinitialization.h:24
+    const bool pos = S > 0.0;
+    double gsq = godunov_axis((phi - pn[0]) / dx, (pn[1] - phi) / dx, pos)
+               + godunov_axis((phi - pn[2]) / dy, (pn[3] - phi) / dy, pos);
+    if (DIM == 3) gsq = gsq + godunov_axis((phi - pn[4]) / dz, (pn[5] - phi) / dz, pos);
+    const double term = -S * (sqrt(gsq) - 1.0);
+
+    int flag;
+    double rt;
+    if (STORED) {
+        flag = flag_[lay.off + id];
+        rt = rt_[lay.off + id];
+    } else {
+        double p0nb[6];
+#pragma unroll
+        for (int q = 0; q < 2 * DIM; ++q) p0nb[q] = phi0[nbi[q]];
+        crossing_of<DIM>(ph0, p0nb, flag, rt);
+    }
+    double forcing = 0.0;
+    if (flag != 0) {
+        bool stable = (phi > 0.0) == (ph0 > 0.0);
+#pragma unroll
+        for (int q = 0; q < 2 * DIM; ++q)
+            if ((flag >> q) & 1) stable = stable && ((pn[q] > 0.0) == (phi0[nbi[q]] > 0.0));
+        if (stable) {
+            double sum = 0.0;
+#pragma unroll
+            for (int q = 0; q < 2 * DIM; ++q)
+                if ((flag >> q) & 1) sum += pn[q];
+            forcing = beta * (rt * sum - phi) / dx;
+        }
+    }
+    phinew_[lay.off + id] = phi + dtau * (term + forcing);
+}
+
+template <int DIM, bool GH>
+__global__ void __launch_bounds__(256) crossings_f64_kernel(Geo g, Lay lay, const double* __restrict__ phi0_,
+                                                            double* __restrict__ rt_,
+                                                            int32_t* __restrict__ flag_) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int j = blockIdx.y * blockDim.y + threadIdx.y;
+    int k = DIM == 3 ? blockIdx.z * blockDim.z + threadIdx.z : 0;
+    if (i >= g.nx || j >= g.ny || k >= g.nz) return;
+    const double* phi0 = phi0_ + lay.off;
+    const Nb<GH> n = make_nb<GH>(g, lay, i, j, k);
+    double nb[6];
+    nb[0] = phi0[n.x(-1)]; nb[1] = phi0[n.x(1)]; nb[2] = phi0[n.y(-1)]; nb[3] = phi0[n.y(1)];
+    if (DIM == 3) { nb[4] = phi0[n.z(-1)]; nb[5] = phi0[n.z(1)]; }
+    int flag;
+    double rt;
+    crossing_of<DIM>(phi0[n.c()], nb, flag, rt);
+    rt_[lay.off + n.c()] = rt;
+    flag_[lay.off + n.c()] = flag;
+}
+
+// Ghost fill of a ghosted array: every ghost element takes the value of its
+// periodic image / clamped neighbour in the interior.
+__global__ void bc_fill_f64_kernel(Geo g, double* G) {
+    const long long nxT = g.nx + 2 * NG, nyT = g.ny + 2 * NG;
+    const long long nzT = g.dim == 3 ? g.nz + 2 * NG : 1;
+    const long long total = nxT * nyT * nzT;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+         e += (long long)gridDim.x * blockDim.x) {
+        int i = (int)(e % nxT);
+        int j = (int)((e / nxT) % nyT);
+        int k = (int)(e / (nxT * nyT));
+        int ii = i - NG, jj = j - NG, kk = g.dim == 3 ? k - NG : 0;
+        bool ghost = ii < 0 || ii >= g.nx || jj < 0 || jj >= g.ny ||
+                     (g.dim == 3 && (kk < 0 || kk >= g.nz));
+        if (!ghost) continue;
+        int si = map_axis(ii, g.nx, g.bcx) + NG;
+        int sj = map_axis(jj, g.ny, g.bcy) + NG;
+        int sk = g.dim == 3 ? map_axis(kk, g.nz, g.bcz) + NG : 0;
+        G[e] = G[(long long)sk * nxT * nyT + (long long)sj * nxT + si];
+    }
+}
+
+// src (FP64, any layout) -> dst compact T
+template <typename T>
+__global__ void pack_kernel(Geo g, const double* __restrict__ src, Lay sl, T* __restrict__ dst) {
+    const long long n = g.cells();
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n;
+         e += (long long)gridDim.x * blockDim.x) {
+        int i = (int)(e % g.nx);
+        int j = (int)((e / g.nx) % g.ny);
+        int k = (int)(e / ((long long)g.nx * g.ny));
+        dst[e] = (T)src[sl.off + i + (long long)j * sl.sy + (long long)k * sl.sz];
+    }
+}
+
+// src compact T -> dst FP64 in layout dl (ghosts filled from the images)
+template <typename T>
+__global__ void unpack_kernel(Geo g, const T* __restrict__ src, double* __restrict__ dst, Lay dl) {
+    if (!dl.ghosted) {
+        const long long n = g.cells();
+        for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n;
+             e += (long long)gridDim.x * blockDim.x)
+            dst[e] = (double)src[e];
+        return;
+    }
+    const long long nxT = g.nx + 2 * NG, nyT = g.ny + 2 * NG;
+    const long long nzT = g.dim == 3 ? g.nz + 2 * NG : 1;
+    const long long total = nxT * nyT * nzT;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+         e += (long long)gridDim.x * blockDim.x) {
+        int i = (int)(e % nxT);
+        int j = (int)((e / nxT) % nyT);
+        int k = (int)(e / (nxT * nyT));
+        int si = map_axis(i - NG, g.nx, g.bcx);
+        int sj = map_axis(j - NG, g.ny, g.bcy);
+        int sk = g.dim == 3 ? map_axis(k - NG, g.nz, g.bcz) : 0;
+        dst[e] = (double)src[(long long)sk * g.nx * g.ny + (long long)sj * g.nx + si];
+    }
+}
+
+inline dim3 cell_grid(const Geo& g, dim3 b) {
+    return dim3((g.nx + b.x - 1) / b.x, (g.ny + b.y - 1) / b.y, (g.nz + b.z - 1) / b.z);
+}
+inline dim3 cell_block(const Geo& g) { return g.dim == 3 ? dim3(32, 4, 2) : dim3(32, 8, 1); }
+
+inline unsigned flat_blocks(long long n) {
+    long long b = (n + 255) / 256;
+    return (unsigned)(b > 152 * 64 ? 152 * 64 : (b < 1 ? 1 : b));
+}
+
+}  // namespace
+
+cudaError_t launch_stage_f64(const StageArgs& a, cudaStream_t st) {
+    dim3 b = cell_block(a.g), gr = cell_grid(a.g, b);
+    const bool gh = a.lay.ghosted != 0;
+#define LSGB_STAGE(D, S, GHV) stage_f64_kernel<D, S, GHV><<<gr, b, 0, st>>>(a)
+    if (a.g.dim == 3) {
+        if (gh) {
+            if (a.stage == 1) LSGB_STAGE(3, 1, true); else if (a.stage == 2) LSGB_STAGE(3, 2, true); else LSGB_STAGE(3, 3, true);
+        } else {
+            if (a.stage == 1) LSGB_STAGE(3, 1, false); else if (a.stage == 2) LSGB_STAGE(3, 2, false); else LSGB_STAGE(3, 3, false);
+        }
+    } else {
+        if (gh) {
+            if (a.stage == 1) LSGB_STAGE(2, 1, true); else if (a.stage == 2) LSGB_STAGE(2, 2, true); else LSGB_STAGE(2, 3, true);
+        } else {
+            if (a.stage == 1) LSGB_STAGE(2, 1, false); else if (a.stage == 2) LSGB_STAGE(2, 2, false); else LSGB_STAGE(2, 3, false);
+        }
+    }
+#undef LSGB_STAGE
+    count_launches(1);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_reinit_f64(const ReinitArgs& a, cudaStream_t st) {
+    dim3 b = cell_block(a.g), gr = cell_grid(a.g, b);
+    const double* pn = (const double*)a.phin;
+    const double* p0 = (const double*)a.phi0;
+    double* out = (double*)a.phinew;
+    if (a.g.dim == 3) {
+        if (a.lay.ghosted)
+            reinit_f64_kernel<3, true, false><<<gr, b, 0, st>>>(a.g, a.lay, pn, p0, out, nullptr, nullptr, a.dx, a.dy, a.dz, a.dtau, a.beta);
+        else
+            reinit_f64_kernel<3, false, false><<<gr, b, 0, st>>>(a.g, a.lay, pn, p0, out, nullptr, nullptr, a.dx, a.dy, a.dz, a.dtau, a.beta);
+    } else {
+        if (a.lay.ghosted)
+            reinit_f64_kernel<2, true, false><<<gr, b, 0, st>>>(a.g, a.lay, pn, p0, out, nullptr, nullptr, a.dx, a.dy, a.dz, a.dtau, a.beta);
+        else
+            reinit_f64_kernel<2, false, false><<<gr, b, 0, st>>>(a.g, a.lay, pn, p0, out, nullptr, nullptr, a.dx, a.dy, a.dz, a.dtau, a.beta);
+    }
+    count_launches(1);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_crossings_f64(const Geo& g, const Lay& lay, const double* phi0, double* rt,
+                                 int32_t* flag, cudaStream_t st) {
+    dim3 b = cell_block(g), gr = cell_grid(g, b);
+    if (g.dim == 3) {
+        if (lay.ghosted) crossings_f64_kernel<3, true><<<gr, b, 0, st>>>(g, lay, phi0, rt, flag);
+        else crossings_f64_kernel<3, false><<<gr, b, 0, st>>>(g, lay, phi0, rt, flag);
+    } else {
+        if (lay.ghosted) crossings_f64_kernel<2, true><<<gr, b, 0, st>>>(g, lay, phi0, rt, flag);
+        else crossings_f64_kernel<2, false><<<gr, b, 0, st>>>(g, lay, phi0, rt, flag);
+    }
+    count_launches(1);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_reinit_step_stored_f64(const Geo& g, const Lay& lay, const double* phin,
+                                          double* phinew, const double* phi0, const double* rt,
+                                          const int32_t* flag, double dx, double dy, double dz,
+                                          double dtau, double beta, cudaStream_t st) {
+    dim3 b = cell_block(g), gr = cell_grid(g, b);
+    if (g.dim == 3) {
+        if (lay.ghosted)
+            reinit_f64_kernel<3, true, true><<<gr, b, 0, st>>>(g, lay, phin, phi0, phinew, rt, flag, dx, dy, dz, dtau, beta);
+        else
+            reinit_f64_kernel<3, false, true><<<gr, b, 0, st>>>(g, lay, phin, phi0, phinew, rt, flag, dx, dy, dz, dtau, beta);
+    } else {
+        if (lay.ghosted)
+            reinit_f64_kernel<2, true, true><<<gr, b, 0, st>>>(g, lay, phin, phi0, phinew, rt, flag, dx, dy, dz, dtau, beta);
+        else
+            reinit_f64_kernel<2, false, true><<<gr, b, 0, st>>>(g, lay, phin, phi0, phinew, rt, flag, dx, dy, dz, dtau, beta);
+    }
+    count_launches(1);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_bc_fill_f64(const Geo& g, double* G, cudaStream_t st) {
+    bc_fill_f64_kernel<<<flat_blocks(layout_elems(g, 1)), 256, 0, st>>>(g, G);
+    count_launches(1);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pack_f64(const Geo& g, const double* src, const Lay& sl, double* dst, cudaStream_t st) {
+    pack_kernel<double><<<flat_blocks(g.cells()), 256, 0, st>>>(g, src, sl, dst);
+    count_launches(1);
+    return cudaGetLastError();
+}
+cudaError_t launch_pack_f32(const Geo& g, const double* src, const Lay& sl, float* dst, cudaStream_t st) {
+    pack_kernel<float><<<flat_blocks(g.cells()), 256, 0, st>>>(g, src, sl, dst);
+    count_launches(1);
+    return cudaGetLastError();
+}
+cudaError_t launch_unpack_f64(const Geo& g, const double* src, double* dst, const Lay& dl, cudaStream_t st) {
+    unpack_kernel<double><<<flat_blocks(layout_elems(g, dl.ghosted)), 256, 0, st>>>(g, src, dst, dl);
+    count_launches(1);
+    return cudaGetLastError();
+}
+cudaError_t launch_unpack_f32(const Geo& g, const float* src, double* dst, const Lay& dl, cudaStream_t st) {
+    unpack_kernel<float><<<flat_blocks(layout_elems(g, dl.ghosted)), 256, 0, st>>>(g, src, dst, dl);
+    count_launches(1);
+    return cudaGetLastError();
+}
+
+}  // namespace lsgb

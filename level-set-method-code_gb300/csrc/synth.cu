@@ -1,0 +1,148 @@
+// synth.cu -- on-device generator of the synthetic benchmark fields.
+//
+// The benchmark grids (256^3, 512^3) are too large to build on the host in a
+// reasonable time, so the fields are evaluated here in FP64 from a small mode
+// table that the host draws from a seed (lsgb/synthetic.py holds the same
+// formulas in numpy for the small grids the tests compare against):
+//   G0(x) = |x - c| - (r0 + sum_m amp_m * Pbar_lm(cos theta) * trig_m(phi))
+//   u(x)  = sum_m C_m cos(2 pi k_m . x + phase_m)
+// with cell centres x_i = i * dx on the periodic unit box.  amp_m already
+// carries the normalisation that makes max |Pbar_lm * trig_m| = 1.
+#include "common.cuh"
+
+namespace lsgb {
+namespace {
+
+__constant__ lsgb_synth c_synth;
+
+// Associated Legendre P_l^m(x) for 0 <= m <= l <= 4 (no Condon-Shortley phase).
+__device__ double assoc_legendre(int l, int m, double x) {
+    const double s = sqrt(fmax(0.0, 1.0 - x * x));
+    // P_m^m = (2m-1)!! s^m
+    double pmm = 1.0;
+    for (int q = 1; q <= m; ++q) pmm *= (2.0 * q - 1.0) * s;
+    if (l == m) return pmm;
+    double pm1 = x * (2.0 * m + 1.0) * pmm;
+    if (l == m + 1) return pm1;
+    double pl = 0.0;
+    for (int ll = m + 2; ll <= l; ++ll) {
+        pl = (x * (2.0 * ll - 1.0) * pm1 - (ll + m - 1.0) * pmm) / (ll - m);
+        pmm = pm1;
+        pm1 = pl;
+    }
+    return pl;
+}
+
+__global__ void synth_kernel(Geo g, double dx, double dy, double dz, double* __restrict__ G,
+                             double* __restrict__ u, double* __restrict__ v,
+                             double* __restrict__ w) {
+    const lsgb_synth& d = c_synth;
+    const long long n = g.cells();
+    const long long nxy = (long long)g.nx * g.ny;
+    const double two_pi = 6.283185307179586476925286766559;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n;
+         e += (long long)gridDim.x * blockDim.x) {
+        const int k = (int)(e / nxy);
+        const long long r = e - (long long)k * nxy;
+        const int j = (int)(r / g.nx);
+        const int i = (int)(r - (long long)j * g.nx);
+        const double x = i * dx, y = j * dy, z = g.dim == 3 ? k * dz : 0.0;
+        const double px = x - d.center[0], py = y - d.center[1], pz = g.dim == 3 ? z - d.center[2] : 0.0;
+        const double rad = sqrt(px * px + py * py + pz * pz);
+        double radius = d.r0;
+        if (g.dim == 3 && rad > 0.0) {
+            const double ct = pz / rad;
+            const double ph = atan2(py, px);
+            for (int m = 0; m < d.n_shape_modes; ++m) {
+                const int l = d.shape_l[m], mm = d.shape_m[m];
+                const int am = mm < 0 ? -mm : mm;
+                const double trig = mm >= 0 ? cos(am * ph) : sin(am * ph);
+                radius += d.shape_amp[m] * assoc_legendre(l, am, ct) * trig;
+            }
+        }
+        G[e] = rad - radius;
+        double uu = 0.0, vv = 0.0, ww = 0.0;
+        for (int m = 0; m < d.n_vel_modes; ++m) {
+            const double th = two_pi * (d.vel_k[m][0] * x + d.vel_k[m][1] * y + d.vel_k[m][2] * z) +
+                              d.vel_phase[m];
+            const double cs = cos(th);
+            uu += d.vel_c[m][0] * cs;
+            vv += d.vel_c[m][1] * cs;
+            ww += d.vel_c[m][2] * cs;
+        }
+        const double sc = d.vel_scale > 0.0 ? d.vel_scale : 1.0;
+        u[e] = uu * sc;
+        v[e] = vv * sc;
+        if (g.dim == 3) w[e] = ww * sc;
+    }
+}
+
+__global__ void scale3_kernel(long long n, double s, double* u, double* v, double* w) {
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n;
+         e += (long long)gridDim.x * blockDim.x) {
+        u[e] *= s;
+        v[e] *= s;
+        if (w) w[e] *= s;
+    }
+}
+
+// computeDeformationVelocity (Local_code/level-set_MPI_3D/include/
+// initial_conditions.h:232-247) at the cell centres x_i = i * dx, written
+// straight into the compact velocity arrays of the solver.
+template <typename T>
+__global__ void deformation_kernel(Geo g, double dx, double dy, double dz, double t, double Tp,
+                                   T* __restrict__ u, T* __restrict__ v, T* __restrict__ w) {
+    const long long n = g.cells();
+    const long long nxy = (long long)g.nx * g.ny;
+    const double pi = 3.14159265358979323846;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n;
+         e += (long long)gridDim.x * blockDim.x) {
+        const int k = (int)(e / nxy);
+        const long long r = e - (long long)k * nxy;
+        const int j = (int)(r / g.nx);
+        const int i = (int)(r - (long long)j * g.nx);
+        const double x = i * dx, y = j * dy, z = k * dz;
+        const double tf = cos(pi * t / Tp);
+        const double spx = sin(pi * x), s2px = sin(2.0 * pi * x);
+        const double spy = sin(pi * y), s2py = sin(2.0 * pi * y);
+        const double spz = sin(pi * z), s2pz = sin(2.0 * pi * z);
+        u[e] = (T)(2.0 * spx * spx * s2py * s2pz * tf);
+        v[e] = (T)(-s2px * spy * spy * s2pz * tf);
+        w[e] = (T)(-s2px * s2py * spz * spz * tf);
+    }
+}
+
+}  // namespace
+
+cudaError_t launch_deformation(const Geo& g, double dx, double dy, double dz, double t, double Tp,
+                               void* u, void* v, void* w, bool f32, cudaStream_t st) {
+    long long blocks = (g.cells() + 255) / 256;
+    if (blocks > 152 * 32) blocks = 152 * 32;
+    if (f32)
+        deformation_kernel<float><<<(unsigned)blocks, 256, 0, st>>>(g, dx, dy, dz, t, Tp, (float*)u, (float*)v, (float*)w);
+    else
+        deformation_kernel<double><<<(unsigned)blocks, 256, 0, st>>>(g, dx, dy, dz, t, Tp, (double*)u, (double*)v, (double*)w);
+    count_launches(1);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_synth(const Geo& g, const lsgb_synth& d, double dx, double dy, double dz,
+                         double* G, double* u, double* v, double* w, cudaStream_t st) {
+    cudaError_t e = cudaMemcpyToSymbolAsync(c_synth, &d, sizeof(d), 0, cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return e;
+    long long blocks = (g.cells() + 255) / 256;
+    if (blocks > 152 * 32) blocks = 152 * 32;
+    synth_kernel<<<(unsigned)blocks, 256, 0, st>>>(g, dx, dy, dz, G, u, v, w);
+    count_launches(1);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_scale3(long long n, double s, double* u, double* v, double* w, cudaStream_t st) {
+    long long blocks = (n + 255) / 256;
+    if (blocks > 152 * 32) blocks = 152 * 32;
+    scale3_kernel<<<(unsigned)blocks, 256, 0, st>>>(n, s, u, v, w);
+    count_launches(1);
+    return cudaGetLastError();
+}
+
+}  // namespace lsgb

@@ -1,0 +1,344 @@
+"""Python binding of the GB300 level-set solver (ctypes over the C ABI).
+
+The product is the CUDA library ``_build/liblsgb.so`` with the C ABI of
+``include/lsgb.h``; this module only marshals arguments.  It never computes a
+result itself and has no CPU fallback: if the library is missing or no GPU is
+present, the calls fail with :class:`LsgbError`.
+
+Arrays
+  * host arrays: float64 numpy arrays;
+  * device arrays: objects with ``data_ptr()`` and ``is_cuda`` (torch tensors);
+  * ``layout="ghosted"`` is the reference's layout with 3 ghost cells per side,
+    shape ``(nz+6, ny+6, nx+6)`` / ``(ny+6, nx+6)``; ``"compact"`` is the
+    interior only, ``(nz, ny, nx)`` / ``(ny, nx)``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+_PKG = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+LIB_PATH = os.path.join(_PKG, "_build", "liblsgb.so")
+
+OK = 0
+BC_PERIODIC, BC_ZERO_GRADIENT = 0, 1
+PREC_F64, PREC_F32 = 0, 1
+LAYOUT_GHOSTED, LAYOUT_COMPACT = 0, 1
+MEM_HOST, MEM_DEVICE = 0, 1
+MAX_MODES = 32
+
+
+class LsgbError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"lsgb error {code}: {msg}")
+        self.code = code
+
+
+class Params(C.Structure):
+    """Mirror of ``lsgb_params`` (include/lsgb.h)."""
+
+    _fields_ = [
+        ("dim", C.c_int), ("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int), ("nghost", C.c_int),
+        ("dx", C.c_double), ("dy", C.c_double), ("dz", C.c_double),
+        ("s_l", C.c_double), ("dt", C.c_double), ("cfl", C.c_double), ("epsilon", C.c_double),
+        ("enable_reinit", C.c_int), ("reinit_interval", C.c_int), ("reinit_iterations", C.c_int),
+        ("reinit_dtau", C.c_double), ("reinit_beta", C.c_double),
+        ("bc_x", C.c_int), ("bc_y", C.c_int), ("bc_z", C.c_int),
+    ]
+
+    def shape(self, layout: str = "ghosted"):
+        g = 6 if layout == "ghosted" else 0
+        if self.dim == 3:
+            return (self.nz + g, self.ny + g, self.nx + g)
+        return (self.ny + g, self.nx + g)
+
+    @property
+    def cells(self) -> int:
+        return self.nx * self.ny * (self.nz if self.dim == 3 else 1)
+
+
+class Synth(C.Structure):
+    """Mirror of ``lsgb_synth`` (include/lsgb.h)."""
+
+    _fields_ = [
+        ("center", C.c_double * 3), ("r0", C.c_double),
+        ("n_shape_modes", C.c_int),
+        ("shape_l", C.c_int * MAX_MODES), ("shape_m", C.c_int * MAX_MODES),
+        ("shape_amp", C.c_double * MAX_MODES),
+        ("n_vel_modes", C.c_int),
+        ("vel_k", (C.c_double * 3) * MAX_MODES), ("vel_c", (C.c_double * 3) * MAX_MODES),
+        ("vel_phase", C.c_double * MAX_MODES), ("vel_scale", C.c_double),
+    ]
+
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    """Load liblsgb.so (raises when it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise LsgbError(-1, f"{LIB_PATH} is missing: run __graft_entry__.build()")
+    L = C.CDLL(LIB_PATH)
+    L.lsgb_last_error.restype = C.c_char_p
+    L.lsgb_version.restype = C.c_char_p
+    L.lsgb_launch_count.restype = C.c_uint64
+    _lib = L
+    return L
+
+
+def _check(rc: int):
+    if rc != OK:
+        raise LsgbError(rc, lib().lsgb_last_error().decode())
+
+
+def version() -> str:
+    return lib().lsgb_version().decode()
+
+
+def launch_count() -> int:
+    return int(lib().lsgb_launch_count())
+
+
+def params(dim: int, nx: int, ny: int, nz: int = 1, **kw) -> Params:
+    """Reference defaults (lsgb_params_default) with keyword overrides."""
+    p = Params()
+    lib().lsgb_params_default(C.byref(p), dim, nx, ny, nz if dim == 3 else 1)
+    for k, v in kw.items():
+        if k in ("bc_x", "bc_y", "bc_z") and isinstance(v, str):
+            v = {"periodic": BC_PERIODIC, "zero_gradient": BC_ZERO_GRADIENT}[v]
+        if not hasattr(p, k):
+            raise AttributeError(k)
+        setattr(p, k, int(v) if isinstance(v, bool) else v)
+    if "reinit_dtau" not in kw and any(k in kw for k in ("dx", "dy", "dz")):
+        h = min(p.dx, p.dy, p.dz) if dim == 3 else min(p.dx, p.dy)
+        p.reinit_dtau = 0.25 * h
+    return p
+
+
+def check_params(p: Params):
+    _check(lib().lsgb_params_check(C.byref(p)))
+
+
+# -- pointer helpers --------------------------------------------------------
+def _is_dev(a) -> bool:
+    return hasattr(a, "data_ptr") and getattr(a, "is_cuda", False)
+
+
+def _ptr(a):
+    if a is None:
+        return None
+    if _is_dev(a):
+        return C.c_void_p(a.data_ptr())
+    if isinstance(a, np.ndarray):
+        if a.dtype != np.float64 or not a.flags.c_contiguous:
+            raise ValueError("host arrays must be C-contiguous float64")
+        return C.c_void_p(a.ctypes.data)
+    if hasattr(a, "data_ptr"):  # torch CPU tensor (pinned host buffers)
+        return C.c_void_p(a.data_ptr())
+    raise TypeError(type(a))
+
+
+def _mem(*arrs) -> int:
+    kinds = {MEM_DEVICE if _is_dev(a) else MEM_HOST for a in arrs if a is not None}
+    if len(kinds) > 1:
+        raise ValueError("mix of host and device arrays")
+    return kinds.pop() if kinds else MEM_HOST
+
+
+def _layout(name: str) -> int:
+    return {"ghosted": LAYOUT_GHOSTED, "compact": LAYOUT_COMPACT}[name]
+
+
+def _stream(stream) -> C.c_void_p:
+    if stream is None:
+        return C.c_void_p(0)
+    if hasattr(stream, "cuda_stream"):
+        return C.c_void_p(stream.cuda_stream)
+    return C.c_void_p(int(stream))
+
+
+# -- drop-in FP64 entry points (device tensors, ghosted layout) -------------
+def rk3_step_f64(p: Params, G_n, G_new, G_1, G_2, u, v, w=None, sl=None, stream=None):
+    """lsgb_rk3_step_f64 -- rk3TimeStep3D / rk3TimeStep on device buffers."""
+    _check(lib().lsgb_rk3_step_f64(C.byref(p), _ptr(G_n), _ptr(G_new), _ptr(G_1), _ptr(G_2),
+                                   _ptr(u), _ptr(v), _ptr(w), _ptr(sl), _stream(stream)))
+
+
+def apply_bc_f64(p: Params, G, stream=None):
+    _check(lib().lsgb_apply_bc_f64(C.byref(p), _ptr(G), _stream(stream)))
+
+
+def reinit_f64(p: Params, phi, phi_tmp, phi0, r_tilde, flag, stream=None):
+    """lsgb_reinit_f64 -- reinitializeWithSwap[3D]; returns (phi, phi_tmp)
+    after the swap (the tensors themselves, reordered)."""
+    a = C.c_void_p(phi.data_ptr())
+    b = C.c_void_p(phi_tmp.data_ptr())
+    _check(lib().lsgb_reinit_f64(C.byref(p), C.byref(a), C.byref(b), _ptr(phi0), _ptr(r_tilde),
+                                 _ptr(flag), _stream(stream)))
+    if a.value == phi.data_ptr():
+        return phi, phi_tmp
+    return phi_tmp, phi
+
+
+def volume_f64(p: Params, G, stream=None):
+    vol = C.c_double()
+    cnt = C.c_int64()
+    _check(lib().lsgb_volume_f64(C.byref(p), _ptr(G), C.byref(vol), C.byref(cnt), _stream(stream)))
+    return vol.value, cnt.value
+
+
+def l2_error_f64(p: Params, G, G_ref, stream=None) -> float:
+    r = C.c_double()
+    _check(lib().lsgb_l2_error_f64(C.byref(p), _ptr(G), _ptr(G_ref), C.byref(r), _stream(stream)))
+    return r.value
+
+
+def max_speed_f64(p: Params, u, v, w=None, stream=None) -> float:
+    r = C.c_double()
+    _check(lib().lsgb_max_speed_f64(C.byref(p), _ptr(u), _ptr(v), _ptr(w), C.byref(r), _stream(stream)))
+    return r.value
+
+
+def cfl_dt(p: Params, max_speed: float) -> float:
+    r = C.c_double()
+    _check(lib().lsgb_cfl_dt(C.byref(p), C.c_double(max_speed), C.byref(r)))
+    return r.value
+
+
+# -- solver handle ------------------------------------------------------------
+class Solver:
+    """Device-resident solver (lsgb_solver_*)."""
+
+    def __init__(self, p: Params, precision: str = "f64"):
+        self._h = C.c_void_p()
+        prec = {"f64": PREC_F64, "f32": PREC_F32}[precision]
+        _check(lib().lsgb_solver_create(C.byref(p), prec, C.byref(self._h)))
+        self.precision = precision
+        self.p = self.params()
+
+    def close(self):
+        if self._h:
+            lib().lsgb_solver_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def params(self) -> Params:
+        p = Params()
+        _check(lib().lsgb_solver_get_params(self._h, C.byref(p)))
+        return p
+
+    def set_stream(self, stream):
+        _check(lib().lsgb_solver_set_stream(self._h, _stream(stream)))
+
+    def set_dt(self, dt: float):
+        _check(lib().lsgb_solver_set_dt(self._h, C.c_double(dt)))
+
+    def set_fields(self, G=None, u=None, v=None, w=None, layout: str = "ghosted"):
+        _check(lib().lsgb_solver_set_fields(self._h, _ptr(G), _ptr(u), _ptr(v), _ptr(w),
+                                            _layout(layout), _mem(G, u, v, w)))
+
+    def set_sl_field(self, sl, layout: str = "ghosted"):
+        _check(lib().lsgb_solver_set_sl_field(self._h, _ptr(sl), _layout(layout), _mem(sl)))
+
+    def get_G(self, layout: str = "ghosted", out=None):
+        p = self.params()
+        if out is None:
+            out = np.empty(p.shape(layout), dtype=np.float64)
+        _check(lib().lsgb_solver_get_G(self._h, _ptr(out), _layout(layout), _mem(out)))
+        return out
+
+    def advance(self, n_steps: int):
+        _check(lib().lsgb_solver_advance(self._h, int(n_steps)))
+
+    def reinit(self):
+        _check(lib().lsgb_solver_reinit(self._h))
+
+    @property
+    def step(self) -> int:
+        s = C.c_int()
+        _check(lib().lsgb_solver_get_step(self._h, C.byref(s)))
+        return s.value
+
+    @step.setter
+    def step(self, v: int):
+        _check(lib().lsgb_solver_set_step(self._h, int(v)))
+
+    def volume(self):
+        vol = C.c_double()
+        cnt = C.c_int64()
+        _check(lib().lsgb_solver_volume(self._h, C.byref(vol), C.byref(cnt)))
+        return vol.value, cnt.value
+
+    def max_speed(self) -> float:
+        r = C.c_double()
+        _check(lib().lsgb_solver_max_speed(self._h, C.byref(r)))
+        return r.value
+
+    def compute_dt(self, cfl: float) -> float:
+        r = C.c_double()
+        _check(lib().lsgb_solver_compute_dt(self._h, C.c_double(cfl), C.byref(r)))
+        return r.value
+
+    def l2_error(self, G_ref, layout: str = "ghosted") -> float:
+        r = C.c_double()
+        _check(lib().lsgb_solver_l2_error(self._h, _ptr(G_ref), _layout(layout), _mem(G_ref), C.byref(r)))
+        return r.value
+
+    def run_host(self, G, u, v, w, n_steps: int, out, layout: str = "ghosted"):
+        _check(lib().lsgb_solver_run_host(self._h, _ptr(G), _ptr(u), _ptr(v), _ptr(w), int(n_steps),
+                                          _ptr(out), _layout(layout)))
+        return out
+
+    def synth(self, d: Synth):
+        _check(lib().lsgb_solver_synth(self._h, C.byref(d)))
+
+
+def _set_velocity_deformation(self, t: float, T: float):
+    """Device-side deformation vortex of the reference's default 3D case."""
+    _check(lib().lsgb_solver_set_velocity_deformation(self._h, C.c_double(t), C.c_double(T)))
+
+
+Solver.set_velocity_deformation = _set_velocity_deformation
+
+
+def _get_field(self, which: str, layout: str = "ghosted", out=None):
+    """Download a resident field ("G", "u", "v", "w", "sl") as FP64."""
+    code = {"G": 0, "u": 1, "v": 2, "w": 3, "sl": 4}[which]
+    p = self.params()
+    if out is None:
+        out = np.empty(p.shape(layout), dtype=np.float64)
+    _check(lib().lsgb_solver_get_field(self._h, code, _ptr(out), _layout(layout), _mem(out)))
+    return out
+
+
+def _enable_timing(self, on: bool = True):
+    _check(lib().lsgb_solver_enable_timing(self._h, int(on)))
+
+
+def _kernel_times(self):
+    """(stage_ms, stage_launches, reinit_ms, reinit_launches) since enable_timing."""
+    a, b = C.c_double(), C.c_double()
+    na, nb = C.c_int64(), C.c_int64()
+    _check(lib().lsgb_solver_kernel_times(self._h, C.byref(a), C.byref(na), C.byref(b), C.byref(nb)))
+    return a.value, na.value, b.value, nb.value
+
+
+Solver.get_field = _get_field
+Solver.enable_timing = _enable_timing
+Solver.kernel_times = _kernel_times

@@ -1,0 +1,230 @@
+"""Seeded synthetic workloads of the benchmark configurations.
+
+No dataset is involved: every input is generated from a seed.  The mode
+tables are drawn here with numpy's PCG64 (``default_rng``), seed
+``20261203 + 1000 * config + instance``; the same table drives
+
+* :func:`host_fields` -- the fields evaluated in numpy FP64 on the host (small
+  grids: tests and the CPU baselines), and
+* :func:`to_device_desc` -- the ``lsgb_synth`` descriptor the device generator
+  (csrc/synth.cu) evaluates in FP64 for the large grids.
+
+Fields (cell centres x_i = i * dx on the periodic unit box):
+  G0 = |x - c| - (r0 + sum_m a_m Y_m(theta, phi))   sphere with l <= 4 modes
+  G0 = |x - c| - r0                                 circle (2D)
+  u  = curl A,  A = sum_m a_m sin(2 pi k_m . x + phase_m),  0 < |k_m| <= kmax,
+       a_m ~ N(0, 1)^3, phase ~ U(0, 2 pi); 2D: stream function, u = (psi_y, -psi_x).
+  The velocity is scaled so that max |u|_2 = 1 over the grid.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+SEED_BASE = 20261203
+
+
+def seed_for(config: int, instance: int = 0) -> int:
+    return SEED_BASE + 1000 * config + instance
+
+
+def _assoc_legendre(l: int, m: int, x):
+    """P_l^m(x), 0 <= m <= l, no Condon-Shortley phase (same recursion as synth.cu)."""
+    x = np.asarray(x, dtype=np.float64)
+    s = np.sqrt(np.maximum(0.0, 1.0 - x * x))
+    pmm = np.ones_like(x)
+    for q in range(1, m + 1):
+        pmm = pmm * ((2.0 * q - 1.0) * s)
+    if l == m:
+        return pmm
+    pm1 = x * (2.0 * m + 1.0) * pmm
+    if l == m + 1:
+        return pm1
+    pl = pm1
+    for ll in range(m + 2, l + 1):
+        pl = (x * (2.0 * ll - 1.0) * pm1 - (ll + m - 1.0) * pmm) / (ll - m)
+        pmm, pm1 = pm1, pl
+    return pl
+
+
+def _legendre_max(l: int, m: int) -> float:
+    xs = np.linspace(-1.0, 1.0, 20001)
+    return float(np.max(np.abs(_assoc_legendre(l, m, xs))))
+
+
+@dataclass
+class Workload:
+    """One synthetic instance: grid, physics and mode table."""
+
+    dim: int
+    n: tuple
+    s_l: float
+    center: tuple = (0.5, 0.5, 0.5)
+    r0: float = 0.2
+    shape_l: list = field(default_factory=list)
+    shape_m: list = field(default_factory=list)
+    shape_amp: list = field(default_factory=list)   # already normalised
+    vel_k: list = field(default_factory=list)
+    vel_c: list = field(default_factory=list)       # 2 pi k x a  (2D: 2 pi a (k_y, -k_x))
+    vel_phase: list = field(default_factory=list)
+    uniform_velocity: tuple | None = None           # config 1: u = (1, 0)
+
+    @property
+    def spacing(self):
+        return tuple(1.0 / q for q in self.n)
+
+
+def draw_modes(rng: np.random.Generator, dim: int, n_vel: int, kmax: int = 4):
+    ks, cs, ph = [], [], []
+    while len(ks) < n_vel:
+        k = rng.integers(-kmax, kmax + 1, size=dim)
+        r2 = int(np.sum(k * k))
+        if r2 == 0 or r2 > kmax * kmax:
+            continue
+        if dim == 3:
+            a = rng.standard_normal(3)
+            c = 2.0 * math.pi * np.cross(k.astype(np.float64), a)
+            ks.append([float(k[0]), float(k[1]), float(k[2])])
+        else:
+            a = rng.standard_normal()
+            c = 2.0 * math.pi * a * np.array([k[1], -k[0], 0.0], dtype=np.float64)
+            ks.append([float(k[0]), float(k[1]), 0.0])
+        cs.append([float(c[0]), float(c[1]), float(c[2])])
+        ph.append(float(rng.uniform(0.0, 2.0 * math.pi)))
+    return ks, cs, ph
+
+
+def draw_shape(rng: np.random.Generator, n_modes: int, amp: float = 0.02):
+    ls, ms, amps = [], [], []
+    for _ in range(n_modes):
+        l = int(rng.integers(1, 5))
+        m = int(rng.integers(-l, l + 1))
+        a = float(rng.uniform(-amp, amp))
+        ls.append(l)
+        ms.append(m)
+        amps.append(a / _legendre_max(l, abs(m)))
+    return ls, ms, amps
+
+
+def config1(n: int = 128) -> Workload:
+    """2D plain FP64: circle r = 0.25 at (0.5, 0.5), u = (1, 0), S_L = 0.1."""
+    return Workload(dim=2, n=(n, n), s_l=0.1, center=(0.5, 0.5, 0.0), r0=0.25,
+                    uniform_velocity=(1.0, 0.0))
+
+
+def sphere_config(config: int, n: int, n_vel: int, s_l: float, instance: int = 0,
+                  n_shape: int = 8, r0: float = 0.2, center=(0.5, 0.5, 0.5)) -> Workload:
+    """Configs 2/3: perturbed sphere + curl of a random vector potential."""
+    rng = np.random.default_rng(seed_for(config, instance))
+    ls, ms, amps = draw_shape(rng, n_shape)
+    ks, cs, ph = draw_modes(rng, 3, n_vel)
+    return Workload(dim=3, n=(n, n, n), s_l=s_l, center=tuple(center), r0=r0, shape_l=ls,
+                    shape_m=ms, shape_amp=amps, vel_k=ks, vel_c=cs, vel_phase=ph)
+
+
+def config2(n: int = 256) -> Workload:
+    return sphere_config(2, n, 16, 0.2)
+
+
+def config3(n: int = 512) -> Workload:
+    return sphere_config(3, n, 24, 0.2)
+
+
+def _coords(wl: Workload, ghosted: bool):
+    g = 3 if ghosted else 0
+    axes = []
+    for q in wl.n:
+        axes.append((np.arange(q + 2 * g, dtype=np.float64) - g) / q)
+    if wl.dim == 3:
+        z, y, x = np.meshgrid(axes[2], axes[1], axes[0], indexing="ij")
+        return x, y, z
+    y, x = np.meshgrid(axes[1], axes[0], indexing="ij")
+    return x, y, np.zeros_like(x)
+
+
+def host_fields(wl: Workload, normalise: bool = True):
+    """(G, u, v, w) float64 in the ghosted layout, ghosts = periodic images.
+    w is None in 2D.  Evaluated at interior cells, then wrapped."""
+    x, y, z = _coords(wl, ghosted=False)
+    px, py = x - wl.center[0], y - wl.center[1]
+    pz = z - wl.center[2] if wl.dim == 3 else np.zeros_like(x)
+    rad = np.sqrt(px * px + py * py + pz * pz)
+    radius = np.full_like(rad, wl.r0)
+    if wl.dim == 3 and wl.shape_l:
+        with np.errstate(invalid="ignore", divide="ignore"):
+            ct = np.where(rad > 0, pz / np.where(rad > 0, rad, 1.0), 0.0)
+        ph = np.arctan2(py, px)
+        for l, m, a in zip(wl.shape_l, wl.shape_m, wl.shape_amp):
+            am = abs(m)
+            trig = np.cos(am * ph) if m >= 0 else np.sin(am * ph)
+            radius = radius + np.where(rad > 0, a * _assoc_legendre(l, am, ct) * trig, 0.0)
+    G = rad - radius
+    if wl.uniform_velocity is not None:
+        u = np.full_like(G, wl.uniform_velocity[0])
+        v = np.full_like(G, wl.uniform_velocity[1])
+        w = np.zeros_like(G) if wl.dim == 3 else None
+    else:
+        u = np.zeros_like(G)
+        v = np.zeros_like(G)
+        w = np.zeros_like(G)
+        for k, c, phs in zip(wl.vel_k, wl.vel_c, wl.vel_phase):
+            th = 2.0 * math.pi * (k[0] * x + k[1] * y + k[2] * z) + phs
+            cs = np.cos(th)
+            u += c[0] * cs
+            v += c[1] * cs
+            w += c[2] * cs
+        if normalise:
+            sp = np.sqrt(u * u + v * v + (w * w if wl.dim == 3 else 0.0))
+            m = float(sp.max())
+            if m > 0:
+                u /= m
+                v /= m
+                w /= m
+        if wl.dim == 2:
+            w = None
+    wrap = lambda a: None if a is None else np.ascontiguousarray(np.pad(a, 3, mode="wrap"))
+    return wrap(G), wrap(u), wrap(v), wrap(w)
+
+
+def to_device_desc(wl: Workload, normalise: bool = True):
+    """The lsgb_synth descriptor of the workload (device generator)."""
+    from . import Synth, MAX_MODES
+
+    d = Synth()
+    for q in range(3):
+        d.center[q] = wl.center[q] if q < len(wl.center) else 0.0
+    d.r0 = wl.r0
+    if len(wl.shape_l) > MAX_MODES or len(wl.vel_k) > MAX_MODES:
+        raise ValueError("too many modes")
+    d.n_shape_modes = len(wl.shape_l)
+    for q, (l, m, a) in enumerate(zip(wl.shape_l, wl.shape_m, wl.shape_amp)):
+        d.shape_l[q], d.shape_m[q], d.shape_amp[q] = l, m, a
+    if wl.uniform_velocity is not None:
+        # a single k = 0 mode with phase 0 gives cos(0) = 1 times c
+        d.n_vel_modes = 1
+        d.vel_c[0][0], d.vel_c[0][1], d.vel_c[0][2] = wl.uniform_velocity[0], wl.uniform_velocity[1], 0.0
+        d.vel_scale = 1.0
+        return d
+    d.n_vel_modes = len(wl.vel_k)
+    for q, (k, c, ph) in enumerate(zip(wl.vel_k, wl.vel_c, wl.vel_phase)):
+        for a in range(3):
+            d.vel_k[q][a] = k[a]
+            d.vel_c[q][a] = c[a]
+        d.vel_phase[q] = ph
+    d.vel_scale = 0.0 if normalise else 1.0
+    return d
+
+
+def cfl_dt(wl: Workload, u, v, w, cfl: float, epsilon: float = 1e-10) -> float:
+    """CFL step from the field max of |u|+|v|+|w| (calculateTimeStep form,
+    Local_code/level-set_MPI_3D/include/config.h:272-293)."""
+    sl = (slice(3, -3),) * wl.dim
+    s = np.abs(u[sl]) + np.abs(v[sl])
+    if wl.dim == 3:
+        s = s + np.abs(w[sl])
+    speed = float(s.max()) + wl.s_l
+    if speed < epsilon:
+        speed = 2.0
+    return cfl * min(wl.spacing) / speed

@@ -1,0 +1,97 @@
+"""Regenerates the golden fixtures in this folder from the reference itself.
+
+Runs the reference's own CPU solver headers (Local_code/level-set_MPI_{2D,3D}/
+include, compiled unmodified into oracle/_ref by oracle/build_ref.sh) on small
+seeded inputs and stores inputs and outputs.  Needs the reference tree (the
+default location or LSGB_REFERENCE_ROOT); the GPU tests only read the .npz /
+.json files written here.
+
+    python tests/golden/make_golden.py
+"""
+import json
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "level-set-method-code_gb300"))
+
+from oracle import Oracle, Problem, build_ref  # noqa: E402
+from lsgb import synthetic as syn  # noqa: E402
+
+
+def small_inputs(pb: Problem, seed: int):
+    """Perturbed sphere/circle SDF with random per-cell velocity (both upwind
+    branches everywhere), ghosts left as the reference's BC makes them."""
+    rng = np.random.default_rng(seed)
+    shp = pb.shape
+    n = (pb.nz, pb.ny, pb.nx) if pb.dim == 3 else (pb.ny, pb.nx)
+    axes = [(np.arange(s) - 3) / q for s, q in zip(shp, n)]
+    grids = np.meshgrid(*axes, indexing="ij")
+    r2 = sum((g - 0.47) ** 2 for g in grids)
+    G = np.sqrt(r2) - 0.31 + 0.01 * rng.standard_normal(shp)
+    vel = [0.7 * rng.standard_normal(shp) + 0.2 for _ in range(pb.dim)]
+    return [np.ascontiguousarray(a) for a in (G, *vel)]
+
+
+def main():
+    if not build_ref():
+        sys.exit("reference tree not found")
+    ref = Oracle("ref")
+    out = {}
+
+    # 3D: one RK3 step, one reinit, a 10-step run with reinit every 3 steps
+    pb3 = Problem(nx=12, ny=10, nz=8, dim=3, s_l=0.15, dt=2e-3, enable_reinit=True,
+                  reinit_interval=3, reinit_iterations=3)
+    G, u, v, w = small_inputs(pb3, syn.seed_for(90))
+    phi, phi0, rt, flag = ref.reinit(pb3, G)
+    run = ref.run(pb3, 10, G, u, v, w)
+    np.savez_compressed(os.path.join(HERE, "golden_3d_small.npz"),
+                        G=G, u=u, v=v, w=w, dt=pb3.dt, s_l=pb3.s_l,
+                        rk3=ref.rk3_step(pb3, G, u, v, w),
+                        rk3_sl0=ref.rk3_step(Problem(**{**pb3.__dict__, "s_l": 0.0}), G, u, v, w),
+                        reinit_phi=phi, reinit_phi0=phi0, reinit_rt=rt, reinit_flag=flag,
+                        run10=run, vol_run10=ref.volume(pb3, run), l2_run10=ref.l2(pb3, run, G))
+
+    # 2D, periodic Y and zero-gradient Y
+    for tag, per in (("periodic", True), ("zerograd", False)):
+        pb2 = Problem(nx=14, ny=11, dim=2, s_l=0.1, dt=2e-3, enable_reinit=True,
+                      reinit_interval=2, reinit_iterations=2, periodic_y=per)
+        G, u, v = small_inputs(pb2, syn.seed_for(91, int(per)))
+        phi, phi0, rt, flag = ref.reinit(pb2, G)
+        run = ref.run(pb2, 9, G, u, v)
+        np.savez_compressed(os.path.join(HERE, f"golden_2d_{tag}.npz"),
+                            G=G, u=u, v=v, dt=pb2.dt, s_l=pb2.s_l,
+                            rk3=ref.rk3_step(pb2, G, u, v),
+                            reinit_phi=phi, reinit_phi0=phi0, reinit_rt=rt, reinit_flag=flag,
+                            run9=run, area_run9=ref.volume(pb2, run), l2_run9=ref.l2(pb2, run, G))
+
+    # configuration 1: 2D 128^2 circle, u = (1, 0), S_L = 0.1, CFL 0.5,
+    # 400 steps, HCR-2 every 10 steps with 5 pseudo-steps
+    wl = syn.config1(128)
+    G, u, v, _ = syn.host_fields(wl)
+    dt = 0.5 * (1.0 / 128) / (1.0 + 0.0 + 0.1)
+    pb = Problem(nx=128, ny=128, dim=2, s_l=0.1, dt=dt, enable_reinit=True, reinit_interval=10,
+                 reinit_iterations=5, periodic_y=True)
+    fin = ref.run(pb, 400, G, u, v)
+    np.savez_compressed(os.path.join(HERE, "golden_config1_128.npz"),
+                        G_final=np.ascontiguousarray(fin[3:-3, 3:-3]), dt=dt,
+                        area0=ref.volume(pb, G), area_final=ref.volume(pb, fin),
+                        l2_final=ref.l2(pb, fin, G))
+
+    # the reference's default 3D case end to end (its committed log pins it)
+    l2, v0, v1, steps = ref.deformation_test()
+    out["deformation_64"] = {"l2": l2, "volume_initial": v0, "volume_final": v1, "steps": steps,
+                             "log_l2": "9.158634e-04", "log_volume_initial": "0.014165",
+                             "log_volume_final": "0.014245", "log_steps": 1501,
+                             "log_source": "Local_code/level-set_MPI_3D/log/simulation.log"}
+    with open(os.path.join(HERE, "golden_scalars.json"), "w") as f:
+        json.dump(out, f, indent=2)
+    print("golden fixtures written")
+
+
+if __name__ == "__main__":
+    main()
