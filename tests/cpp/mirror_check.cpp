@@ -59,6 +59,11 @@ int main(int argc, char** argv) {
         cudaMemcpy(dst[q], h.data(), b, cudaMemcpyHostToDevice);
     }
     try {
+        // initial boundary fill of G and the velocity (src/main.cpp:259-260)
+        lsgb::applyBoundaryConditions3D(G, sp);
+        lsgb::applyBoundaryConditions3D(u, sp);
+        lsgb::applyBoundaryConditions3D(v, sp);
+        lsgb::applyBoundaryConditions3D(w, sp);
         for (int step = 0; step < nsteps; ++step) {
             lsgb::rk3TimeStep3D(G, Gn, G1, G2, nullptr, u, v, w, sp);
             double* t = G; G = Gn; Gn = t;
