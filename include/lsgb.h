@@ -142,6 +142,25 @@ LSGB_API int lsgb_reinit_f64(const lsgb_params* p, double** phi, double** phi_tm
 LSGB_API int lsgb_volume_f64(const lsgb_params* p, const double* G, double* volume, int64_t* count,
                     void* stream);
 
+/* Allocation-free form of lsgb_volume_f64, for callers that must not have the
+ * library allocate device memory during the call: a host whose own pool
+ * already holds the device, or a monitoring hook inside the caller's time
+ * loop that may not block in the allocator.  No counterpart in the reference.
+ * Same results as lsgb_volume_f64 (exact count, volume = count * cell volume).
+ * Its scratch is one fixed device array inside the library (512 KiB, kept by
+ * every GPU that loads the library until the process exits):
+ *   - at most LSGB_NOALLOC_MAX_CELLS interior cells (2^30, e.g. 1024^3) per
+ *     call; larger grids return LSGB_ERR_INVALID;
+ *   - the first call on a device looks the array's address up; make that
+ *     first call before any stream capture;
+ *   - all calls share the array: calls that overlap on the GPU race.
+ * Synchronises the stream.  Calls no cudaMalloc / cudaFree. */
+#define LSGB_NOALLOC_CHUNK 16384
+#define LSGB_NOALLOC_MAX_PARTIALS 65536
+#define LSGB_NOALLOC_MAX_CELLS ((long long)LSGB_NOALLOC_CHUNK * LSGB_NOALLOC_MAX_PARTIALS)
+LSGB_API int lsgb_volume_f64_noalloc(const lsgb_params* p, const double* G, double* volume,
+                                     int64_t* count, void* stream);
+
 /* sqrt(mean over interior of (G - G_ref)^2).  Replaces computeL2Error3D
  * (io.h:229-258) / computeL2Error (2D io.h:194-220).  Synchronises. */
 LSGB_API int lsgb_l2_error_f64(const lsgb_params* p, const double* G, const double* G_ref, double* l2,

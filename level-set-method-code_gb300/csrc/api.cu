@@ -275,6 +275,22 @@ extern "C" int lsgb_volume_f64(const lsgb_params* p, const double* G, double* vo
     return LSGB_OK;
 }
 
+extern "C" int lsgb_volume_f64_noalloc(const lsgb_params* p, const double* G, double* volume,
+                                       int64_t* count, void* stream) {
+    LSGB_TRY(check_params(p));
+    Geo g = geo_of(*p);
+    if (g.cells() > LSGB_NOALLOC_MAX_CELLS)
+        return fail(LSGB_ERR_INVALID,
+                    "grid has %lld interior cells; lsgb_volume_f64_noalloc accepts at most %lld "
+                    "(use lsgb_volume_f64)", g.cells(), (long long)LSGB_NOALLOC_MAX_CELLS);
+    LSGB_TRY(check_dev(G, "G"));
+    double cnt = 0.0;
+    LSGB_CUDA(noalloc_count_negative_f64(g, ghosted_layout(g), G, &cnt, (cudaStream_t)stream));
+    if (count) *count = (int64_t)cnt;
+    if (volume) *volume = cnt * cell_volume(*p);
+    return LSGB_OK;
+}
+
 extern "C" int lsgb_l2_error_f64(const lsgb_params* p, const double* G, const double* G_ref,
                                  double* l2, void* stream) {
     LSGB_TRY(check_params(p));

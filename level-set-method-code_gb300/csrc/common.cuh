@@ -152,6 +152,11 @@ cudaError_t launch_deformation(const Geo& g, double dx, double dy, double dz, do
                                void* u, void* v, void* w, bool f32, cudaStream_t st);
 cudaError_t launch_scale3(long long n, double s, double* u, double* v, double* w, cudaStream_t st);
 
+// Allocation-free interior G < 0 count (noalloc.cu); writes the host double
+// *count and synchronises st.  Grid size screened by the caller.
+cudaError_t noalloc_count_negative_f64(const Geo& g, const Lay& lay, const double* G, double* count,
+                                       cudaStream_t st);
+
 // Bookkeeping of kernel launches (lsgb_launch_count).
 void count_launches(uint64_t n);
 
