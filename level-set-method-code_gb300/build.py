@@ -27,7 +27,7 @@ COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler",
 EXTRA = {
     "f64_kernels.cu": ["--fmad=false"],
 }
-SOURCES = ["api.cu", "f64_kernels.cu", "f32_kernels.cu", "reduce.cu", "synth.cu", "noalloc.cu"]
+SOURCES = ["api.cu", "f64_kernels.cu", "f32_kernels.cu", "reduce.cu", "synth.cu", "noalloc.cu", "stage3d_f32.cu"]
 
 
 def _nvcc() -> str:

@@ -104,6 +104,7 @@ cudaError_t launch_reinit_step_stored_f64(const Geo& g, const Lay& lay, const do
 
 cudaError_t launch_stage_f64(const StageArgs& a, cudaStream_t st);
 cudaError_t launch_stage_f32(const StageArgs& a, cudaStream_t st);
+cudaError_t launch_stage3d_f32_tiled(const StageArgs& a, cudaStream_t st);
 cudaError_t launch_reinit_f64(const ReinitArgs& a, cudaStream_t st);
 cudaError_t launch_reinit_f32(const ReinitArgs& a, cudaStream_t st);
 

@@ -179,18 +179,23 @@ __global__ void __launch_bounds__(256) reinit_f32_kernel(Geo g, const float* __r
     }
     const float term = -S * (sqrtf(gsq) - 1.0f);
 
-    // interface constraint, FP64
+    // interface constraint.  The crossing test phi0_c * phi0_nb < 0 of
+    // computeInterfaceCrossings3D is a sign test: the exact product of two
+    // floats is never rounded to zero in FP64, so comparing signs in FP32
+    // decides it identically; only flagged cells go on to FP64 arithmetic.
     int flag = 0;
-    double sum0 = 0.0;
-    int cnt = 0;
 #pragma unroll
-    for (int q = 0; q < 2 * DIM; ++q) {
-        if ((double)ph0 * (double)p0[q] < 0.0) { sum0 += (double)p0[q]; cnt++; flag |= 1 << q; }
-    }
+    for (int q = 0; q < 2 * DIM; ++q)
+        if ((ph0 < 0.0f && p0[q] > 0.0f) || (ph0 > 0.0f && p0[q] < 0.0f)) flag |= 1 << q;
     float out;
     bool forced = false;
     double outd = 0.0;
     if (flag != 0) {
+        double sum0 = 0.0;
+        int cnt = 0;
+#pragma unroll
+        for (int q = 0; q < 2 * DIM; ++q)
+            if ((flag >> q) & 1) { sum0 += (double)p0[q]; cnt++; }
         bool stable = (phi > 0.0f) == (ph0 > 0.0f);
 #pragma unroll
         for (int q = 0; q < 2 * DIM; ++q)
@@ -238,11 +243,8 @@ cudaError_t launch_stage_f32(const StageArgs& a, cudaStream_t st) {
     const float* w = (const float*)a.w;
     const float* sl = (const float*)a.sl;
 #define LSGB_S32(D, S) stage_f32_kernel<D, S><<<gr, b, 0, st>>>(a.g, Gin, Gn, Gout, u, v, w, sl, c)
-    if (a.g.dim == 3) {
-        if (a.stage == 1) LSGB_S32(3, 1); else if (a.stage == 2) LSGB_S32(3, 2); else LSGB_S32(3, 3);
-    } else {
-        if (a.stage == 1) LSGB_S32(2, 1); else if (a.stage == 2) LSGB_S32(2, 2); else LSGB_S32(2, 3);
-    }
+    if (a.g.dim == 3) return launch_stage3d_f32_tiled(a, st);
+    if (a.stage == 1) LSGB_S32(2, 1); else if (a.stage == 2) LSGB_S32(2, 2); else LSGB_S32(2, 3);
 #undef LSGB_S32
     count_launches(1);
     return cudaGetLastError();
