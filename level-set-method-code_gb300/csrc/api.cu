@@ -361,6 +361,17 @@ namespace {
 
 size_t nbytes(const lsgb_solver* s) { return s->esz * (size_t)s->g.cells(); }
 
+// Device flag (one int after the reduction slots) that kernels with bounded
+// waits set when a wait gives up; cleared when reported.
+int* err_flag(lsgb_solver* s) { return (int*)(s->scratch + 2 * (RED_BLOCKS + 1) + 2); }
+
+int flag_result(lsgb_solver* s, int flag) {
+    if (!flag) return LSGB_OK;
+    cudaMemsetAsync(err_flag(s), 0, sizeof(int), s->st);
+    return fail(LSGB_ERR_CUDA, "a bounded in-kernel wait gave up (bulk copy did not arrive); results of the "
+                               "last steps are not valid");
+}
+
 int ensure_stage(lsgb_solver* s) {
     if (s->stage64) return LSGB_OK;
     size_t b = sizeof(double) * (size_t)layout_elems(s->g, 1);
@@ -435,6 +446,7 @@ int launch_stage(lsgb_solver* s, const StageArgs& a) {
 int rk3_step(lsgb_solver* s) {
     StageArgs a = stage_args(s->p, s->g, s->lay);
     a.u = s->u; a.v = s->v; a.w = s->w; a.sl = s->sl;
+    a.err = err_flag(s);
     a.Gn = s->G;
     a.Gin = s->G; a.Gout = s->A; a.stage = 1;
     LSGB_TRY(launch_stage(s, a));
@@ -481,13 +493,21 @@ int reinit(lsgb_solver* s) {
     return LSGB_OK;
 }
 
+// Reads the two result slots and the in-kernel error flag (synchronises).
 int reduce_read(lsgb_solver* s, double* r2) {
-    LSGB_CUDA(cudaMemcpyAsync(s->h_res, s->scratch + 2 * (RED_BLOCKS + 1), 2 * sizeof(double),
+    LSGB_CUDA(cudaMemcpyAsync(s->h_res, s->scratch + 2 * (RED_BLOCKS + 1), 3 * sizeof(double),
                               cudaMemcpyDeviceToHost, s->st));
     LSGB_CUDA(cudaStreamSynchronize(s->st));
     r2[0] = s->h_res[0];
     r2[1] = s->h_res[1];
-    return LSGB_OK;
+    return flag_result(s, ((const int*)(s->h_res + 2))[0]);
+}
+
+// The flag alone (after a synchronising call that did not read it).
+int check_flag(lsgb_solver* s) {
+    LSGB_CUDA(cudaMemcpyAsync(s->h_res + 2, err_flag(s), sizeof(int), cudaMemcpyDeviceToHost, s->st));
+    LSGB_CUDA(cudaStreamSynchronize(s->st));
+    return flag_result(s, ((const int*)(s->h_res + 2))[0]);
 }
 
 double* red_out(lsgb_solver* s) { return s->scratch + 2 * (RED_BLOCKS + 1); }
@@ -518,11 +538,13 @@ extern "C" int lsgb_solver_create(const lsgb_params* p, int precision, lsgb_solv
     void** fields[6] = {&s->G, &s->A, &s->B, &s->u, &s->v, &s->w};
     for (int q = 0; q < (s->p.dim == 3 ? 6 : 5) && rc == LSGB_OK; ++q) rc = alloc_field(s, fields[q]);
     if (rc == LSGB_OK) {
-        e = cudaMalloc((void**)&s->scratch, reduce_scratch_bytes() + 2 * sizeof(double));
+        e = cudaMalloc((void**)&s->scratch, reduce_scratch_bytes() + 4 * sizeof(double));
         if (e != cudaSuccess) rc = fail(LSGB_ERR_ALLOC, "scratch: %s", cudaGetErrorString(e));
+        else if ((e = cudaMemset(s->scratch, 0, reduce_scratch_bytes() + 4 * sizeof(double))) != cudaSuccess)
+            rc = fail(LSGB_ERR_CUDA, "scratch: %s", cudaGetErrorString(e));
     }
     if (rc == LSGB_OK) {
-        e = cudaMallocHost((void**)&s->h_res, 2 * sizeof(double));
+        e = cudaMallocHost((void**)&s->h_res, 4 * sizeof(double));
         if (e != cudaSuccess) rc = fail(LSGB_ERR_ALLOC, "pinned result slots: %s", cudaGetErrorString(e));
     }
     if (rc != LSGB_OK) {
@@ -625,6 +647,7 @@ extern "C" int lsgb_solver_get_G(lsgb_solver* s, double* G, int layout, int memo
         LSGB_CUDA(cudaMemcpyAsync(G, ddst, dbytes, cudaMemcpyDeviceToHost, s->st));
         LSGB_CUDA(cudaStreamSynchronize(s->st));
     }
+    LSGB_TRY(check_flag(s));
     return LSGB_OK;
 }
 

@@ -82,6 +82,7 @@ struct StageArgs {
     const void* sl;          // nullable per-cell flame speed (same layout)
     double s_l, eps, dx, dy, dz, dt;
     int stage;               // 1, 2, 3
+    int* err;                // nullable device error flag (bounded waits)
 };
 
 // HCR-2 pseudo-step arguments (handle path: r~ and flags recomputed from phi0).
@@ -104,7 +105,8 @@ cudaError_t launch_reinit_step_stored_f64(const Geo& g, const Lay& lay, const do
 
 cudaError_t launch_stage_f64(const StageArgs& a, cudaStream_t st);
 cudaError_t launch_stage_f32(const StageArgs& a, cudaStream_t st);
-cudaError_t launch_stage3d_f32_tiled(const StageArgs& a, cudaStream_t st);
+// err: device flag set when a bounded in-kernel wait gives up (nullable: no TMA path)
+cudaError_t launch_stage3d_f32_tiled(const StageArgs& a, int* err, cudaStream_t st);
 cudaError_t launch_reinit_f64(const ReinitArgs& a, cudaStream_t st);
 cudaError_t launch_reinit_f32(const ReinitArgs& a, cudaStream_t st);
 

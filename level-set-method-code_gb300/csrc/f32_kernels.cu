@@ -243,7 +243,7 @@ cudaError_t launch_stage_f32(const StageArgs& a, cudaStream_t st) {
     const float* w = (const float*)a.w;
     const float* sl = (const float*)a.sl;
 #define LSGB_S32(D, S) stage_f32_kernel<D, S><<<gr, b, 0, st>>>(a.g, Gin, Gn, Gout, u, v, w, sl, c)
-    if (a.g.dim == 3) return launch_stage3d_f32_tiled(a, st);
+    if (a.g.dim == 3) return launch_stage3d_f32_tiled(a, a.err, st);
     if (a.stage == 1) LSGB_S32(2, 1); else if (a.stage == 2) LSGB_S32(2, 2); else LSGB_S32(2, 3);
 #undef LSGB_S32
     count_launches(1);

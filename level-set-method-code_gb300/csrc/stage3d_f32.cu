@@ -37,6 +37,12 @@
 // (R(i+1) - R(i)) / h otherwise.
 #include "common.cuh"
 
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include <cstring>
+#include <mutex>
+
 namespace lsgb {
 namespace {
 
@@ -54,10 +60,20 @@ constexpr int NFX = (TX + 1) * TY;
 constexpr int NFY = TX * (TY + 1);
 constexpr int RING = PW * PH - TX * TY;
 constexpr int RPT = (RING + NT - 1) / NT;
-constexpr int QXPT = (NQX + NT - 1) / NT;
-constexpr int QYPT = (NQY + NT - 1) / NT;
-constexpr int FXPT = (NFX + NT - 1) / NT;
-constexpr int FYPT = (NFY + NT - 1) / NT;
+constexpr int NQ = NQX + NQY;
+constexpr int NF = NFX + NFY;
+constexpr int QPT = (NQ + NT - 1) / NT;
+constexpr int FPT = (NF + NT - 1) / NT;
+constexpr int FROT = 96;        // face-task rotation (balances per-warp work)
+constexpr int MINB = 3;         // resident CTAs per SM the register budget targets
+constexpr int NSTAGE = 3;                // TMA pipeline depth (plane pairs in flight)
+constexpr int NFIELD = 5;                // u, v, w, G^n, S_L
+constexpr int FTILE = 2 * TY * TX;       // floats of one field tile (2 planes)
+constexpr long long WAIT_CYCLES = 2000000000LL;  // bounded mbarrier wait (~1 s of SM clock)
+
+struct TmaMaps {
+    CUtensorMap m[NFIELD];
+};
 
 struct Coef {
     float inv_dx, inv_dy, inv_dz, inv_2dx, inv_2dy, inv_2dz, s_l, eps, dt;
@@ -115,28 +131,73 @@ __device__ __forceinline__ int wrapg(int x, int n, int bc) {
     return x < 0 ? 0 : (x >= n ? n - 1 : x);
 }
 
-template <int STAGE>
-__global__ void __launch_bounds__(NT, 2)
+
+// ---- TMA / mbarrier primitives (PTX) ----------------------------------------
+__device__ __forceinline__ uint32_t saddr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* b, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(saddr(b)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* b, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(saddr(b)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_test(uint64_t* b, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(saddr(b)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Poll with a limit: returns false if the phase did not complete within
+// WAIT_CYCLES SM clocks (about a second).
+__device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t parity) {
+    if (mbar_test(b, parity)) return true;
+    const long long t0 = clock64();
+    while (!mbar_test(b, parity))
+        if (clock64() - t0 > WAIT_CYCLES) return false;
+    return true;
+}
+__device__ __forceinline__ void tma_load_3d(float* dst, const CUtensorMap* tm, int x, int y, int z, uint64_t* b) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];"
+        ::"r"(saddr(dst)), "l"(tm), "r"(x), "r"(y), "r"(z), "r"(saddr(b))
+        : "memory");
+}
+
+// IDX: element offsets (int when the field has < 2^31 cells).  TMA: stream
+// u, v, w, G^n and S_L through a NSTAGE-deep pipeline of bulk tensor copies
+// (one thread issues, mbarriers signal arrival); otherwise plain loads.
+template <int STAGE, bool TMA, typename IDX>
+__global__ void __launch_bounds__(NT, MINB)
 stage3d_f32_pair(Geo g, const float* __restrict__ Gin, const float* __restrict__ Gn,
                  float* __restrict__ Gout, const float* __restrict__ u, const float* __restrict__ v,
-                 const float* __restrict__ w, const float* __restrict__ sl, Coef c) {
+                 const float* __restrict__ w, const float* __restrict__ sl, Coef c,
+                 const __grid_constant__ TmaMaps tm, int* __restrict__ err) {
     __shared__ float2 P2[2][PH][PW];
-    __shared__ float2 QX[TY][QXW];
-    __shared__ float2 QY[QYH][TX];
-    __shared__ float2 FXL[TY][TX + 1], FXR[TY][TX + 1];
-    __shared__ float2 FYL[TY + 1][TX], FYR[TY + 1][TX];
+    __shared__ float2 QA[NQ];          // x-indicators [TY][QXW], then y-indicators [QYH][TX]
+    __shared__ float2 FL[NF], FR[NF];  // x-faces [TY][TX+1], then y-faces [TY+1][TX]
+    __shared__ IDX zoff[ZC + 10];
+    __shared__ __align__(8) uint64_t mbar[NSTAGE];
+    extern __shared__ __align__(128) float stg[];  // NSTAGE x NFIELD x FTILE (TMA only)
 
     const int tx = threadIdx.x, ty = threadIdx.y;
     const int t = ty * TX + tx;
     const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY;
     const int z0 = blockIdx.z * ZC;
     const int z1 = min(z0 + ZC, g.nz);
-    const long long sz = (long long)g.nx * g.ny;
+    const int niter = (z1 - z0 + 1) / 2;
+    const IDX sz = (IDX)g.nx * g.ny;
     const bool valid = (i0 + tx) < g.nx && (j0 + ty) < g.ny;
-    const int col = wrapg(j0 + ty, g.ny, g.bcy) * g.nx + wrapg(i0 + tx, g.nx, g.bcx);
+    const IDX col = (IDX)wrapg(j0 + ty, g.ny, g.bcy) * g.nx + wrapg(i0 + tx, g.nx, g.bcx);
+    const bool has_sl = sl != nullptr;
 
     // ---- fixed per-thread task tables (offsets into one staged plane) ----
-    int ring_s[RPT], ring_g[RPT];
+    // halo ring of the staged plane pair: 3 full rows above and below, 3 cells
+    // left and right of each tile row
+    int ring_s[RPT];
+    IDX ring_g[RPT];
 #pragma unroll
     for (int r = 0; r < RPT; ++r) {
         const int q = t + r * NT;
@@ -151,51 +212,83 @@ stage3d_f32_pair(Geo g, const float* __restrict__ Gin, const float* __restrict__
             lx = s < 3 ? s : TX + s;
         }
         ring_s[r] = q < RING ? ly * PW + lx : -1;
-        ring_g[r] = q < RING ? wrapg(j0 + ly - 3, g.ny, g.bcy) * g.nx + wrapg(i0 + lx - 3, g.nx, g.bcx) : 0;
+        ring_g[r] = q < RING ? (IDX)wrapg(j0 + ly - 3, g.ny, g.bcy) * g.nx + wrapg(i0 + lx - 3, g.nx, g.bcx) : 0;
     }
-    int qx_src[QXPT], qy_src[QYPT], fx_src[FXPT], fy_src[FYPT];
+    // Indicator tasks: x-indicators of tile cells x in [-2, TX+1] (NQX), then
+    // y-indicators of tile cells y in [-2, TY+1] (NQY), one list so every warp
+    // carries 2 or 3 tasks.  Encoded: sample offset | (y-axis << 30).
+    int q_src[QPT], q_dst[QPT];
 #pragma unroll
-    for (int r = 0; r < QXPT; ++r) {  // x-indicator of tile cell (cx-2, row): samples P2[row+3][cx..cx+2]
-        const int q = t + r * NT, row = q / QXW, cx = q % QXW;
-        qx_src[r] = q < NQX ? (row + 3) * PW + cx : -1;
+    for (int r = 0; r < QPT; ++r) {
+        const int q = t + r * NT;
+        q_dst[r] = q < NQ ? q : -1;
+        if (q < NQX) {
+            const int row = q / QXW, cx = q % QXW;
+            q_src[r] = (row + 3) * PW + cx;                  // P2[row+3][cx..cx+2]
+        } else {
+            const int qq = q - NQX, cy = qq / TX, cl = qq % TX;
+            q_src[r] = (cy * PW + cl + 3) | (1 << 30);       // P2[cy..cy+2][cl+3]
+        }
     }
+    // Face tasks: x-faces (NFX) then y-faces (NFY), rotated so that the warps
+    // with a third face task are not the ones with a third indicator task.
+    int f_src[FPT], f_q[FPT], f_dst[FPT];
 #pragma unroll
-    for (int r = 0; r < QYPT; ++r) {  // y-indicator of tile cell (col, cy-2): samples P2[cy..cy+2][col+3]
-        const int q = t + r * NT, cy = q / TX, cl = q % TX;
-        qy_src[r] = q < NQY ? cy * PW + cl + 3 : -1;
-    }
-#pragma unroll
-    for (int r = 0; r < FXPT; ++r) {  // x-face f in row: samples P2[row+3][f..f+5], QX[row][f..f+3]
-        const int q = t + r * NT, row = q / (TX + 1), f = q % (TX + 1);
-        fx_src[r] = q < NFX ? row * 65536 + f : -1;
-    }
-#pragma unroll
-    for (int r = 0; r < FYPT; ++r) {  // y-face between rows rr-1, rr: P2[rr..rr+5][cl+3], QY[rr..rr+3][cl]
-        const int q = t + r * NT, rr = q / TX, cl = q % TX;
-        fy_src[r] = q < NFY ? rr * 65536 + cl : -1;
+    for (int r = 0; r < FPT; ++r) {
+        const int f = ((t + FROT) % NT) + r * NT;
+        f_dst[r] = f < NF ? f : -1;
+        if (f < NFX) {
+            const int row = f / (TX + 1), fc = f % (TX + 1);
+            f_src[r] = (row + 3) * PW + fc;                  // P2[row+3][fc..fc+5]
+            f_q[r] = row * QXW + fc;                         // QA[row][fc..fc+3]
+        } else {
+            const int ff = f - NFX, rr = ff / TX, cl = ff % TX;
+            f_src[r] = (rr * PW + cl + 3) | (1 << 30);       // P2[rr..rr+5][cl+3]
+            f_q[r] = NQX + rr * TX + cl;                     // QY[rr..rr+3][cl]
+        }
     }
 
-    // plane offset of z-index k, k in [z0 - 3, z1 + 6): the wrap needs no
-    // integer division (one conditional add / subtract per chunk edge)
-    auto plane = [&](int k) -> long long {
-        int kk = k;
+    // plane offsets of z-indices z0-3 .. z1+6 (periodic wrap or clamp), one
+    // table per CTA so the loop does no index arithmetic on z
+    for (int d = t; d < ZC + 10; d += NT) {
+        int kk = z0 - 3 + d;
         if (g.bcz == LSGB_BC_PERIODIC) {
             while (kk < 0) kk += g.nz;
             while (kk >= g.nz) kk -= g.nz;
         } else {
             kk = kk < 0 ? 0 : (kk >= g.nz ? g.nz - 1 : kk);
         }
-        return (long long)kk * sz;
+        zoff[d] = (IDX)kk * sz;
+    }
+
+    // ---- TMA pipeline prologue ----
+    auto issue = [&](int it) {
+        const int s = it % NSTAGE;
+        const int kz = z0 + 2 * it;
+        float* base = stg + s * NFIELD * FTILE;
+        const uint32_t nf = 3 + (STAGE > 1 ? 1 : 0) + (has_sl ? 1 : 0);
+        mbar_expect_tx(&mbar[s], nf * FTILE * 4);
+        tma_load_3d(base + 0 * FTILE, &tm.m[0], i0, j0, kz, &mbar[s]);
+        tma_load_3d(base + 1 * FTILE, &tm.m[1], i0, j0, kz, &mbar[s]);
+        tma_load_3d(base + 2 * FTILE, &tm.m[2], i0, j0, kz, &mbar[s]);
+        if (STAGE > 1) tma_load_3d(base + 3 * FTILE, &tm.m[3], i0, j0, kz, &mbar[s]);
+        if (has_sl) tma_load_3d(base + 4 * FTILE, &tm.m[4], i0, j0, kz, &mbar[s]);
     };
+    if (TMA && t == 0) {
+        for (int s = 0; s < NSTAGE; ++s) mbar_init(&mbar[s], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();  // zoff table and barriers ready
+    if (TMA && t == 0)
+        for (int it = 0; it < NSTAGE - 1 && it < niter; ++it) issue(it);
 
     // ---- z queues: G(k-3 .. k+4) and q_z(k-1 .. k+1) of the own column ----
     float zq[8];
 #pragma unroll
-    for (int d = 0; d < 8; ++d) zq[d] = __ldg(Gin + plane(z0 - 3 + d) + col);
-    // indicators at k-1, k, k+1 (triples centred there)
+    for (int d = 0; d < 8; ++d) zq[d] = __ldg(Gin + zoff[d] + col);
     float2 qz_a = qbeta(make_float2(zq[1], zq[2]), make_float2(zq[2], zq[3]), make_float2(zq[3], zq[4]));  // (q(k-1), q(k))
     float qz_k1 = qbeta(make_float2(zq[3], zq[3]), make_float2(zq[4], zq[4]), make_float2(zq[5], zq[5])).x;  // q(k+1)
-    float qz_m2 = qbeta(make_float2(zq[0], zq[0]), make_float2(zq[1], zq[1]), make_float2(zq[2], zq[2])).x;  // q(k-2)
+    const float qz_m2 = qbeta(make_float2(zq[0], zq[0]), make_float2(zq[1], zq[1]), make_float2(zq[2], zq[2])).x;  // q(k-2)
     // face k-1/2 (between k-1 and k): samples G(k-3..k+2), q(k-2), q(k-1), q(k), q(k+1)
     float zprevL, zprevR;
     {
@@ -206,82 +299,86 @@ stage3d_f32_pair(Geo g, const float* __restrict__ Gin, const float* __restrict__
         zprevR = R.x;
     }
     float2 ring_v[RPT];
-    {
-        const long long pa = plane(z0), pb = plane(z0 + 1);
 #pragma unroll
-        for (int r = 0; r < RPT; ++r)
-            ring_v[r] = ring_s[r] >= 0 ? make_float2(__ldg(Gin + pa + ring_g[r]), __ldg(Gin + pb + ring_g[r]))
-                                       : make_float2(0.0f, 0.0f);
-    }
+    for (int r = 0; r < RPT; ++r)
+        ring_v[r] = ring_s[r] >= 0 ? make_float2(__ldg(Gin + zoff[3] + ring_g[r]), __ldg(Gin + zoff[4] + ring_g[r]))
+                                   : make_float2(0.0f, 0.0f);
 
     int buf = 0;
-    for (int k = z0; k < z1; k += 2) {
+    for (int it = 0; it < niter; ++it) {
+        const int k = z0 + 2 * it;
+        const IDX* zo = zoff + 2 * it + 3;  // zo[d] = offset of plane k + d
         float2* P = &P2[buf][0][0];
         P[(ty + 3) * PW + tx + 3] = make_float2(zq[3], zq[4]);
 #pragma unroll
         for (int r = 0; r < RPT; ++r)
             if (ring_s[r] >= 0) P[ring_s[r]] = ring_v[r];
 
-        // loads for this pair's update and the next pair's staging
-        const long long oa = (long long)k * sz + col;
-        const long long ob = plane(k + 1) + col;
-        const float2 uu = make_float2(__ldg(u + oa), __ldg(u + ob));
-        const float2 vv = make_float2(__ldg(v + oa), __ldg(v + ob));
-        const float2 ww = make_float2(__ldg(w + oa), __ldg(w + ob));
-        float2 gn = c2(0.0f);
-        if (STAGE > 1) gn = make_float2(__ldg(Gn + oa), __ldg(Gn + ob));
-        float2 s_l = c2(c.s_l);
-        if (sl) s_l = make_float2(__ldg(sl + oa), __ldg(sl + ob));
-        const float zn0 = __ldg(Gin + plane(k + 5) + col);
-        const float zn1 = __ldg(Gin + plane(k + 6) + col);
-        if (k + 2 < z1) {
-            const long long na = plane(k + 2), nb = plane(k + 3);
+        // loads for this pair's update (plain path) and the next pair's staging
+        const IDX oa = zo[0] + col;
+        const IDX ob = zo[1] + col;
+        float2 uu, vv, ww, gn = c2(0.0f), s_l = c2(c.s_l);
+        if (!TMA) {
+            uu = make_float2(__ldg(u + oa), __ldg(u + ob));
+            vv = make_float2(__ldg(v + oa), __ldg(v + ob));
+            ww = make_float2(__ldg(w + oa), __ldg(w + ob));
+            if (STAGE > 1) gn = make_float2(__ldg(Gn + oa), __ldg(Gn + ob));
+            if (has_sl) s_l = make_float2(__ldg(sl + oa), __ldg(sl + ob));
+        }
+        const float zn0 = __ldg(Gin + zo[5] + col);
+        const float zn1 = __ldg(Gin + zo[6] + col);
+        if (it + 1 < niter) {
+            const IDX na = zo[2], nb = zo[3];
 #pragma unroll
             for (int r = 0; r < RPT; ++r)
                 if (ring_s[r] >= 0) ring_v[r] = make_float2(__ldg(Gin + na + ring_g[r]), __ldg(Gin + nb + ring_g[r]));
         }
         __syncthreads();
+        if (TMA && t == 0 && it + NSTAGE - 1 < niter) {
+            // the stage being refilled was last read in iteration it-1, which
+            // every thread finished before the barrier above
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            issue(it + NSTAGE - 1);
+        }
 
         // ---- per-cell indicators (x, y in shared memory; z in registers) ----
 #pragma unroll
-        for (int r = 0; r < QXPT; ++r)
-            if (qx_src[r] >= 0) {
-                const float2* s = P + qx_src[r];
-                (&QX[0][0])[t + r * NT] = qbeta(s[0], s[1], s[2]);
-            }
-#pragma unroll
-        for (int r = 0; r < QYPT; ++r)
-            if (qy_src[r] >= 0) {
-                const float2* s = P + qy_src[r];
-                (&QY[0][0])[t + r * NT] = qbeta(s[0], s[PW], s[2 * PW]);
+        for (int r = 0; r < QPT; ++r)
+            if (q_dst[r] >= 0) {
+                const int st = (q_src[r] >> 30) ? PW : 1;
+                const float2* s = P + (q_src[r] & 0x3fffffff);
+                QA[q_dst[r]] = qbeta(s[0], s[st], s[2 * st]);
             }
         // q_z(k+2), q_z(k+3): triples centred at k+2 and k+3
         const float2 qz_b = qbeta(make_float2(zq[4], zq[5]), make_float2(zq[5], zq[6]), make_float2(zq[6], zq[7]));
-        __syncthreads();
+        if (TMA) {
+            const bool ok = mbar_wait(&mbar[it % NSTAGE], (uint32_t)((it / NSTAGE) & 1));
+            if (__syncthreads_or(!ok)) {
+                // a bulk copy did not arrive in time: flag it, give the copies
+                // still in flight a bounded chance to land, and leave
+                if (t == 0) {
+                    atomicExch(err, 1);
+                    for (int j = it; j < niter && j < it + NSTAGE; ++j)
+                        mbar_wait(&mbar[j % NSTAGE], (uint32_t)((j / NSTAGE) & 1));
+                }
+                return;
+            }
+        } else {
+            __syncthreads();
+        }
 
         // ---- faces ----
 #pragma unroll
-        for (int r = 0; r < FXPT; ++r)
-            if (fx_src[r] >= 0) {
-                const int row = fx_src[r] >> 16, f = fx_src[r] & 0xffff;
-                const float2* s = P + (row + 3) * PW + f;
-                const float2* q = &QX[row][f];
+        for (int r = 0; r < FPT; ++r)
+            if (f_dst[r] >= 0) {
+                const bool yf = f_src[r] >> 30;
+                const int st = yf ? PW : 1, qs = yf ? TX : 1;
+                const float2* s = P + (f_src[r] & 0x3fffffff);
+                const float2* q = QA + f_q[r];
                 float2 L, R;
-                face(s[0], s[1], s[2], s[3], s[4], s[5], q[0], q[1], q[2], q[3], L, R);
-                FXL[row][f] = L;
-                FXR[row][f] = R;
-            }
-#pragma unroll
-        for (int r = 0; r < FYPT; ++r)
-            if (fy_src[r] >= 0) {
-                const int rr = fy_src[r] >> 16, cl = fy_src[r] & 0xffff;
-                const float2* s = P + rr * PW + cl + 3;
-                const float2* q = &QY[rr][cl];
-                float2 L, R;
-                face(s[0], s[PW], s[2 * PW], s[3 * PW], s[4 * PW], s[5 * PW], q[0], q[TX], q[2 * TX],
-                     q[3 * TX], L, R);
-                FYL[rr][cl] = L;
-                FYR[rr][cl] = R;
+                face(s[0], s[st], s[2 * st], s[3 * st], s[4 * st], s[5 * st], q[0], q[qs], q[2 * qs], q[3 * qs], L, R);
+                FL[f_dst[r]] = L;
+                FR[f_dst[r]] = R;
             }
         // z faces k+1/2 and k+3/2 as one pair: samples G(k-2+m), G(k-1+m)
         float2 zL, zR;
@@ -292,6 +389,14 @@ stage3d_f32_pair(Geo g, const float* __restrict__ Gin, const float* __restrict__
         __syncthreads();
 
         // ---- cell update for planes k, k+1 ----
+        if (TMA) {
+            const float* sb = stg + (it % NSTAGE) * NFIELD * FTILE + ty * TX + tx;
+            uu = make_float2(sb[0 * FTILE], sb[0 * FTILE + TX * TY]);
+            vv = make_float2(sb[1 * FTILE], sb[1 * FTILE + TX * TY]);
+            ww = make_float2(sb[2 * FTILE], sb[2 * FTILE + TX * TY]);
+            if (STAGE > 1) gn = make_float2(sb[3 * FTILE], sb[3 * FTILE + TX * TY]);
+            if (has_sl) s_l = make_float2(sb[4 * FTILE], sb[4 * FTILE + TX * TY]);
+        }
         const float2* ctr = P + (ty + 3) * PW + tx + 3;
         const float2 gc = ctr[0];
         float2 ue = uu, ve = vv, we = ww;
@@ -300,17 +405,17 @@ stage3d_f32_pair(Geo g, const float* __restrict__ Gin, const float* __restrict__
             const float2 gy = mul2(sub2(ctr[PW], ctr[-PW]), c2(c.inv_2dy));
             const float2 gz = mul2(make_float2(zq[4] - zq[2], zq[5] - zq[3]), c2(c.inv_2dz));
             const float2 sq = fma2(gx, gx, fma2(gy, gy, fma2(gz, gz, c2(c.eps))));
-            const float2 f = make_float2(s_l.x > c.eps ? s_l.x * rsqrtf(sq.x) : 0.0f,
-                                         s_l.y > c.eps ? s_l.y * rsqrtf(sq.y) : 0.0f);
-            const float2 nf = mul2(f, c2(-1.0f));
-            ue = fma2(nf, gx, ue);
-            ve = fma2(nf, gy, ve);
-            we = fma2(nf, gz, we);
+            const float2 f = make_float2(s_l.x > c.eps ? -s_l.x * rsqrtf(sq.x) : 0.0f,
+                                         s_l.y > c.eps ? -s_l.y * rsqrtf(sq.y) : 0.0f);
+            ue = fma2(f, gx, ue);
+            ve = fma2(f, gy, ve);
+            we = fma2(f, gz, we);
         }
-        const float2 dxL = sub2(FXL[ty][tx + 1], FXL[ty][tx]);
-        const float2 dxR = sub2(FXR[ty][tx + 1], FXR[ty][tx]);
-        const float2 dyL = sub2(FYL[ty + 1][tx], FYL[ty][tx]);
-        const float2 dyR = sub2(FYR[ty + 1][tx], FYR[ty][tx]);
+        const int xf = ty * (TX + 1) + tx, yfc = NFX + ty * TX + tx;
+        const float2 dxL = sub2(FL[xf + 1], FL[xf]);
+        const float2 dxR = sub2(FR[xf + 1], FR[xf]);
+        const float2 dyL = sub2(FL[yfc + TX], FL[yfc]);
+        const float2 dyR = sub2(FR[yfc + TX], FR[yfc]);
         // z: plane k uses faces (k-1/2, k+1/2) = (prev, zL.x); plane k+1 (zL.x, zL.y)
         const float2 dzL = sub2(zL, make_float2(zprevL, zL.x));
         const float2 dzR = sub2(zR, make_float2(zprevR, zR.x));
@@ -332,7 +437,6 @@ stage3d_f32_pair(Geo g, const float* __restrict__ Gin, const float* __restrict__
         for (int d = 0; d < 6; ++d) zq[d] = zq[d + 2];
         zq[6] = zn0;
         zq[7] = zn1;
-        qz_m2 = qz_a.y;                      // unused past the prologue; kept for clarity
         qz_a = make_float2(qz_k1, qz_b.x);   // (q(k+1), q(k+2)) -> new (q(k'-1), q(k'))
         qz_k1 = qz_b.y;                      // q(k+3) -> new q(k'+1)
         zprevL = zL.y;
@@ -341,9 +445,63 @@ stage3d_f32_pair(Geo g, const float* __restrict__ Gin, const float* __restrict__
     }
 }
 
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no -lcuda).
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+    });
+    return fn;
+}
+
+// 3D map over a compact FP32 field with a (32, 8, 2) box; zero fill outside.
+bool encode_field(CUtensorMap* m, const float* ptr, const Geo& g) {
+    PFN_cuTensorMapEncodeTiled_v12000 fn = encode_fn();
+    if (!fn || !ptr) return false;
+    cuuint64_t dims[3] = {(cuuint64_t)g.nx, (cuuint64_t)g.ny, (cuuint64_t)g.nz};
+    cuuint64_t strides[2] = {(cuuint64_t)g.nx * 4, (cuuint64_t)g.nx * g.ny * 4};
+    cuuint32_t box[3] = {TX, TY, 2};
+    cuuint32_t estr[3] = {1, 1, 1};
+    return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, (void*)ptr, dims, strides, box, estr,
+              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+template <int STAGE, bool TMA, typename IDX>
+cudaError_t launch_one(const StageArgs& a, const Coef& c, const TmaMaps& tm, int* err, cudaStream_t st) {
+    const dim3 block(TX, TY, 1);
+    const dim3 grid((a.g.nx + TX - 1) / TX, (a.g.ny + TY - 1) / TY, (a.g.nz + ZC - 1) / ZC);
+    const size_t dyn = TMA ? (size_t)NSTAGE * NFIELD * FTILE * sizeof(float) : 0;
+    auto kern = stage3d_f32_pair<STAGE, TMA, IDX>;
+    if (TMA) {
+        static bool attr_set = false;  // per instantiation
+        if (!attr_set) {
+            cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+            if (e != cudaSuccess) return e;
+            attr_set = true;
+        }
+    }
+    kern<<<grid, block, dyn, st>>>(a.g, (const float*)a.Gin, (const float*)a.Gn, (float*)a.Gout,
+                                    (const float*)a.u, (const float*)a.v, (const float*)a.w,
+                                    (const float*)a.sl, c, tm, err);
+    return cudaGetLastError();
+}
+
+template <bool TMA, typename IDX>
+cudaError_t launch_stage(const StageArgs& a, const Coef& c, const TmaMaps& tm, int* err, cudaStream_t st) {
+    if (a.stage == 1) return launch_one<1, TMA, IDX>(a, c, tm, err, st);
+    if (a.stage == 2) return launch_one<2, TMA, IDX>(a, c, tm, err, st);
+    return launch_one<3, TMA, IDX>(a, c, tm, err, st);
+}
+
 }  // namespace
 
-cudaError_t launch_stage3d_f32_tiled(const StageArgs& a, cudaStream_t st) {
+cudaError_t launch_stage3d_f32_tiled(const StageArgs& a, int* err, cudaStream_t st) {
     Coef c;
     c.inv_dx = (float)(1.0 / a.dx);
     c.inv_dy = (float)(1.0 / a.dy);
@@ -354,20 +512,19 @@ cudaError_t launch_stage3d_f32_tiled(const StageArgs& a, cudaStream_t st) {
     c.s_l = (float)a.s_l;
     c.eps = (float)a.eps;
     c.dt = (float)a.dt;
-    const dim3 block(TX, TY, 1);
-    const dim3 grid((a.g.nx + TX - 1) / TX, (a.g.ny + TY - 1) / TY, (a.g.nz + ZC - 1) / ZC);
-    const float* Gin = (const float*)a.Gin;
-    const float* Gn = (const float*)a.Gn;
-    float* Gout = (float*)a.Gout;
-    const float* u = (const float*)a.u;
-    const float* v = (const float*)a.v;
-    const float* w = (const float*)a.w;
-    const float* sl = (const float*)a.sl;
-    if (a.stage == 1) stage3d_f32_pair<1><<<grid, block, 0, st>>>(a.g, Gin, Gn, Gout, u, v, w, sl, c);
-    else if (a.stage == 2) stage3d_f32_pair<2><<<grid, block, 0, st>>>(a.g, Gin, Gn, Gout, u, v, w, sl, c);
-    else stage3d_f32_pair<3><<<grid, block, 0, st>>>(a.g, Gin, Gn, Gout, u, v, w, sl, c);
+    TmaMaps tm;
+    std::memset(&tm, 0, sizeof(tm));
+    // bulk tensor copies need 16-byte row pitch and an error flag to report into
+    bool tma = err != nullptr && (a.g.nx % 4) == 0;
+    const void* fields[NFIELD] = {a.u, a.v, a.w, a.stage > 1 ? a.Gn : nullptr, a.sl};
+    for (int f = 0; f < NFIELD && tma; ++f)
+        if (fields[f] && !encode_field(&tm.m[f], (const float*)fields[f], a.g)) tma = false;
+    const bool small = a.g.cells() < (1LL << 31) - 1;
+    cudaError_t e;
+    if (tma) e = small ? launch_stage<true, int>(a, c, tm, err, st) : launch_stage<true, long long>(a, c, tm, err, st);
+    else e = small ? launch_stage<false, int>(a, c, tm, err, st) : launch_stage<false, long long>(a, c, tm, err, st);
     count_launches(1);
-    return cudaGetLastError();
+    return e;
 }
 
 }  // namespace lsgb
