@@ -53,6 +53,9 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=2, help="timed end-to-end calls (0 = skip)")
     ap.add_argument("--e2e-rk-steps", type=int, default=50, help="RK3 steps per end-to-end call")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline sample length")
+    ap.add_argument("--batch-steps", type=int, default=200, help="RK3 steps of the batched form (0 = skip)")
+    ap.add_argument("--adjoint-steps", type=int, default=300, help="RK3 steps of the adjoint form (0 = skip)")
+    ap.add_argument("--adjoint-n", type=int, default=192)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--json-out", default=None)
     return ap.parse_args()
@@ -287,6 +290,90 @@ def run_reference(args, dist: Dist):
     print(json.dumps(line), flush=True)
 
 
+def measure_batched(torch, lsgb, syn, steps: int, dist: Dist):
+    """Configuration 4: 48 2D (64^2..1024^2) + 48 3D (32^3..192^3) instances,
+    FP32-bulk, HCR-2 every 5 steps, tiles from the autotuner, advanced together
+    with one captured CUDA graph per reinit period; `steps` RK3 steps timed
+    with CUDA events on the batch stream."""
+    wls = syn.config4()
+    cells = 0
+    with lsgb.Batch("f32", lanes=8) as b:
+        for wl in wls:
+            n = wl.n[0]
+            p = lsgb.params(wl.dim, n, n, n, s_l=wl.s_l, enable_reinit=True, reinit_interval=RK_PER_BENCH_STEP,
+                            reinit_iterations=REINIT_ITERS)
+            s = b.add(p)
+            s.synth(syn.to_device_desc(wl))
+            s.compute_dt(CFL)
+            cells += n ** wl.dim
+        t0 = time.perf_counter()
+        b.autotune()
+        tune_s = time.perf_counter() - t0
+        tiles = [s.get_tile() for s in b.instances]
+        b.advance(6)  # warm-up: direct step 0 + the captured period
+        b.sync()
+        stream = torch.cuda.ExternalStream(b.stream_handle())
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        n0 = lsgb.launch_count()
+        e0.record(stream)
+        b.advance(steps)
+        e1.record(stream)
+        b.sync()
+        ms = e0.elapsed_time(e1)
+        launches = lsgb.launch_count() - n0
+        replays, kernels = b.stats()
+    ms = dist.max(ms)
+    return {"value": dist.world * cells * steps / (ms * 1e-3) / 1e9, "unit": "Gcell-updates/s",
+            "instances": len(wls), "cells_per_step": cells, "rk3_steps": steps, "ms": ms,
+            "kernels_launched": launches, "graph_replays": replays, "kernels_per_graph": kernels,
+            "autotune_s": tune_s, "tiles_2d": sorted(set(t for t, w in zip(tiles, wls) if w.dim == 2)),
+            "tiles_3d": sorted(set(t for t, w in zip(tiles, wls) if w.dim == 3)),
+            "workload": "config4: 48 2D (64^2..1024^2) + 48 3D (32^3..192^3), FP32-bulk, reinit every 5"}
+
+
+def measure_adjoint(torch, lsgb, n: int, steps: int, dist: Dist):
+    """Configuration 5: gradient of the smoothed-Heaviside front mismatch with
+    respect to the per-cell flame speed S_L(x) at n^3 (FP32-bulk), through
+    the discrete adjoint with checkpoints every 20 steps.  Times one plain
+    forward of `steps` RK3 steps and the forward-with-checkpoints + loss +
+    backward, both with CUDA events on the solver's stream."""
+    import numpy as np
+    from lsgb import adjoint as adj
+    p, G0, u, v, w, sl, sl_t = adj.workload(n, steps)
+    stream = torch.cuda.Stream()
+    prob = adj.Problem(p, G0, u, v, w, "f32", checkpoint=20)
+    prob.s.set_stream(stream)
+    prob.target(sl_t, steps)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    prob.run(sl, steps)  # warm
+    prob.s.volume()
+    prob.run(sl, 0)
+    ev[0].record(stream)
+    prob.s.advance(steps)
+    ev[1].record(stream)
+    prob.s.volume()
+    prob.run(sl, 0)
+    n0 = lsgb.launch_count()
+    ev[2].record(stream)
+    prob.a.forward(steps)
+    loss = prob.a.loss(seed=True)
+    prob.a.backward()
+    ev[3].record(stream)
+    torch.cuda.synchronize()
+    launches = lsgb.launch_count() - n0
+    fwd_ms = dist.max(ev[0].elapsed_time(ev[1]))
+    adj_ms = dist.max(ev[2].elapsed_time(ev[3]))
+    g = prob.a.grad("sl")
+    prob.close()
+    cells = n ** 3
+    return {"value": dist.world * cells * steps / (adj_ms * 1e-3) / 1e9, "unit": "Gcell-updates/s (forward+backward)",
+            "forward_ms": fwd_ms, "forward_backward_ms": adj_ms, "adjoint_over_forward": adj_ms / fwd_ms,
+            "loss": loss, "grad_l2": float(np.linalg.norm(g)), "kernels_launched": launches,
+            "rk3_steps": steps, "checkpoint_interval": 20,
+            "workload": f"config5 {n}^3 periodic, FP32-bulk, S_L(x) = 0.15 + 0.05 f(x) (8 modes), "
+                        "reinit every 10, L = 1/2 sum (H(G_T) - H(G_target))^2 dV, eps = 1.5 dx"}
+
+
 def run_ours(args, dist: Dist):
     import numpy as np
     import torch
@@ -321,7 +408,7 @@ def run_ours(args, dist: Dist):
     traffic = load_traffic("f32", n)
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
-                "kernel": "stage_f32_kernel (fused WENO5 RHS + RK3 stage combine)",
+                "kernel": "stage3d_f32_pair (fused WENO5 RHS + RK3 stage combine, TMA-fed 2.5D tiles)",
                 "algorithmic_bytes_per_launch": cells * s_bytes * 17 / 3,
                 "launches": st_n, "avg_launch_ms": st_ms / max(st_n, 1)}
     step_bytes = cells * s_bytes * (17 + (4 + 5 * REINIT_ITERS) / RK_PER_BENCH_STEP)
@@ -385,6 +472,15 @@ def run_ours(args, dist: Dist):
 
     s32.close()
 
+    # --- batched form: 96 uneven 2D/3D instances, one CUDA graph per reinit period ---
+    batched = None
+    if args.batch_steps > 0:
+        batched = measure_batched(torch, lsgb, syn, args.batch_steps, dist)
+
+    adjoint = None
+    if args.adjoint_steps > 0:
+        adjoint = measure_adjoint(torch, lsgb, args.adjoint_n, args.adjoint_steps, dist)
+
     cpu = None
     if not args.no_cpu_baseline and dist.rank == 0 and dist.world == 1:
         rate, periods, el, threads, _ = cpu_sample(n, 16, args.cpu_seconds)
@@ -412,6 +508,8 @@ def run_ours(args, dist: Dist):
             "fp64": fp64,
             "precision_vs_fp64": prec,
             "reinit_avg_launch_ms": re_ms / max(re_n, 1),
+            "batched": batched,
+            "adjoint": adjoint,
         }
         s = json.dumps(line)
         print(s, flush=True)

@@ -253,6 +253,77 @@ LSGB_API int lsgb_solver_enable_timing(lsgb_solver* s, int enable);
 LSGB_API int lsgb_solver_kernel_times(lsgb_solver* s, double* stage_ms, int64_t* stage_launches,
                                       double* reinit_ms, int64_t* reinit_launches);
 
+/* Tile shape of the FP32 stage kernels: the z-chunk length (16, 32, 64) of
+ * the 3D tiles or the block height (2, 4, 8) of the 2D blocks; 0 = default.
+ * Every shape gives bit-identical results; only the speed differs. */
+LSGB_API int lsgb_solver_set_tile(lsgb_solver* s, int tile);
+LSGB_API int lsgb_solver_get_tile(const lsgb_solver* s, int* tile);
+
+/* Autotuner: times one stage launch per candidate tile shape (reps launches
+ * each, CUDA events on the handle's stream; the state G is not modified) and
+ * keeps the fastest.  Needs G and the velocity.  FP64 handles have one shape. */
+LSGB_API int lsgb_solver_autotune(lsgb_solver* s, int reps, int* best_tile, float* best_ms);
+
+/* ------------------------------------------------------------------------
+ * Batches: many independent instances (any mix of 2D and 3D sizes, one
+ * precision) advanced together.  Instances keep their own lsgb_solver handle
+ * for fields, reductions and output; lsgb_batch_advance runs all of them with
+ * one captured CUDA graph per reinit period, the instances spread over
+ * n_lanes concurrent streams.  Instances must share the step counter and the
+ * reinit cadence.  Each instance's result equals its single-instance run bit
+ * for bit.  Not in the reference (its variants run one instance per process).
+ * ------------------------------------------------------------------------ */
+typedef struct lsgb_batch lsgb_batch;
+LSGB_API int lsgb_batch_create(int precision, int n_lanes, lsgb_batch** out);
+LSGB_API int lsgb_batch_destroy(lsgb_batch* b);
+/* New instance owned by the batch; *solver (nullable) is its handle. */
+LSGB_API int lsgb_batch_add(lsgb_batch* b, const lsgb_params* p, lsgb_solver** solver, int* index);
+LSGB_API int lsgb_batch_size(const lsgb_batch* b, int* n);
+LSGB_API int lsgb_batch_solver(lsgb_batch* b, int index, lsgb_solver** out);
+/* lsgb_solver_autotune on every instance. */
+LSGB_API int lsgb_batch_autotune(lsgb_batch* b, int reps);
+/* Advance every instance n_steps steps (asynchronous on the batch stream;
+ * later calls on an instance's own handle are ordered after it). */
+LSGB_API int lsgb_batch_advance(lsgb_batch* b, int n_steps);
+/* Wait for the batch and report any in-kernel wait that gave up. */
+LSGB_API int lsgb_batch_sync(lsgb_batch* b);
+/* Graph replays so far and kernels per replayed graph. */
+LSGB_API int lsgb_batch_stats(const lsgb_batch* b, int64_t* graph_launches, int64_t* kernels_per_graph);
+/* The batch's stream (void* cudaStream_t), for events around lsgb_batch_advance. */
+LSGB_API int lsgb_batch_stream(lsgb_batch* b, void** stream);
+
+/* ------------------------------------------------------------------------
+ * Discrete adjoint of lsgb_solver_advance (not in the reference, which has no
+ * gradients).  The forward records checkpoints of G every checkpoint_interval
+ * steps; the backward recomputes one checkpoint segment at a time on a tape
+ * (every RK3 stage input and every HCR-2 pseudo-step input) and runs the
+ * vector-Jacobian products of the stage kernels and the pseudo-steps in
+ * reverse.  Upwind branches, Godunov selections, crossing flags and the
+ * stability mask are taken from the forward state.  Periodic boundaries only.
+ * Gradients are deterministic (no atomics) and independent of the checkpoint
+ * interval.
+ * ------------------------------------------------------------------------ */
+typedef struct lsgb_adjoint lsgb_adjoint;
+LSGB_API int lsgb_adjoint_create(lsgb_solver* s, int checkpoint_interval, lsgb_adjoint** out);
+LSGB_API int lsgb_adjoint_destroy(lsgb_adjoint* a);
+/* Advance the solver n_steps steps (same results as lsgb_solver_advance),
+ * recording checkpoints; the solver ends at G_T. */
+LSGB_API int lsgb_adjoint_forward(lsgb_adjoint* a, int n_steps);
+/* Target field for the smoothed-Heaviside mismatch
+ *   L = 1/2 sum_cells (H(G_T) - H(G_target))^2 dV,  H(g) = (1 - tanh(g / eps)) / 2. */
+LSGB_API int lsgb_adjoint_set_target(lsgb_adjoint* a, const double* G_target, int layout, int memory,
+                                     double eps);
+/* L of the solver's current G against the target; seed != 0 also stores
+ * dL/dG_T as the seed of the next backward. */
+LSGB_API int lsgb_adjoint_loss(lsgb_adjoint* a, int seed, double* loss);
+/* Reverse sweep over the last forward.  dL_dGT (FP64, layout / memory) is the
+ * seed; NULL uses the seed stored by lsgb_adjoint_loss. */
+LSGB_API int lsgb_adjoint_backward(lsgb_adjoint* a, const double* dL_dGT, int layout, int memory);
+/* Gradient of the last backward as FP64: which = LSGB_FIELD_G (dL/dG_0),
+ * LSGB_FIELD_U / _V / _W (velocity), LSGB_FIELD_SL (per-cell S_L; with a
+ * scalar S_L the sum of this field is dL/dS_L). */
+LSGB_API int lsgb_adjoint_get_grad(lsgb_adjoint* a, int which, double* out, int layout, int memory);
+
 /* Deformation-vortex velocity of the reference's default 3D test case at time
  * t with period T, evaluated on the device at the cell centres x_i = i * dx:
  * computeDeformationVelocity / updateDeformationVelocity

@@ -1,0 +1,466 @@
+// adjoint.cu -- discrete adjoint (vector-Jacobian products) of the fused RK3
+// stage and of the HCR-2 pseudo-step, on compact periodic fields.
+//
+// The forward maps being differentiated are the stage kernels of
+// f64_kernels.cu / stage3d_f32.cu (computeRHS3D + rk3Stage{1,2,3}_3D,
+// Local_code/level-set_MPI_3D/include/rk3.h:31-121, with the WENO-5 of
+// weno5.h:28-196) and the pseudo-step reinitStep3D
+// (reinitialization.h:95-193).  Piecewise choices are frozen at the forward
+// state: the upwind branch u_eff >= 0 (weno5.h:99), the Godunov selection of
+// weno5_gradient_magnitude_3d (weno5.h:202-248), the crossing flags and the
+// stability mask of the interface constraint, and the s_l > epsilon gate.
+// Everything else (WENO weights, |grad G|, u_eff, sign(phi0), r~) is
+// differentiated exactly.
+//
+// Each transpose is two passes and needs no atomics, so results do not
+// depend on scheduling:
+//   coef pass    one thread per cell c forms lambda_c * dF_c/dG_{c+o} for every
+//                stencil offset o and stores it in plane o (structure of
+//                arrays), plus the point-wise parameter sensitivities;
+//   gather pass  one thread per cell m sums plane o at m - o over all o in a
+//                fixed order.
+// Boundaries are periodic on every axis (the wrapped neighbour map is a
+// bijection, so the gather is the exact transpose).
+#include "common.cuh"
+
+namespace lsgb {
+namespace {
+
+constexpr double ADJ_WENO_EPS = 1.0e-6;  // weno5.h:22
+
+struct Idx {
+    int nx, ny, nz;
+    __device__ __forceinline__ long long at(int i, int j, int k) const {
+        return (long long)i + (long long)nx * ((long long)j + (long long)ny * k);
+    }
+};
+
+__device__ __forceinline__ int wrap(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
+
+// WENO reconstruction f = sum_k w_k p_k over the candidate stencils of
+// (a0..a4) with linear weights (d0, d1, d2), and df/da.  With
+// alpha_k = d_k / (eps + beta_k)^2 and w_k = alpha_k / sum alpha:
+//   df/da_j = sum_k w_k dp_k/da_j - 2 sum_k (p_k - f) w_k / (eps + beta_k) dbeta_k/da_j.
+// beta_k = 13/12 (a_k - 2 a_{k+1} + a_{k+2})^2 + 1/4 (a_{k+2} - a_k)^2 is the
+// reference's indicator (weno5.h:28-37).  weno5_left (:39-58) is
+// (a) = (v0..v4), d = (0.1, 0.6, 0.3); weno5_right (:60-81) is the same
+// formula on the reversed stencil with d = (0.3, 0.6, 0.1).
+template <typename R>
+__device__ __forceinline__ void weno_grad(R a0, R a1, R a2, R a3, R a4, R d0, R d1, R d2, R& f, R* df) {
+    const R eps = (R)ADJ_WENO_EPS;
+    const R c1312 = (R)(13.0 / 12.0), c136 = (R)(13.0 / 6.0), c133 = (R)(13.0 / 3.0);
+    const R e0 = a0 - (R)2 * a1 + a2, e1 = a1 - (R)2 * a2 + a3, e2 = a2 - (R)2 * a3 + a4;
+    const R h0 = a2 - a0, h1 = a3 - a1, h2 = a4 - a2;
+    const R q0 = eps + c1312 * e0 * e0 + (R)0.25 * h0 * h0;
+    const R q1 = eps + c1312 * e1 * e1 + (R)0.25 * h1 * h1;
+    const R q2 = eps + c1312 * e2 * e2 + (R)0.25 * h2 * h2;
+    const R al0 = d0 / (q0 * q0), al1 = d1 / (q1 * q1), al2 = d2 / (q2 * q2);
+    const R inv = (R)1 / (al0 + al1 + al2);
+    const R w0 = al0 * inv, w1 = al1 * inv, w2 = al2 * inv;
+    const R sixth = (R)(1.0 / 6.0);
+    const R p0 = ((R)2 * a0 - (R)7 * a1 + (R)11 * a2) * sixth;
+    const R p1 = (-a1 + (R)5 * a2 + (R)2 * a3) * sixth;
+    const R p2 = ((R)2 * a2 + (R)5 * a3 - a4) * sixth;
+    f = w0 * p0 + w1 * p1 + w2 * p2;
+    const R c0 = (R)-2 * (p0 - f) * w0 / q0;
+    const R cc1 = (R)-2 * (p1 - f) * w1 / q1;
+    const R c2 = (R)-2 * (p2 - f) * w2 / q2;
+    // dbeta_k / d(a_k, a_{k+1}, a_{k+2})
+    const R b0l = c136 * e0 - (R)0.5 * h0, b0m = -c133 * e0, b0r = c136 * e0 + (R)0.5 * h0;
+    const R b1l = c136 * e1 - (R)0.5 * h1, b1m = -c133 * e1, b1r = c136 * e1 + (R)0.5 * h1;
+    const R b2l = c136 * e2 - (R)0.5 * h2, b2m = -c133 * e2, b2r = c136 * e2 + (R)0.5 * h2;
+    df[0] = w0 * ((R)2 * sixth) + c0 * b0l;
+    df[1] = w0 * ((R)-7 * sixth) + w1 * (-sixth) + c0 * b0m + cc1 * b1l;
+    df[2] = w0 * ((R)11 * sixth) + w1 * ((R)5 * sixth) + w2 * ((R)2 * sixth) + c0 * b0r + cc1 * b1m + c2 * b2l;
+    df[3] = w1 * ((R)2 * sixth) + w2 * ((R)5 * sixth) + cc1 * b1r + c2 * b2m;
+    df[4] = w2 * (-sixth) + c2 * b2r;
+}
+
+// Upwind WENO derivative D = (f_{i+1/2} - f_{i-1/2}) / h of the 7-point line
+// s[0..6] = G[i-3..i+3] (weno5_dx_3d, weno5.h:90-124) and dD/ds.
+template <typename R>
+__device__ __forceinline__ void axis_grad(const R* s, R vel, R inv_h, R& D, R* dD) {
+    R fl, fr, tl[5], tr[5];
+    if (vel >= (R)0) {
+        weno_grad(s[0], s[1], s[2], s[3], s[4], (R)0.1, (R)0.6, (R)0.3, fl, tl);
+        weno_grad(s[1], s[2], s[3], s[4], s[5], (R)0.1, (R)0.6, (R)0.3, fr, tr);
+        dD[0] = -tl[0] * inv_h;
+#pragma unroll
+        for (int q = 1; q <= 4; ++q) dD[q] = (tr[q - 1] - tl[q]) * inv_h;
+        dD[5] = tr[4] * inv_h;
+        dD[6] = (R)0;
+    } else {
+        // reversed stencils: f_{i-1/2} from s[5..1], f_{i+1/2} from s[6..2]
+        weno_grad(s[5], s[4], s[3], s[2], s[1], (R)0.3, (R)0.6, (R)0.1, fl, tl);
+        weno_grad(s[6], s[5], s[4], s[3], s[2], (R)0.3, (R)0.6, (R)0.1, fr, tr);
+        dD[0] = (R)0;
+        dD[1] = -tl[4] * inv_h;
+#pragma unroll
+        for (int q = 2; q <= 5; ++q) dD[q] = (tr[6 - q] - tl[5 - q]) * inv_h;
+        dD[6] = tr[0] * inv_h;
+    }
+    D = (fr - fl) * inv_h;
+}
+
+// ---------------------------------------------------------------------------
+// RK3 stage
+// ---------------------------------------------------------------------------
+
+// Planes of the stage transpose: 0 = centre, then per axis the offsets
+// -3, -2, -1, +1, +2, +3 (axis a uses planes 1 + 6a .. 6 + 6a).
+__device__ __forceinline__ int stage_off(int q) { return q < 3 ? q - 3 : q - 2; }
+
+template <typename T, int DIM>
+__global__ void __launch_bounds__(256) stage_adj_coef_kernel(AdjStageArgs a) {
+    const Geo g = a.g;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = DIM == 3 ? blockIdx.z * blockDim.z + threadIdx.z : 0;
+    if (i >= g.nx || j >= g.ny || k >= g.nz) return;
+    typedef T R;
+    const Idx ix{g.nx, g.ny, g.nz};
+    const T* __restrict__ G = (const T*)a.Gin;
+    const long long c = ix.at(i, j, k);
+    R s[3][7];
+#pragma unroll
+    for (int d = -3; d <= 3; ++d) {
+        s[0][d + 3] = G[ix.at(wrap(i + d, g.nx), j, k)];
+        s[1][d + 3] = G[ix.at(i, wrap(j + d, g.ny), k)];
+        if (DIM == 3) s[2][d + 3] = G[ix.at(i, j, wrap(k + d, g.nz))];
+    }
+    const R S = a.sl ? ((const T*)a.sl)[c] : (R)a.s_l;
+    const R h[3] = {(R)a.dx, (R)a.dy, (R)a.dz};
+    R gr[3] = {(R)0, (R)0, (R)0};
+    R gm = (R)1;
+    const bool active = (double)S > a.eps;
+    if (active) {
+        R q = (R)0;
+#pragma unroll
+        for (int ax = 0; ax < DIM; ++ax) {
+            gr[ax] = (s[ax][4] - s[ax][2]) / ((R)2 * h[ax]);
+            q += gr[ax] * gr[ax];
+        }
+        gm = sqrt(q + (R)a.eps);
+    }
+    const T* vel[3] = {(const T*)a.u, (const T*)a.v, (const T*)a.w};
+    R ue[3], D[3], dD[3][7];
+#pragma unroll
+    for (int ax = 0; ax < DIM; ++ax) {
+        ue[ax] = vel[ax][c] - S * gr[ax] / gm;
+        axis_grad(s[ax], ue[ax], (R)1 / h[ax], D[ax], dD[ax]);
+    }
+    // R = -(sum_a ue_a D_a);  dR/dg_b = S (D_b / gm - (D . g) g_b / gm^3);  dR/dS = (D . g) / gm
+    R dg = (R)0;
+#pragma unroll
+    for (int ax = 0; ax < DIM; ++ax) dg += D[ax] * gr[ax];
+    const R wc = (R)(a.cdt) * ((const T*)a.lam)[c];
+    T* coef = (T*)a.coef;
+    const long long P = g.cells();
+    R centre = (R)0;
+#pragma unroll
+    for (int ax = 0; ax < DIM; ++ax) {
+        R dRg = (R)0;
+        if (active) dRg = S * (D[ax] / gm - dg * gr[ax] / (gm * gm * gm));
+        const R half = dRg / ((R)2 * h[ax]);
+        centre += -ue[ax] * dD[ax][3];
+#pragma unroll
+        for (int q = 0; q < 6; ++q) {
+            const int sidx = stage_off(q) + 3;
+            R v = -ue[ax] * dD[ax][sidx];
+            if (sidx == 4) v += half;
+            if (sidx == 2) v -= half;
+            coef[(long long)(1 + 6 * ax + q) * P + c] = (T)(wc * v);
+        }
+    }
+    coef[c] = (T)(wc * centre);
+    if (a.gS) a.gS[c] += (double)(wc * (active ? dg / gm : (R)0));
+    if (a.gu) {
+        a.gu[c] += (double)(-wc * D[0]);
+        a.gv[c] += (double)(-wc * D[1]);
+        if (DIM == 3) a.gw[c] += (double)(-wc * D[2]);
+    }
+}
+
+// out[m] = c_self lam[m] + addend[m] + sum_o plane_o[m - o];
+// acc[m] = (acc_init ? 0 : acc[m]) + c_n lam[m] when acc is given.
+template <typename T, int DIM>
+__global__ void __launch_bounds__(256) stage_adj_gather_kernel(AdjGatherArgs a) {
+    const Geo g = a.g;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = DIM == 3 ? blockIdx.z * blockDim.z + threadIdx.z : 0;
+    if (i >= g.nx || j >= g.ny || k >= g.nz) return;
+    const Idx ix{g.nx, g.ny, g.nz};
+    const long long m = ix.at(i, j, k);
+    const long long P = g.cells();
+    const T* __restrict__ coef = (const T*)a.coef;
+    const T lam = ((const T*)a.lam)[m];
+    T sum = coef[m];
+#pragma unroll
+    for (int q = 0; q < 6; ++q) {
+        const int o = stage_off(q);
+        sum += coef[(long long)(1 + q) * P + ix.at(wrap(i - o, g.nx), j, k)];
+    }
+#pragma unroll
+    for (int q = 0; q < 6; ++q) {
+        const int o = stage_off(q);
+        sum += coef[(long long)(7 + q) * P + ix.at(i, wrap(j - o, g.ny), k)];
+    }
+    if (DIM == 3) {
+#pragma unroll
+        for (int q = 0; q < 6; ++q) {
+            const int o = stage_off(q);
+            sum += coef[(long long)(13 + q) * P + ix.at(i, j, wrap(k - o, g.nz))];
+        }
+    }
+    T out = (T)a.c_self * lam + sum;
+    if (a.addend) out += ((const T*)a.addend)[m];
+    ((T*)a.out)[m] = out;
+    if (a.acc) {
+        T* acc = (T*)a.acc;
+        acc[m] = (a.acc_init ? (T)0 : acc[m]) + (T)a.c_n * lam;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// HCR-2 pseudo-step
+// ---------------------------------------------------------------------------
+
+// Planes: 0..6 for phi^m (centre, -x, +x, -y, +y, -z, +z), 7..13 for phi0.
+__device__ __forceinline__ void nb_off(int q, int& ox, int& oy, int& oz) {
+    ox = oy = oz = 0;
+    const int sgn = (q & 1) ? 1 : -1;
+    if (q < 2) ox = sgn;
+    else if (q < 4) oy = sgn;
+    else oz = sgn;
+}
+
+template <typename T, int DIM>
+__global__ void __launch_bounds__(256) reinit_adj_coef_kernel(AdjReinitArgs a) {
+    const Geo g = a.g;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = DIM == 3 ? blockIdx.z * blockDim.z + threadIdx.z : 0;
+    if (i >= g.nx || j >= g.ny || k >= g.nz) return;
+    typedef T R;
+    const Idx ix{g.nx, g.ny, g.nz};
+    const long long c = ix.at(i, j, k);
+    const T* __restrict__ phin = (const T*)a.phin;
+    const T* __restrict__ phi0 = (const T*)a.phi0;
+    long long nb[6];
+#pragma unroll
+    for (int q = 0; q < 2 * DIM; ++q) {
+        int ox, oy, oz;
+        nb_off(q, ox, oy, oz);
+        nb[q] = ix.at(wrap(i + ox, g.nx), wrap(j + oy, g.ny), wrap(k + oz, g.nz));
+    }
+    const R phi = phin[c], ph0 = phi0[c];
+    R pn[6], p0[6];
+#pragma unroll
+    for (int q = 0; q < 2 * DIM; ++q) { pn[q] = phin[nb[q]]; p0[q] = phi0[nb[q]]; }
+    const R dx = (R)a.dx;
+    const R h[3] = {(R)a.dx, (R)a.dy, (R)a.dz};
+    const R rad = sqrt(ph0 * ph0 + dx * dx);
+    const R S = ph0 / rad;  // smoothSign (reinitialization.h:24)
+    const R dS = dx * dx / (rad * rad * rad);
+    const bool pos = S > (R)0;
+    // Godunov |grad phi|^2 with the selected one-sided difference per axis
+    R gsq = (R)0, dgc = (R)0, dgn[6];
+#pragma unroll
+    for (int ax = 0; ax < DIM; ++ax) {
+        const R inv = (R)1 / h[ax];
+        const R dm = (phi - pn[2 * ax]) * inv;
+        const R dp = (pn[2 * ax + 1] - phi) * inv;
+        const R A = pos ? (dm > (R)0 ? dm : (R)0) : (dm < (R)0 ? dm : (R)0);
+        const R B = pos ? (dp < (R)0 ? dp : (R)0) : (dp > (R)0 ? dp : (R)0);
+        dgn[2 * ax] = dgn[2 * ax + 1] = (R)0;
+        if (A * A >= B * B) {
+            gsq += A * A;  // d(A^2) = 2 A dA, dA = (dphi - dpn_minus) / h where A = dm
+            dgc += (R)2 * A * inv;
+            dgn[2 * ax] = (R)-2 * A * inv;
+        } else {
+            gsq += B * B;
+            dgc += (R)-2 * B * inv;
+            dgn[2 * ax + 1] = (R)2 * B * inv;
+        }
+    }
+    const R sq = sqrt(gsq);
+    const R dterm = sq > (R)0 ? -S / ((R)2 * sq) : (R)0;  // d term / d gsq
+    R cphi = dterm * dgc;          // d(term + forcing) / d phi_c
+    R c0 = -(sq - (R)1) * dS;      // d(term + forcing) / d phi0_c
+    R cn[6], c0n[6];
+#pragma unroll
+    for (int q = 0; q < 2 * DIM; ++q) { cn[q] = dterm * dgn[q]; c0n[q] = (R)0; }
+    // interface constraint (computeInterfaceCrossings3D :46-89, stability
+    // check :95-130, forcing :160-178), evaluated in FP64 as in the forward
+    int flag = 0;
+#pragma unroll
+    for (int q = 0; q < 2 * DIM; ++q)
+        if ((double)ph0 * (double)p0[q] < 0.0) flag |= 1 << q;
+    if (flag) {
+        bool stable = (phi > (R)0) == (ph0 > (R)0);
+#pragma unroll
+        for (int q = 0; q < 2 * DIM; ++q)
+            if ((flag >> q) & 1) stable = stable && ((pn[q] > (R)0) == (p0[q] > (R)0));
+        if (stable) {
+            double sum0 = 0.0, sumn = 0.0;
+#pragma unroll
+            for (int q = 0; q < 2 * DIM; ++q)
+                if ((flag >> q) & 1) { sum0 += (double)p0[q]; sumn += (double)pn[q]; }
+            const double bdx = a.beta / a.dx;
+            const bool has_rt = fabs(sum0) > 1e-15;
+            const double rt = has_rt ? (double)ph0 / sum0 : 0.0;
+            cphi += (R)(-bdx);
+            if (has_rt) {
+                const double drt_c = 1.0 / sum0, drt_n = -(double)ph0 / (sum0 * sum0);
+                c0 += (R)(bdx * sumn * drt_c);
+#pragma unroll
+                for (int q = 0; q < 2 * DIM; ++q)
+                    if ((flag >> q) & 1) {
+                        cn[q] += (R)(bdx * rt);
+                        c0n[q] = (R)(bdx * sumn * drt_n);
+                    }
+            }
+        }
+    }
+    const R mu = ((const T*)a.mu)[c];
+    const R md = mu * (R)a.dtau;
+    T* coef = (T*)a.coef;
+    const long long P = g.cells();
+    coef[c] = (T)(mu + md * cphi);
+    coef[7 * P + c] = (T)(md * c0);
+#pragma unroll
+    for (int q = 0; q < 2 * DIM; ++q) {
+        coef[(long long)(1 + q) * P + c] = (T)(md * cn[q]);
+        coef[(long long)(8 + q) * P + c] = (T)(md * c0n[q]);
+    }
+}
+
+// mu_out[m] = sum_o plane_o[m - o]  (o over centre and the 2 DIM neighbours)
+// lam0[m]   = (first ? 0 : lam0[m]) + sum_o plane_{7+o}[m - o]
+// last:      mu_out[m] += lam0[m]   (phi^0 = phi0)
+template <typename T, int DIM>
+__global__ void __launch_bounds__(256) reinit_adj_gather_kernel(AdjReinitGatherArgs a) {
+    const Geo g = a.g;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = DIM == 3 ? blockIdx.z * blockDim.z + threadIdx.z : 0;
+    if (i >= g.nx || j >= g.ny || k >= g.nz) return;
+    const Idx ix{g.nx, g.ny, g.nz};
+    const long long m = ix.at(i, j, k);
+    const long long P = g.cells();
+    const T* __restrict__ coef = (const T*)a.coef;
+    T s = coef[m], s0 = coef[7 * P + m];
+#pragma unroll
+    for (int q = 0; q < 2 * DIM; ++q) {
+        int ox, oy, oz;
+        nb_off(q, ox, oy, oz);
+        // plane q of cell c holds d F_c / d phi_{c + o}: cell m receives it from c = m - o
+        const long long c = ix.at(wrap(i - ox, g.nx), wrap(j - oy, g.ny), wrap(k - oz, g.nz));
+        s += coef[(long long)(1 + q) * P + c];
+        s0 += coef[(long long)(8 + q) * P + c];
+    }
+    T* lam0 = (T*)a.lam0;
+    const T l0 = (a.first ? (T)0 : lam0[m]) + s0;
+    if (a.last) ((T*)a.mu_out)[m] = s + l0;
+    else {
+        ((T*)a.mu_out)[m] = s;
+        lam0[m] = l0;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// smoothed-Heaviside mismatch  L = 1/2 sum (H(G) - H(Gt))^2 dV,
+// H(g) = (1 - tanh(g / eps)) / 2; lam = dL/dG = (H(G) - H(Gt)) H'(G) dV
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(RED_THREADS) heaviside_kernel(long long n, const T* __restrict__ G,
+                                                                const double* __restrict__ Gt, double eps,
+                                                                double dv, T* __restrict__ lam,
+                                                                double* __restrict__ partials) {
+    __shared__ double red[RED_THREADS];
+    double acc = 0.0;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n;
+         e += (long long)gridDim.x * blockDim.x) {
+        const double th = tanh((double)G[e] / eps);
+        const double d = 0.5 * (1.0 - th) - 0.5 * (1.0 - tanh(Gt[e] / eps));
+        acc += 0.5 * d * d * dv;
+        if (lam) lam[e] = (T)(d * (-0.5 * (1.0 - th * th) / eps) * dv);
+    }
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (int s = RED_THREADS / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) partials[blockIdx.x] = red[0];
+}
+
+__global__ void __launch_bounds__(RED_THREADS) sum_partials_kernel(const double* __restrict__ partials, int n,
+                                                                   double* __restrict__ out) {
+    __shared__ double red[RED_THREADS];
+    double acc = 0.0;
+    for (int e = threadIdx.x; e < n; e += blockDim.x) acc += partials[e];
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (int s = RED_THREADS / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[0] = red[0];
+}
+
+dim3 cell_block(const Geo& g) { return g.dim == 3 ? dim3(32, 4, 2) : dim3(32, 8, 1); }
+dim3 cell_grid(const Geo& g, dim3 b) {
+    return dim3((g.nx + b.x - 1) / b.x, (g.ny + b.y - 1) / b.y, g.dim == 3 ? (g.nz + b.z - 1) / b.z : 1);
+}
+
+}  // namespace
+
+template <typename T>
+cudaError_t launch_stage_adj(const AdjStageArgs& c, const AdjGatherArgs& gth, cudaStream_t st) {
+    const dim3 b = cell_block(c.g), gr = cell_grid(c.g, b);
+    if (c.g.dim == 3) {
+        stage_adj_coef_kernel<T, 3><<<gr, b, 0, st>>>(c);
+        stage_adj_gather_kernel<T, 3><<<gr, b, 0, st>>>(gth);
+    } else {
+        stage_adj_coef_kernel<T, 2><<<gr, b, 0, st>>>(c);
+        stage_adj_gather_kernel<T, 2><<<gr, b, 0, st>>>(gth);
+    }
+    count_launches(2);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_reinit_adj(const AdjReinitArgs& c, const AdjReinitGatherArgs& gth, cudaStream_t st) {
+    const dim3 b = cell_block(c.g), gr = cell_grid(c.g, b);
+    if (c.g.dim == 3) {
+        reinit_adj_coef_kernel<T, 3><<<gr, b, 0, st>>>(c);
+        reinit_adj_gather_kernel<T, 3><<<gr, b, 0, st>>>(gth);
+    } else {
+        reinit_adj_coef_kernel<T, 2><<<gr, b, 0, st>>>(c);
+        reinit_adj_gather_kernel<T, 2><<<gr, b, 0, st>>>(gth);
+    }
+    count_launches(2);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_heaviside(const Geo& g, const T* G, const double* Gt, double eps, double dv, T* lam,
+                             double* partials, double* out, cudaStream_t st) {
+    heaviside_kernel<T><<<RED_BLOCKS, RED_THREADS, 0, st>>>(g.cells(), G, Gt, eps, dv, lam, partials);
+    sum_partials_kernel<<<1, RED_THREADS, 0, st>>>(partials, RED_BLOCKS, out);
+    count_launches(2);
+    return cudaGetLastError();
+}
+
+template cudaError_t launch_stage_adj<float>(const AdjStageArgs&, const AdjGatherArgs&, cudaStream_t);
+template cudaError_t launch_stage_adj<double>(const AdjStageArgs&, const AdjGatherArgs&, cudaStream_t);
+template cudaError_t launch_reinit_adj<float>(const AdjReinitArgs&, const AdjReinitGatherArgs&, cudaStream_t);
+template cudaError_t launch_reinit_adj<double>(const AdjReinitArgs&, const AdjReinitGatherArgs&, cudaStream_t);
+template cudaError_t launch_heaviside<float>(const Geo&, const float*, const double*, double, double, float*,
+                                             double*, double*, cudaStream_t);
+template cudaError_t launch_heaviside<double>(const Geo&, const double*, const double*, double, double, double*,
+                                              double*, double*, cudaStream_t);
+
+}  // namespace lsgb

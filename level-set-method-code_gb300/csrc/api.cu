@@ -6,6 +6,7 @@
 // f64_kernels.cu / f32_kernels.cu / reduce.cu / synth.cu on one stream.
 #include "common.cuh"
 
+#include <algorithm>
 #include <atomic>
 #include <cmath>
 #include <cstdarg>
@@ -18,6 +19,8 @@ namespace lsgb {
 
 static std::atomic<uint64_t> g_launches{0};
 void count_launches(uint64_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+// launches recorded into a graph during capture run only when the graph does
+void uncount_launches(uint64_t n) { g_launches.fetch_sub(n, std::memory_order_relaxed); }
 
 namespace {
 
@@ -349,6 +352,7 @@ struct lsgb_solver {
     double* scratch = nullptr;   // reduction partials + results
     double* h_res = nullptr;     // pinned result slots
     int step = 0;
+    int tile = 0;  // tile-shape choice handed to the stage kernels (0 = default)
     bool have_G = false, have_vel = false;
     // kernel timing (lsgb_solver_enable_timing)
     bool timing = false;
@@ -441,25 +445,28 @@ int launch_stage(lsgb_solver* s, const StageArgs& a) {
     return LSGB_OK;
 }
 
-// One TVD-RK3 step: G -> A (stage 1), A -> B (stage 2), (G, B) -> A (stage 3),
-// then A is the new G.
+// One TVD-RK3 step: G -> A (stage 1), A -> B (stage 2), (G, B) -> G (stage 3).
+// Stage 3 writes in place: G^n enters only point-wise, read by the thread that
+// writes the same cell, so every cell's G^n is read before it is replaced.
+// The buffers keep their roles, which makes captured step sequences
+// replayable.
 int rk3_step(lsgb_solver* s) {
     StageArgs a = stage_args(s->p, s->g, s->lay);
     a.u = s->u; a.v = s->v; a.w = s->w; a.sl = s->sl;
     a.err = err_flag(s);
+    a.tile = s->tile;
     a.Gn = s->G;
     a.Gin = s->G; a.Gout = s->A; a.stage = 1;
     LSGB_TRY(launch_stage(s, a));
     a.Gin = s->A; a.Gout = s->B; a.stage = 2;
     LSGB_TRY(launch_stage(s, a));
-    a.Gin = s->B; a.Gout = s->A; a.stage = 3;
+    a.Gin = s->B; a.Gout = s->G; a.stage = 3;
     LSGB_TRY(launch_stage(s, a));
-    std::swap(s->G, s->A);
     return LSGB_OK;
 }
 
-// HCR-2 with phi0 = the current G buffer (left untouched), pseudo-steps
-// ping-ponging through A and B; r~ and flags are recomputed from phi0 inside
+// HCR-2 with phi0 = the current G buffer (left untouched until the end),
+// pseudo-steps ping-ponging through A and B; r~ and flags are recomputed from phi0 inside
 // each pseudo-step (same operations as the stored form).
 int reinit(lsgb_solver* s) {
     if (s->p.reinit_iterations <= 0) return LSGB_OK;
@@ -484,12 +491,9 @@ int reinit(lsgb_solver* s) {
         LSGB_TRY(timed_end(s, ev));
         cur = bufs[it & 1];
     }
-    // the result becomes G; the old G and the other buffer are the scratch pair
-    void* old = s->G;
-    void* other = cur == s->A ? s->B : s->A;
-    s->G = cur;
-    s->A = old;
-    s->B = other;
+    // the result goes back into G (one copy per reinitialisation, so the
+    // buffers keep their roles)
+    LSGB_CUDA(cudaMemcpyAsync(s->G, cur, nbytes(s), cudaMemcpyDeviceToDevice, s->st));
     return LSGB_OK;
 }
 
@@ -870,4 +874,704 @@ extern "C" int lsgb_solver_kernel_times(lsgb_solver* s, double* stage_ms, int64_
     if (reinit_ms) *reinit_ms = t[1];
     if (reinit_launches) *reinit_launches = c[1];
     return LSGB_OK;
+}
+
+// ---------------------------------------------------------------------------
+// tile shapes and the autotuner
+// ---------------------------------------------------------------------------
+namespace {
+
+// Tile shapes the FP32 kernels accept: z-chunk length of the 3D tiles,
+// block height of the 2D blocks.  FP64 kernels have one shape.
+int tile_candidates(const lsgb_solver* s, int* c) {
+    if (s->prec != LSGB_PREC_F32) return 0;
+    if (s->p.dim == 3) { c[0] = 16; c[1] = 32; c[2] = 64; return 3; }
+    c[0] = 2; c[1] = 4; c[2] = 8; return 3;
+}
+
+}  // namespace
+
+extern "C" int lsgb_solver_set_tile(lsgb_solver* s, int tile) {
+    LSGB_TRY(solver_ok(s));
+    int c[4], n = tile_candidates(s, c);
+    bool ok = tile == 0;
+    for (int i = 0; i < n; ++i) ok = ok || tile == c[i];
+    if (!ok) return fail(LSGB_ERR_INVALID, "tile %d is not a shape of this solver", tile);
+    s->tile = tile;
+    return LSGB_OK;
+}
+
+extern "C" int lsgb_solver_get_tile(const lsgb_solver* s, int* tile) {
+    LSGB_TRY(solver_ok(s));
+    if (!tile) return fail(LSGB_ERR_INVALID, "tile is NULL");
+    *tile = s->tile;
+    return LSGB_OK;
+}
+
+// Times one RK3 stage-1 launch (G -> A, the state is not touched) for every
+// candidate shape with CUDA events on the handle's stream and keeps the
+// fastest.  Needs G and the velocity set.
+extern "C" int lsgb_solver_autotune(lsgb_solver* s, int reps, int* best_tile, float* best_ms) {
+    LSGB_TRY(solver_ok(s));
+    if (!s->have_G || !s->have_vel) return fail(LSGB_ERR_STATE, "fields not set");
+    int c[4], n = tile_candidates(s, c);
+    if (n == 0) {
+        if (best_tile) *best_tile = 0;
+        if (best_ms) *best_ms = 0.0f;
+        return LSGB_OK;
+    }
+    if (reps < 1) reps = 3;
+    cudaEvent_t e0, e1;
+    LSGB_CUDA(cudaEventCreate(&e0));
+    LSGB_CUDA(cudaEventCreate(&e1));
+    int best = c[0];
+    float tbest = 1e30f;
+    int rc = LSGB_OK;
+    for (int i = 0; i < n && rc == LSGB_OK; ++i) {
+        StageArgs a = stage_args(s->p, s->g, s->lay);
+        a.u = s->u; a.v = s->v; a.w = s->w; a.sl = s->sl;
+        a.err = err_flag(s);
+        a.tile = c[i];
+        a.Gn = s->G; a.Gin = s->G; a.Gout = s->A; a.stage = 1;
+        rc = launch_stage(s, a);  // warm-up
+        if (rc != LSGB_OK) break;
+        cudaEventRecord(e0, s->st);
+        for (int r = 0; r < reps && rc == LSGB_OK; ++r) rc = launch_stage(s, a);
+        cudaEventRecord(e1, s->st);
+        if (cudaEventSynchronize(e1) != cudaSuccess) { rc = fail(LSGB_ERR_CUDA, "autotune timing failed"); break; }
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        ms /= reps;
+        if (ms < tbest) { tbest = ms; best = c[i]; }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    LSGB_TRY(rc);
+    LSGB_TRY(check_flag(s));
+    s->tile = best;
+    if (best_tile) *best_tile = best;
+    if (best_ms) *best_ms = tbest;
+    return LSGB_OK;
+}
+
+// ---------------------------------------------------------------------------
+// batches: many independent instances advanced together in CUDA graphs
+// ---------------------------------------------------------------------------
+struct lsgb_batch {
+    int prec;
+    std::vector<lsgb_solver*> inst;
+    cudaStream_t main = nullptr;
+    std::vector<cudaStream_t> lanes;
+    std::vector<cudaEvent_t> lane_done;
+    cudaEvent_t fork = nullptr, done = nullptr;
+    cudaGraphExec_t block = nullptr;  // one reinit period of steps for every instance
+    int block_len = 0;
+    int64_t graph_launches = 0, graph_kernels = 0;
+};
+
+namespace {
+
+int batch_ok(const lsgb_batch* b) {
+    if (!b) return fail(LSGB_ERR_INVALID, "batch is NULL");
+    return LSGB_OK;
+}
+
+void batch_drop_graph(lsgb_batch* b) {
+    if (b->block) cudaGraphExecDestroy(b->block);
+    b->block = nullptr;
+    b->block_len = 0;
+}
+
+// Instances share one step counter and one reinit cadence, which lets the
+// batch replay a captured period.
+int batch_uniform(const lsgb_batch* b, int* step, int* interval, int* reinit) {
+    const lsgb_solver* f = b->inst[0];
+    for (const lsgb_solver* s : b->inst)
+        if (s->step != f->step || s->p.enable_reinit != f->p.enable_reinit ||
+            (f->p.enable_reinit && s->p.reinit_interval != f->p.reinit_interval))
+            return fail(LSGB_ERR_STATE, "batched instances need the same step counter and reinit cadence");
+    *step = f->step;
+    *interval = f->p.enable_reinit ? f->p.reinit_interval : 1;
+    *reinit = f->p.enable_reinit;
+    return LSGB_OK;
+}
+
+// Launches n steps for every instance on the lanes (each instance keeps its
+// lane), with the reinit cadence of the reference main loop.
+int batch_launch_steps(lsgb_batch* b, int n_steps) {
+    LSGB_CUDA(cudaEventRecord(b->fork, b->main));
+    for (cudaStream_t l : b->lanes) LSGB_CUDA(cudaStreamWaitEvent(l, b->fork, 0));
+    for (int q = 0; q < n_steps; ++q) {
+        for (size_t i = 0; i < b->inst.size(); ++i) {
+            lsgb_solver* s = b->inst[i];
+            cudaStream_t own = s->st;
+            s->st = b->lanes[i % b->lanes.size()];
+            int rc = rk3_step(s);
+            if (rc == LSGB_OK && s->p.enable_reinit && s->step > 0 && s->step % s->p.reinit_interval == 0)
+                rc = reinit(s);
+            s->st = own;
+            LSGB_TRY(rc);
+            s->step++;
+        }
+    }
+    for (size_t l = 0; l < b->lanes.size(); ++l) {
+        LSGB_CUDA(cudaEventRecord(b->lane_done[l], b->lanes[l]));
+        LSGB_CUDA(cudaStreamWaitEvent(b->main, b->lane_done[l], 0));
+    }
+    return LSGB_OK;
+}
+
+}  // namespace
+
+extern "C" int lsgb_batch_create(int precision, int n_lanes, lsgb_batch** out) {
+    if (!out) return fail(LSGB_ERR_INVALID, "out is NULL");
+    if (precision != LSGB_PREC_F64 && precision != LSGB_PREC_F32)
+        return fail(LSGB_ERR_INVALID, "unknown precision %d", precision);
+    if (n_lanes < 1 || n_lanes > 64) return fail(LSGB_ERR_INVALID, "n_lanes must lie in [1, 64]");
+    lsgb_batch* b = new lsgb_batch();
+    b->prec = precision;
+    cudaError_t e = cudaStreamCreateWithFlags(&b->main, cudaStreamNonBlocking);
+    for (int l = 0; l < n_lanes && e == cudaSuccess; ++l) {
+        cudaStream_t st;
+        cudaEvent_t ev;
+        e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+        if (e == cudaSuccess) b->lanes.push_back(st);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+        if (e == cudaSuccess) b->lane_done.push_back(ev);
+    }
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming);
+    if (e != cudaSuccess) {
+        lsgb_batch_destroy(b);
+        return fail(LSGB_ERR_CUDA, "batch streams: %s", cudaGetErrorString(e));
+    }
+    *out = b;
+    return LSGB_OK;
+}
+
+extern "C" int lsgb_batch_destroy(lsgb_batch* b) {
+    if (!b) return LSGB_OK;
+    if (b->main) cudaStreamSynchronize(b->main);
+    batch_drop_graph(b);
+    for (lsgb_solver* s : b->inst) lsgb_solver_destroy(s);
+    for (cudaStream_t l : b->lanes) cudaStreamDestroy(l);
+    for (cudaEvent_t ev : b->lane_done) cudaEventDestroy(ev);
+    if (b->fork) cudaEventDestroy(b->fork);
+    if (b->done) cudaEventDestroy(b->done);
+    if (b->main) cudaStreamDestroy(b->main);
+    delete b;
+    return LSGB_OK;
+}
+
+extern "C" int lsgb_batch_add(lsgb_batch* b, const lsgb_params* p, lsgb_solver** solver, int* index) {
+    LSGB_TRY(batch_ok(b));
+    lsgb_solver* s = nullptr;
+    LSGB_TRY(lsgb_solver_create(p, b->prec, &s));
+    b->inst.push_back(s);
+    batch_drop_graph(b);
+    if (solver) *solver = s;
+    if (index) *index = (int)b->inst.size() - 1;
+    return LSGB_OK;
+}
+
+extern "C" int lsgb_batch_size(const lsgb_batch* b, int* n) {
+    LSGB_TRY(batch_ok(b));
+    if (!n) return fail(LSGB_ERR_INVALID, "n is NULL");
+    *n = (int)b->inst.size();
+    return LSGB_OK;
+}
+
+extern "C" int lsgb_batch_solver(lsgb_batch* b, int index, lsgb_solver** out) {
+    LSGB_TRY(batch_ok(b));
+    if (!out || index < 0 || index >= (int)b->inst.size()) return fail(LSGB_ERR_INVALID, "bad instance index");
+    *out = b->inst[index];
+    return LSGB_OK;
+}
+
+extern "C" int lsgb_batch_autotune(lsgb_batch* b, int reps) {
+    LSGB_TRY(batch_ok(b));
+    for (lsgb_solver* s : b->inst) LSGB_TRY(lsgb_solver_autotune(s, reps, nullptr, nullptr));
+    batch_drop_graph(b);
+    return LSGB_OK;
+}
+
+extern "C" int lsgb_batch_advance(lsgb_batch* b, int n_steps) {
+    LSGB_TRY(batch_ok(b));
+    if (n_steps < 0) return fail(LSGB_ERR_INVALID, "n_steps < 0");
+    if (b->inst.empty() || n_steps == 0) return LSGB_OK;
+    for (lsgb_solver* s : b->inst)
+        if (!s->have_G || !s->have_vel) return fail(LSGB_ERR_STATE, "an instance has no fields");
+    int step, interval, reinit_on;
+    LSGB_TRY(batch_uniform(b, &step, &interval, &reinit_on));
+    // order the batch after any work queued on the instances' own streams
+    for (lsgb_solver* s : b->inst) {
+        LSGB_CUDA(cudaEventRecord(b->done, s->st));
+        LSGB_CUDA(cudaStreamWaitEvent(b->main, b->done, 0));
+    }
+    // Steps before the first period boundary run as direct launches.  A
+    // period starts at a step s with s % interval == 1 (the reinit then runs
+    // after its last step), so its launch sequence is the same every time and
+    // one captured graph replays it.
+    int remaining = n_steps;
+    auto direct = [&](int n) -> int {
+        LSGB_TRY(batch_launch_steps(b, n));
+        remaining -= n;
+        return LSGB_OK;
+    };
+    const int L = interval;
+    int head = 0;
+    while (head < remaining && (L == 1 ? false : ((step + head) % L) != 1)) head++;
+    if (head > 0) LSGB_TRY(direct(head));
+    if (remaining >= L) {
+        if (!b->block || b->block_len != L) {
+            batch_drop_graph(b);
+            // capture one period; batch_launch_steps advances the host-side
+            // step counters, which are restored after the capture
+            std::vector<int> steps0;
+            for (lsgb_solver* s : b->inst) steps0.push_back(s->step);
+            uint64_t k0 = lsgb_launch_count();
+            LSGB_CUDA(cudaStreamBeginCapture(b->main, cudaStreamCaptureModeThreadLocal));
+            int rc = batch_launch_steps(b, L);
+            cudaGraph_t graph = nullptr;
+            cudaError_t e = cudaStreamEndCapture(b->main, &graph);
+            for (size_t i = 0; i < b->inst.size(); ++i) b->inst[i]->step = steps0[i];
+            if (rc != LSGB_OK) { if (graph) cudaGraphDestroy(graph); return rc; }
+            if (e != cudaSuccess) return fail(LSGB_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e));
+            e = cudaGraphInstantiate(&b->block, graph, 0);
+            cudaGraphDestroy(graph);
+            if (e != cudaSuccess) { b->block = nullptr; return fail(LSGB_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e)); }
+            b->block_len = L;
+            b->graph_kernels = (int64_t)(lsgb_launch_count() - k0);
+            uncount_launches((uint64_t)b->graph_kernels);
+        }
+        while (remaining >= L) {
+            LSGB_CUDA(cudaGraphLaunch(b->block, b->main));
+            count_launches((uint64_t)b->graph_kernels);
+            b->graph_launches++;
+            for (lsgb_solver* s : b->inst) s->step += L;
+            remaining -= L;
+        }
+    }
+    if (remaining > 0) LSGB_TRY(direct(remaining));
+    // later calls on an instance's own stream see the batch's results
+    LSGB_CUDA(cudaEventRecord(b->done, b->main));
+    for (lsgb_solver* s : b->inst) LSGB_CUDA(cudaStreamWaitEvent(s->st, b->done, 0));
+    return LSGB_OK;
+}
+
+extern "C" int lsgb_batch_sync(lsgb_batch* b) {
+    LSGB_TRY(batch_ok(b));
+    LSGB_CUDA(cudaStreamSynchronize(b->main));
+    for (lsgb_solver* s : b->inst) LSGB_TRY(check_flag(s));
+    return LSGB_OK;
+}
+
+extern "C" int lsgb_batch_stats(const lsgb_batch* b, int64_t* graph_launches, int64_t* kernels_per_graph) {
+    LSGB_TRY(batch_ok(b));
+    if (graph_launches) *graph_launches = b->graph_launches;
+    if (kernels_per_graph) *kernels_per_graph = b->graph_kernels;
+    return LSGB_OK;
+}
+
+extern "C" int lsgb_batch_stream(lsgb_batch* b, void** stream) {
+    LSGB_TRY(batch_ok(b));
+    if (!stream) return fail(LSGB_ERR_INVALID, "stream is NULL");
+    *stream = (void*)b->main;
+    return LSGB_OK;
+}
+
+// ---------------------------------------------------------------------------
+// discrete adjoint (adjoint.cu kernels)
+// ---------------------------------------------------------------------------
+
+struct lsgb_adjoint {
+    lsgb_solver* s = nullptr;
+    int ckpt = 20;             // checkpoint interval (steps)
+    int n_steps = 0;           // steps of the last forward
+    int step0 = 0;             // solver step when that forward started
+    bool have_fwd = false, have_seed = false, have_target = false, have_grad = false;
+    double eps = 0.0;          // Heaviside width
+    size_t slot = 0;           // bytes per field slot (multiple of 256)
+    int tape_slots = 0, ckpt_slots = 0;
+    char* tape = nullptr;      // recompute tape of one segment
+    char* ckpts = nullptr;     // G at every segment start
+    void* coef = nullptr;      // ADJ_PLANES coefficient planes
+    void* lam[4] = {nullptr, nullptr, nullptr, nullptr};  // lambda buffers (solver precision)
+    double* grad[4] = {nullptr, nullptr, nullptr, nullptr};  // dL/dS_L, dL/du, dL/dv, dL/dw
+    double* target = nullptr;  // FP64 compact target
+};
+
+namespace {
+
+// Slots of one recorded step on the tape: stage inputs, HCR-2 inputs
+// phi^0 .. phi^{M-1} (phi^0 = phi0), and the slot holding the step's result.
+struct TapeStep {
+    int gn, g1, g2;
+    int r0;      // first HCR-2 slot, -1 when no reinitialisation follows the step
+    int out;
+};
+
+bool reinit_after(const lsgb_params& p, int step) {
+    return p.enable_reinit && p.reinit_iterations > 0 && step > 0 && step % p.reinit_interval == 0;
+}
+
+// Tape layout of the steps [t0, t1) starting in slot 0.
+std::vector<TapeStep> tape_plan(const lsgb_params& p, int t0, int t1, int* slots) {
+    std::vector<TapeStep> v;
+    int cur = 0;
+    for (int t = t0; t < t1; ++t) {
+        TapeStep r;
+        r.gn = cur; r.g1 = cur + 1; r.g2 = cur + 2;
+        int next = cur + 3;
+        r.r0 = -1;
+        if (reinit_after(p, t)) { r.r0 = next; next += p.reinit_iterations; }
+        r.out = next;
+        cur = next;
+        v.push_back(r);
+    }
+    *slots = cur + 1;
+    return v;
+}
+
+int adj_ok(const lsgb_adjoint* a) {
+    if (!a || !a->s) return fail(LSGB_ERR_INVALID, "adjoint handle is NULL");
+    return LSGB_OK;
+}
+
+int adj_alloc(void** p, size_t bytes, const char* what) {
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) { *p = nullptr; return fail(LSGB_ERR_ALLOC, "%s (%zu B): %s", what, bytes, cudaGetErrorString(e)); }
+    return LSGB_OK;
+}
+
+void* tslot(lsgb_adjoint* a, int q) { return a->tape + (size_t)q * a->slot; }
+
+// Recompute the steps [t0, t1) from tape slot 0 with the solver's kernels,
+// keeping every stage and pseudo-step input.
+int adj_record(lsgb_adjoint* a, const std::vector<TapeStep>& plan) {
+    lsgb_solver* s = a->s;
+    StageArgs st = stage_args(s->p, s->g, s->lay);
+    st.u = s->u; st.v = s->v; st.w = s->w; st.sl = s->sl;
+    st.err = err_flag(s);
+    st.tile = s->tile;
+    ReinitArgs r;
+    r.g = s->g;
+    r.lay = s->lay;
+    r.dx = s->p.dx;
+    r.dy = s->p.dy;
+    r.dz = s->p.dim == 3 ? s->p.dz : s->p.dx;
+    r.dtau = s->p.reinit_dtau;
+    r.beta = s->p.reinit_beta;
+    for (const TapeStep& t : plan) {
+        st.Gn = tslot(a, t.gn);
+        st.Gin = tslot(a, t.gn); st.Gout = tslot(a, t.g1); st.stage = 1;
+        LSGB_TRY(launch_stage(s, st));
+        st.Gin = tslot(a, t.g1); st.Gout = tslot(a, t.g2); st.stage = 2;
+        LSGB_TRY(launch_stage(s, st));
+        st.Gin = tslot(a, t.g2); st.stage = 3;
+        st.Gout = tslot(a, t.r0 >= 0 ? t.r0 : t.out);
+        LSGB_TRY(launch_stage(s, st));
+        if (t.r0 >= 0) {
+            r.phi0 = tslot(a, t.r0);
+            for (int m = 0; m < s->p.reinit_iterations; ++m) {
+                r.phin = tslot(a, t.r0 + m);
+                r.phinew = tslot(a, m + 1 < s->p.reinit_iterations ? t.r0 + m + 1 : t.out);
+                if (s->prec == LSGB_PREC_F64) LSGB_CUDA(launch_reinit_f64(r, s->st));
+                else LSGB_CUDA(launch_reinit_f32(r, s->st));
+            }
+        }
+    }
+    return LSGB_OK;
+}
+
+template <typename T>
+int adj_reverse_step(lsgb_adjoint* a, const TapeStep& t, void** L) {
+    lsgb_solver* s = a->s;
+    const Geo g = s->g;
+    void* others[3];
+    int q = 0;
+    for (int b = 0; b < 4; ++b)
+        if (a->lam[b] != *L) others[q++] = a->lam[b];
+    void* X = others[0];
+    void* Y = others[1];
+    void* ACC = others[2];
+    if (t.r0 >= 0) {
+        // phi^{m+1} = F(phi^m, phi0), m = M-1 .. 0
+        const int M = s->p.reinit_iterations;
+        AdjReinitArgs rc;
+        rc.g = g;
+        rc.phi0 = tslot(a, t.r0);
+        rc.coef = a->coef;
+        rc.dx = s->p.dx;
+        rc.dy = s->p.dy;
+        rc.dz = s->p.dim == 3 ? s->p.dz : s->p.dx;
+        rc.dtau = s->p.reinit_dtau;
+        rc.beta = s->p.reinit_beta;
+        AdjReinitGatherArgs rg;
+        rg.g = g;
+        rg.coef = a->coef;
+        rg.lam0 = ACC;
+        void* mu = *L;
+        void* spare = X;
+        for (int m = M - 1; m >= 0; --m) {
+            rc.phin = tslot(a, t.r0 + m);
+            rc.mu = mu;
+            rg.mu_out = spare;
+            rg.first = m == M - 1;
+            rg.last = m == 0;
+            LSGB_CUDA(launch_reinit_adj<T>(rc, rg, s->st));
+            std::swap(mu, spare);
+        }
+        *L = mu;
+        X = spare;
+    }
+    AdjStageArgs c;
+    std::memset(&c, 0, sizeof(c));
+    c.g = g;
+    c.u = s->u; c.v = s->v; c.w = s->w; c.sl = s->sl;
+    c.s_l = s->p.s_l;
+    c.eps = s->p.epsilon;
+    c.dx = s->p.dx;
+    c.dy = s->p.dy;
+    c.dz = s->p.dim == 3 ? s->p.dz : s->p.dx;
+    c.coef = a->coef;
+    c.gS = a->grad[0];
+    c.gu = a->grad[1];
+    c.gv = a->grad[2];
+    c.gw = s->p.dim == 3 ? a->grad[3] : nullptr;
+    AdjGatherArgs gt;
+    std::memset(&gt, 0, sizeof(gt));
+    gt.g = g;
+    gt.coef = a->coef;
+    const double dt = s->p.dt;
+    // stage 3: G^{n+1} = 1/3 G^n + 2/3 G2 + 2/3 dt L(G2)
+    c.Gin = tslot(a, t.g2); c.cdt = 2.0 / 3.0 * dt; c.lam = *L;
+    gt.lam = *L; gt.out = X; gt.acc = ACC; gt.acc_init = 1; gt.c_self = 2.0 / 3.0; gt.c_n = 1.0 / 3.0;
+    gt.addend = nullptr;
+    LSGB_CUDA(launch_stage_adj<T>(c, gt, s->st));
+    // stage 2: G2 = 3/4 G^n + 1/4 G1 + 1/4 dt L(G1)
+    c.Gin = tslot(a, t.g1); c.cdt = 0.25 * dt; c.lam = X;
+    gt.lam = X; gt.out = Y; gt.acc = ACC; gt.acc_init = 0; gt.c_self = 0.25; gt.c_n = 0.75;
+    LSGB_CUDA(launch_stage_adj<T>(c, gt, s->st));
+    // stage 1: G1 = G^n + dt L(G^n)
+    c.Gin = tslot(a, t.gn); c.cdt = dt; c.lam = Y;
+    gt.lam = Y; gt.out = *L; gt.acc = nullptr; gt.addend = ACC; gt.c_self = 1.0; gt.c_n = 0.0;
+    LSGB_CUDA(launch_stage_adj<T>(c, gt, s->st));
+    return LSGB_OK;
+}
+
+// FP64 array (layout, memory) -> FP64 compact device array dst.
+int load_f64_compact(lsgb_solver* s, double* dst, const double* src, int layout, int memory) {
+    Lay sl = layout == LSGB_LAYOUT_GHOSTED ? ghosted_layout(s->g) : compact_layout(s->g);
+    size_t sbytes = sizeof(double) * (size_t)layout_elems(s->g, sl.ghosted);
+    const double* dsrc = src;
+    if (memory == LSGB_MEM_HOST) {
+        if (!sl.ghosted) {
+            LSGB_CUDA(cudaMemcpyAsync(dst, src, sbytes, cudaMemcpyHostToDevice, s->st));
+            return LSGB_OK;
+        }
+        LSGB_TRY(ensure_stage(s));
+        LSGB_CUDA(cudaMemcpyAsync(s->stage64, src, sbytes, cudaMemcpyHostToDevice, s->st));
+        dsrc = s->stage64;
+    } else {
+        LSGB_TRY(check_dev(src, "field"));
+    }
+    LSGB_CUDA(launch_pack_f64(s->g, dsrc, sl, dst, s->st));
+    return LSGB_OK;
+}
+
+// compact device array (FP64 or FP32) -> FP64 out (layout, memory); synchronises.
+int store_compact(lsgb_solver* s, const void* src, bool f64, double* out, int layout, int memory) {
+    Lay dl = layout == LSGB_LAYOUT_GHOSTED ? ghosted_layout(s->g) : compact_layout(s->g);
+    size_t dbytes = sizeof(double) * (size_t)layout_elems(s->g, dl.ghosted);
+    double* ddst = out;
+    if (memory == LSGB_MEM_HOST) {
+        LSGB_TRY(ensure_stage(s));
+        ddst = s->stage64;
+    } else {
+        LSGB_TRY(check_dev(out, "out"));
+    }
+    if (f64) LSGB_CUDA(launch_unpack_f64(s->g, (const double*)src, ddst, dl, s->st));
+    else LSGB_CUDA(launch_unpack_f32(s->g, (const float*)src, ddst, dl, s->st));
+    if (memory == LSGB_MEM_HOST) LSGB_CUDA(cudaMemcpyAsync(out, ddst, dbytes, cudaMemcpyDeviceToHost, s->st));
+    LSGB_CUDA(cudaStreamSynchronize(s->st));
+    return LSGB_OK;
+}
+
+}  // namespace
+
+extern "C" int lsgb_adjoint_create(lsgb_solver* s, int checkpoint_interval, lsgb_adjoint** out) {
+    LSGB_TRY(solver_ok(s));
+    if (!out) return fail(LSGB_ERR_INVALID, "out is NULL");
+    if (checkpoint_interval < 1) return fail(LSGB_ERR_INVALID, "checkpoint_interval must be >= 1");
+    if (s->g.bcx != LSGB_BC_PERIODIC || s->g.bcy != LSGB_BC_PERIODIC ||
+        (s->g.dim == 3 && s->g.bcz != LSGB_BC_PERIODIC))
+        return fail(LSGB_ERR_UNSUPPORTED, "the adjoint supports periodic boundaries on every axis");
+    lsgb_adjoint* a = new lsgb_adjoint();
+    a->s = s;
+    a->ckpt = checkpoint_interval;
+    a->slot = (nbytes(s) + 255) / 256 * 256;
+    int rc = adj_alloc(&a->coef, (size_t)ADJ_PLANES * nbytes(s), "adjoint coefficient planes");
+    for (int b = 0; b < 4 && rc == LSGB_OK; ++b) rc = adj_alloc(&a->lam[b], a->slot, "adjoint field");
+    for (int b = 0; b < 4 && rc == LSGB_OK; ++b)
+        rc = adj_alloc((void**)&a->grad[b], sizeof(double) * (size_t)s->g.cells(), "gradient field");
+    if (rc != LSGB_OK) {
+        std::string keep = g_err;
+        lsgb_adjoint_destroy(a);
+        g_err = keep;
+        return rc;
+    }
+    *out = a;
+    return LSGB_OK;
+}
+
+extern "C" int lsgb_adjoint_destroy(lsgb_adjoint* a) {
+    if (!a) return LSGB_OK;
+    if (a->s && a->s->st) cudaStreamSynchronize(a->s->st);
+    void* ptrs[] = {a->tape, a->ckpts, a->coef, a->lam[0], a->lam[1], a->lam[2], a->lam[3],
+                    a->grad[0], a->grad[1], a->grad[2], a->grad[3], a->target};
+    for (void* q : ptrs)
+        if (q) cudaFree(q);
+    delete a;
+    return LSGB_OK;
+}
+
+extern "C" int lsgb_adjoint_forward(lsgb_adjoint* a, int n_steps) {
+    LSGB_TRY(adj_ok(a));
+    lsgb_solver* s = a->s;
+    if (n_steps < 1) return fail(LSGB_ERR_INVALID, "n_steps must be >= 1");
+    if (!s->have_G || !s->have_vel) return fail(LSGB_ERR_STATE, "fields not set");
+    const int nseg = (n_steps + a->ckpt - 1) / a->ckpt;
+    if (nseg > a->ckpt_slots) {
+        LSGB_CUDA(cudaStreamSynchronize(s->st));
+        if (a->ckpts) cudaFree(a->ckpts);
+        a->ckpts = nullptr;
+        a->ckpt_slots = 0;
+        LSGB_TRY(adj_alloc((void**)&a->ckpts, (size_t)nseg * a->slot, "checkpoints"));
+        a->ckpt_slots = nseg;
+    }
+    a->step0 = s->step;
+    a->have_fwd = a->have_seed = a->have_grad = false;
+    for (int seg = 0; seg < nseg; ++seg) {
+        LSGB_CUDA(cudaMemcpyAsync(a->ckpts + (size_t)seg * a->slot, s->G, nbytes(s), cudaMemcpyDeviceToDevice, s->st));
+        const int n = std::min(a->ckpt, n_steps - seg * a->ckpt);
+        LSGB_TRY(lsgb_solver_advance(s, n));
+    }
+    a->n_steps = n_steps;
+    a->have_fwd = true;
+    return LSGB_OK;
+}
+
+extern "C" int lsgb_adjoint_set_target(lsgb_adjoint* a, const double* G_target, int layout, int memory,
+                                       double eps) {
+    LSGB_TRY(adj_ok(a));
+    if (!G_target) return fail(LSGB_ERR_INVALID, "G_target is NULL");
+    if (!std::isfinite(eps) || eps <= 0.0) return fail(LSGB_ERR_INVALID, "eps must be positive");
+    if (layout != LSGB_LAYOUT_GHOSTED && layout != LSGB_LAYOUT_COMPACT)
+        return fail(LSGB_ERR_INVALID, "unknown layout %d", layout);
+    if (memory != LSGB_MEM_HOST && memory != LSGB_MEM_DEVICE)
+        return fail(LSGB_ERR_INVALID, "unknown memory kind %d", memory);
+    if (!a->target)
+        LSGB_TRY(adj_alloc((void**)&a->target, sizeof(double) * (size_t)a->s->g.cells(), "target field"));
+    LSGB_TRY(load_f64_compact(a->s, a->target, G_target, layout, memory));
+    a->eps = eps;
+    a->have_target = true;
+    return LSGB_OK;
+}
+
+extern "C" int lsgb_adjoint_loss(lsgb_adjoint* a, int seed, double* loss) {
+    LSGB_TRY(adj_ok(a));
+    lsgb_solver* s = a->s;
+    if (!a->have_target) return fail(LSGB_ERR_STATE, "no target set");
+    if (!s->have_G) return fail(LSGB_ERR_STATE, "G has not been set");
+    const double dv = cell_volume(s->p);
+    if (s->prec == LSGB_PREC_F64)
+        LSGB_CUDA(launch_heaviside<double>(s->g, (const double*)s->G, a->target, a->eps, dv,
+                                           seed ? (double*)a->lam[0] : nullptr, s->scratch, red_out(s), s->st));
+    else
+        LSGB_CUDA(launch_heaviside<float>(s->g, (const float*)s->G, a->target, a->eps, dv,
+                                          seed ? (float*)a->lam[0] : nullptr, s->scratch, red_out(s), s->st));
+    double r[2];
+    LSGB_TRY(reduce_read(s, r));
+    if (loss) *loss = r[0];
+    if (seed) a->have_seed = true;
+    return LSGB_OK;
+}
+
+extern "C" int lsgb_adjoint_backward(lsgb_adjoint* a, const double* dL_dGT, int layout, int memory) {
+    LSGB_TRY(adj_ok(a));
+    lsgb_solver* s = a->s;
+    if (!a->have_fwd) return fail(LSGB_ERR_STATE, "no forward recorded");
+    if (dL_dGT) {
+        if (layout != LSGB_LAYOUT_GHOSTED && layout != LSGB_LAYOUT_COMPACT)
+            return fail(LSGB_ERR_INVALID, "unknown layout %d", layout);
+        if (memory != LSGB_MEM_HOST && memory != LSGB_MEM_DEVICE)
+            return fail(LSGB_ERR_INVALID, "unknown memory kind %d", memory);
+        LSGB_TRY(load_field(s, a->lam[0], dL_dGT, layout, memory));
+    } else if (!a->have_seed) {
+        return fail(LSGB_ERR_STATE, "no seed: pass dL_dGT or call lsgb_adjoint_loss with seed");
+    }
+    a->have_seed = false;
+    // tape size: the longest segment plan
+    const int nseg = (a->n_steps + a->ckpt - 1) / a->ckpt;
+    int need = 0;
+    for (int seg = 0; seg < nseg; ++seg) {
+        const int t0 = a->step0 + seg * a->ckpt, t1 = std::min(t0 + a->ckpt, a->step0 + a->n_steps);
+        int slots = 0;
+        tape_plan(s->p, t0, t1, &slots);
+        need = std::max(need, slots);
+    }
+    if (need > a->tape_slots) {
+        LSGB_CUDA(cudaStreamSynchronize(s->st));
+        if (a->tape) cudaFree(a->tape);
+        a->tape = nullptr;
+        a->tape_slots = 0;
+        LSGB_TRY(adj_alloc((void**)&a->tape, (size_t)need * a->slot, "adjoint tape"));
+        a->tape_slots = need;
+    }
+    for (int b = 0; b < 4; ++b)
+        LSGB_CUDA(cudaMemsetAsync(a->grad[b], 0, sizeof(double) * (size_t)s->g.cells(), s->st));
+    // the current adjoint field lives in one of the four buffers
+    void* L = a->lam[0];
+    for (int seg = nseg - 1; seg >= 0; --seg) {
+        const int t0 = a->step0 + seg * a->ckpt, t1 = std::min(t0 + a->ckpt, a->step0 + a->n_steps);
+        int slots = 0;
+        std::vector<TapeStep> plan = tape_plan(s->p, t0, t1, &slots);
+        LSGB_CUDA(cudaMemcpyAsync(tslot(a, 0), a->ckpts + (size_t)seg * a->slot, nbytes(s),
+                                  cudaMemcpyDeviceToDevice, s->st));
+        LSGB_TRY(adj_record(a, plan));
+        for (int q = (int)plan.size() - 1; q >= 0; --q) {
+            if (s->prec == LSGB_PREC_F64) LSGB_TRY(adj_reverse_step<double>(a, plan[q], &L));
+            else LSGB_TRY(adj_reverse_step<float>(a, plan[q], &L));
+        }
+    }
+    // keep dL/dG_0 in lam[0]
+    if (L != a->lam[0]) {
+        for (int b = 1; b < 4; ++b)
+            if (a->lam[b] == L) std::swap(a->lam[0], a->lam[b]);
+    }
+    LSGB_TRY(check_flag(s));
+    a->have_grad = true;
+    return LSGB_OK;
+}
+
+extern "C" int lsgb_adjoint_get_grad(lsgb_adjoint* a, int which, double* out, int layout, int memory) {
+    LSGB_TRY(adj_ok(a));
+    lsgb_solver* s = a->s;
+    if (!a->have_grad) return fail(LSGB_ERR_STATE, "no backward has run");
+    if (!out) return fail(LSGB_ERR_INVALID, "out is NULL");
+    if (layout != LSGB_LAYOUT_GHOSTED && layout != LSGB_LAYOUT_COMPACT)
+        return fail(LSGB_ERR_INVALID, "unknown layout %d", layout);
+    if (memory != LSGB_MEM_HOST && memory != LSGB_MEM_DEVICE)
+        return fail(LSGB_ERR_INVALID, "unknown memory kind %d", memory);
+    switch (which) {
+        case LSGB_FIELD_G: return store_compact(s, a->lam[0], s->prec == LSGB_PREC_F64, out, layout, memory);
+        case LSGB_FIELD_SL: return store_compact(s, a->grad[0], true, out, layout, memory);
+        case LSGB_FIELD_U: return store_compact(s, a->grad[1], true, out, layout, memory);
+        case LSGB_FIELD_V: return store_compact(s, a->grad[2], true, out, layout, memory);
+        case LSGB_FIELD_W:
+            if (s->p.dim != 3) return fail(LSGB_ERR_INVALID, "no w in 2D");
+            return store_compact(s, a->grad[3], true, out, layout, memory);
+        default: return fail(LSGB_ERR_INVALID, "unknown field %d", which);
+    }
 }

@@ -83,6 +83,7 @@ struct StageArgs {
     double s_l, eps, dx, dy, dz, dt;
     int stage;               // 1, 2, 3
     int* err;                // nullable device error flag (bounded waits)
+    int tile;                // tile-shape choice (0 = default; see lsgb_solver_set_tile)
 };
 
 // HCR-2 pseudo-step arguments (handle path: r~ and flags recomputed from phi0).
@@ -159,6 +160,63 @@ cudaError_t launch_scale3(long long n, double s, double* u, double* v, double* w
 // *count and synchronises st.  Grid size screened by the caller.
 cudaError_t noalloc_count_negative_f64(const Geo& g, const Lay& lay, const double* G, double* count,
                                        cudaStream_t st);
+
+// Discrete adjoint (adjoint.cu).  Compact periodic fields of type T; the
+// coefficient buffer holds ADJ_PLANES planes of cells() elements.
+constexpr int ADJ_PLANES = 19;
+
+// coefficient pass of the stage transpose: lam = adjoint of the stage
+// output, cdt = (RHS weight of the stage) * dt; gS/gu/gv/gw (nullable, FP64)
+// accumulate the point-wise parameter sensitivities.
+struct AdjStageArgs {
+    Geo g;
+    const void* Gin;
+    const void* u;
+    const void* v;
+    const void* w;
+    const void* sl;
+    double s_l, eps, dx, dy, dz, cdt;
+    const void* lam;
+    void* coef;
+    double* gS;
+    double* gu;
+    double* gv;
+    double* gw;
+};
+// gather pass: out = c_self lam + addend + transpose; acc (+)= c_n lam
+struct AdjGatherArgs {
+    Geo g;
+    const void* coef;
+    const void* lam;
+    const void* addend;
+    void* out;
+    void* acc;
+    int acc_init;
+    double c_self, c_n;
+};
+struct AdjReinitArgs {
+    Geo g;
+    const void* phin;
+    const void* phi0;
+    const void* mu;
+    void* coef;
+    double dx, dy, dz, dtau, beta;
+};
+struct AdjReinitGatherArgs {
+    Geo g;
+    const void* coef;
+    void* mu_out;
+    void* lam0;
+    int first, last;
+};
+template <typename T>
+cudaError_t launch_stage_adj(const AdjStageArgs& c, const AdjGatherArgs& gth, cudaStream_t st);
+template <typename T>
+cudaError_t launch_reinit_adj(const AdjReinitArgs& c, const AdjReinitGatherArgs& gth, cudaStream_t st);
+// loss = 1/2 sum (H(G) - H(Gt))^2 dv into out[0]; lam (nullable) = dL/dG
+template <typename T>
+cudaError_t launch_heaviside(const Geo& g, const T* G, const double* Gt, double eps, double dv, T* lam,
+                             double* partials, double* out, cudaStream_t st);
 
 // Bookkeeping of kernel launches (lsgb_launch_count).
 void count_launches(uint64_t n);

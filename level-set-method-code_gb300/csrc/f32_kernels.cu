@@ -234,7 +234,9 @@ cudaError_t launch_stage_f32(const StageArgs& a, cudaStream_t st) {
     c.s_l = (float)a.s_l;
     c.eps = (float)a.eps;
     c.dt = (float)a.dt;
-    dim3 b = cell_block(a.g), gr = cell_grid(a.g, b);
+    dim3 b = cell_block(a.g);
+    if (a.g.dim == 2 && (a.tile == 2 || a.tile == 4)) b.y = a.tile;  // tuned 2D block height (32 x {2,4,8})
+    dim3 gr = cell_grid(a.g, b);
     const float* Gin = (const float*)a.Gin;
     const float* Gn = (const float*)a.Gn;
     float* Gout = (float*)a.Gout;

@@ -49,7 +49,7 @@ namespace {
 constexpr int TX = 32;
 constexpr int TY = 8;
 constexpr int NT = TX * TY;
-constexpr int ZC = 64;          // planes per CTA (even)
+constexpr int MAXZC = 64;       // longest z chunk a CTA marches (planes, even)
 constexpr int PW = TX + 6;      // staged plane tile
 constexpr int PH = TY + 6;
 constexpr int QXW = TX + 4;     // x-indicators for tile x in [-2, TX+1]
@@ -77,6 +77,7 @@ struct TmaMaps {
 
 struct Coef {
     float inv_dx, inv_dy, inv_dz, inv_2dx, inv_2dy, inv_2dz, s_l, eps, dt;
+    int zc;  // z-chunk length (even, <= MAXZC): tile shape chosen per grid by the autotuner
 };
 
 __device__ __forceinline__ float2 c2(float a) { return make_float2(a, a); }
@@ -178,15 +179,15 @@ stage3d_f32_pair(Geo g, const float* __restrict__ Gin, const float* __restrict__
     __shared__ float2 P2[2][PH][PW];
     __shared__ float2 QA[NQ];          // x-indicators [TY][QXW], then y-indicators [QYH][TX]
     __shared__ float2 FL[NF], FR[NF];  // x-faces [TY][TX+1], then y-faces [TY+1][TX]
-    __shared__ IDX zoff[ZC + 10];
+    __shared__ IDX zoff[MAXZC + 10];
     __shared__ __align__(8) uint64_t mbar[NSTAGE];
     extern __shared__ __align__(128) float stg[];  // NSTAGE x NFIELD x FTILE (TMA only)
 
     const int tx = threadIdx.x, ty = threadIdx.y;
     const int t = ty * TX + tx;
     const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY;
-    const int z0 = blockIdx.z * ZC;
-    const int z1 = min(z0 + ZC, g.nz);
+    const int z0 = blockIdx.z * c.zc;
+    const int z1 = min(z0 + c.zc, g.nz);
     const int niter = (z1 - z0 + 1) / 2;
     const IDX sz = (IDX)g.nx * g.ny;
     const bool valid = (i0 + tx) < g.nx && (j0 + ty) < g.ny;
@@ -250,7 +251,7 @@ stage3d_f32_pair(Geo g, const float* __restrict__ Gin, const float* __restrict__
 
     // plane offsets of z-indices z0-3 .. z1+6 (periodic wrap or clamp), one
     // table per CTA so the loop does no index arithmetic on z
-    for (int d = t; d < ZC + 10; d += NT) {
+    for (int d = t; d < c.zc + 10; d += NT) {
         int kk = z0 - 3 + d;
         if (g.bcz == LSGB_BC_PERIODIC) {
             while (kk < 0) kk += g.nz;
@@ -475,7 +476,7 @@ bool encode_field(CUtensorMap* m, const float* ptr, const Geo& g) {
 template <int STAGE, bool TMA, typename IDX>
 cudaError_t launch_one(const StageArgs& a, const Coef& c, const TmaMaps& tm, int* err, cudaStream_t st) {
     const dim3 block(TX, TY, 1);
-    const dim3 grid((a.g.nx + TX - 1) / TX, (a.g.ny + TY - 1) / TY, (a.g.nz + ZC - 1) / ZC);
+    const dim3 grid((a.g.nx + TX - 1) / TX, (a.g.ny + TY - 1) / TY, (a.g.nz + c.zc - 1) / c.zc);
     const size_t dyn = TMA ? (size_t)NSTAGE * NFIELD * FTILE * sizeof(float) : 0;
     auto kern = stage3d_f32_pair<STAGE, TMA, IDX>;
     if (TMA) {
@@ -512,6 +513,7 @@ cudaError_t launch_stage3d_f32_tiled(const StageArgs& a, int* err, cudaStream_t 
     c.s_l = (float)a.s_l;
     c.eps = (float)a.eps;
     c.dt = (float)a.dt;
+    c.zc = (a.tile == 16 || a.tile == 32) ? a.tile : MAXZC;
     TmaMaps tm;
     std::memset(&tm, 0, sizeof(tm));
     // bulk tensor copies need 16-byte row pitch and an error flag to report into

@@ -342,3 +342,150 @@ def _kernel_times(self):
 Solver.get_field = _get_field
 Solver.enable_timing = _enable_timing
 Solver.kernel_times = _kernel_times
+
+
+def _set_tile(self, tile: int):
+    _check(lib().lsgb_solver_set_tile(self._h, int(tile)))
+
+
+def _get_tile(self) -> int:
+    t = C.c_int()
+    _check(lib().lsgb_solver_get_tile(self._h, C.byref(t)))
+    return t.value
+
+
+def _autotune(self, reps: int = 3):
+    """Pick the fastest tile shape for this grid (lsgb_solver_autotune)."""
+    t = C.c_int()
+    ms = C.c_float()
+    _check(lib().lsgb_solver_autotune(self._h, int(reps), C.byref(t), C.byref(ms)))
+    return t.value, ms.value
+
+
+Solver.set_tile = _set_tile
+Solver.get_tile = _get_tile
+Solver.autotune = _autotune
+
+
+class _Borrowed(Solver):
+    """Solver handle owned by a Batch (not destroyed by Python)."""
+
+    def __init__(self, handle):
+        self._h = handle
+        self.precision = None
+        self.p = self.params()
+
+    def close(self):
+        self._h = C.c_void_p()
+
+
+class Batch:
+    """Many independent instances advanced together (lsgb_batch_*)."""
+
+    def __init__(self, precision: str = "f32", lanes: int = 8):
+        self._h = C.c_void_p()
+        prec = {"f64": PREC_F64, "f32": PREC_F32}[precision]
+        _check(lib().lsgb_batch_create(prec, int(lanes), C.byref(self._h)))
+        self.instances = []
+
+    def add(self, p: Params) -> Solver:
+        h = C.c_void_p()
+        idx = C.c_int()
+        _check(lib().lsgb_batch_add(self._h, C.byref(p), C.byref(h), C.byref(idx)))
+        s = _Borrowed(h)
+        self.instances.append(s)
+        return s
+
+    def autotune(self, reps: int = 3):
+        _check(lib().lsgb_batch_autotune(self._h, int(reps)))
+
+    def advance(self, n_steps: int):
+        _check(lib().lsgb_batch_advance(self._h, int(n_steps)))
+
+    def sync(self):
+        _check(lib().lsgb_batch_sync(self._h))
+
+    def stats(self):
+        a, b = C.c_int64(), C.c_int64()
+        _check(lib().lsgb_batch_stats(self._h, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
+    def stream_handle(self) -> int:
+        p = C.c_void_p()
+        _check(lib().lsgb_batch_stream(self._h, C.byref(p)))
+        return p.value or 0
+
+    def close(self):
+        if self._h:
+            for s in self.instances:
+                s.close()
+            lib().lsgb_batch_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+
+class Adjoint:
+    """Discrete adjoint of a solver's steps (lsgb_adjoint_*).
+
+    ``forward(n)`` advances the solver with checkpoints every
+    ``checkpoint_interval`` steps; ``backward(dL_dGT)`` (or the seed stored by
+    ``loss(seed=True)``) runs the reverse sweep; ``grad(name)`` returns
+    dL/d(name) for name in "G0", "sl", "u", "v", "w".  Destroy it before its
+    solver."""
+
+    _CODES = {"G0": 0, "u": 1, "v": 2, "w": 3, "sl": 4}
+
+    def __init__(self, solver: Solver, checkpoint_interval: int = 20):
+        self._h = C.c_void_p()
+        self.solver = solver
+        _check(lib().lsgb_adjoint_create(solver._h, int(checkpoint_interval), C.byref(self._h)))
+
+    def close(self):
+        if self._h:
+            lib().lsgb_adjoint_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def forward(self, n_steps: int):
+        _check(lib().lsgb_adjoint_forward(self._h, int(n_steps)))
+
+    def set_target(self, G_target, eps: float, layout: str = "ghosted"):
+        _check(lib().lsgb_adjoint_set_target(self._h, _ptr(G_target), _layout(layout), _mem(G_target),
+                                             C.c_double(eps)))
+
+    def loss(self, seed: bool = False) -> float:
+        r = C.c_double()
+        _check(lib().lsgb_adjoint_loss(self._h, int(seed), C.byref(r)))
+        return r.value
+
+    def backward(self, dL_dGT=None, layout: str = "ghosted"):
+        _check(lib().lsgb_adjoint_backward(self._h, _ptr(dL_dGT), _layout(layout), _mem(dL_dGT)))
+
+    def grad(self, which: str = "sl", layout: str = "compact", out=None):
+        p = self.solver.params()
+        if out is None:
+            out = np.empty(p.shape(layout), dtype=np.float64)
+        _check(lib().lsgb_adjoint_get_grad(self._h, self._CODES[which], _ptr(out), _layout(layout), _mem(out)))
+        return out

@@ -228,3 +228,23 @@ def cfl_dt(wl: Workload, u, v, w, cfl: float, epsilon: float = 1e-10) -> float:
     if speed < epsilon:
         speed = 2.0
     return cfl * min(wl.spacing) / speed
+
+
+def config4(n2d: int = 48, n3d: int = 48, n_vel: int = 8):
+    """Batched form: n2d 2D instances with N = round(exp(U(ln 64, ln 1024)))
+    per axis and n3d 3D instances with N = round(exp(U(ln 32, ln 192))); a
+    circle / sphere of radius U(0.15, 0.3) at a random centre, an n_vel-mode
+    random divergence-free velocity and S_L ~ U(0.05, 0.3) per instance."""
+    out = []
+    for j in range(n2d + n3d):
+        rng = np.random.default_rng(seed_for(4, j))
+        dim = 2 if j < n2d else 3
+        lo, hi = (64, 1024) if dim == 2 else (32, 192)
+        n = int(round(math.exp(rng.uniform(math.log(lo), math.log(hi)))))
+        r0 = float(rng.uniform(0.15, 0.3))
+        c = rng.uniform(0.3, 0.7, 3)
+        s_l = float(rng.uniform(0.05, 0.3))
+        ks, cs, ph = draw_modes(rng, dim, n_vel)
+        out.append(Workload(dim=dim, n=(n,) * dim, s_l=s_l, center=(float(c[0]), float(c[1]), float(c[2]) if dim == 3 else 0.0),
+                            r0=r0, vel_k=ks, vel_c=cs, vel_phase=ph))
+    return out

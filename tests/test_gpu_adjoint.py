@@ -1,0 +1,145 @@
+"""Discrete adjoint of the solver (needs a GB300).
+
+Checks, with the tolerances stated per test:
+  * FP64 adjoint vs central finite differences of the FP64 forward along
+    smooth random directions in S_L, G0 and u (relative step 1e-6; the
+    frozen upwind / Godunov / constraint choices do not flip at that step):
+    relative error <= 1e-5;
+  * the same directional derivative from finite differences of the oracle's
+    forward (the CPU restatement of the reference) on the ghosted layout;
+  * gradients are bit-identical for every checkpoint interval;
+  * the FP32 adjoint against the FP64 adjoint: relative L2 <= 1e-3;
+  * the torch autograd Function gives the native gradients.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def small(lsgb_mod, dim):
+    from lsgb import adjoint as adj
+    n, steps = (20, 12) if dim == 3 else (40, 15)
+    p, G0, u, v, w, sl, sl_t = adj.workload(n, steps, dim=dim, reinit_interval=5)
+    return adj, p, steps, G0, u, v, w, sl, sl_t
+
+
+def loss_of(prob, G0, u, sl, steps):
+    prob.G0, prob.u = G0, u
+    return prob.loss(sl, steps)
+
+
+@pytest.mark.parametrize("dim", [3, 2])
+def test_adjoint_matches_fd_f64(cuda, lsgb_mod, dim):
+    adj, p, steps, G0, u, v, w, sl, sl_t = small(lsgb_mod, dim)
+    prob = adj.Problem(p, G0, u, v, w, "f64", checkpoint=4)
+    try:
+        prob.target(sl_t, steps)
+        L, g_sl = prob.gradient(sl, steps)
+        g_G0 = prob.a.grad("G0")
+        g_u = prob.a.grad("u")
+        assert L > 0 and np.isfinite(g_sl).all() and np.abs(g_sl).max() > 0
+        checks = []
+        for q in range(3):
+            d = adj.fourier_field(sl.shape[::-1], 11 + q)
+            d /= np.linalg.norm(d)
+            h = 1e-6 * np.linalg.norm(sl)
+            fd = (loss_of(prob, G0, u, sl + h * d, steps) - loss_of(prob, G0, u, sl - h * d, steps)) / (2 * h)
+            checks.append(("sl", fd, float(np.sum(g_sl * d))))
+        d = adj.fourier_field(sl.shape[::-1], 31)
+        d /= np.linalg.norm(d)
+        h = 1e-6 * np.linalg.norm(G0)
+        fd = (loss_of(prob, G0 + h * d, u, sl, steps) - loss_of(prob, G0 - h * d, u, sl, steps)) / (2 * h)
+        checks.append(("G0", fd, float(np.sum(g_G0 * d))))
+        h = 1e-6 * np.linalg.norm(u)
+        fd = (loss_of(prob, G0, u + h * d, sl, steps) - loss_of(prob, G0, u - h * d, sl, steps)) / (2 * h)
+        checks.append(("u", fd, float(np.sum(g_u * d))))
+        prob.G0, prob.u = G0, u
+    finally:
+        prob.close()
+    for name, fd, ad in checks:
+        print(f"dim={dim} {name}: fd={fd:.10e} adjoint={ad:.10e} rel={abs(fd - ad) / abs(fd):.2e}")
+        assert abs(fd - ad) <= 1e-5 * abs(fd), (name, fd, ad)
+
+
+def test_adjoint_matches_fd_of_oracle(cuda, lsgb_mod, port):
+    from oracle import Problem as OProblem
+    adj, p, steps, G0, u, v, w, sl, sl_t = small(lsgb_mod, 3)
+    n = p.nx
+    pb = OProblem(n, n, n, dt=p.dt, s_l=p.s_l, enable_reinit=True, reinit_interval=5, reinit_iterations=2)
+    gh = lambda a: np.ascontiguousarray(np.pad(a, 3, mode="wrap"))
+    eps, dv = 1.5 / n, 1.0 / n ** 3
+
+    def oracle_loss(s_field, G_target):
+        out = port.run(pb, steps, gh(G0), gh(u), gh(v), gh(w), sl=gh(s_field))[3:-3, 3:-3, 3:-3]
+        h, ht = 0.5 * (1 - np.tanh(out / eps)), 0.5 * (1 - np.tanh(G_target / eps))
+        return 0.5 * np.sum((h - ht) ** 2) * dv
+
+    prob = adj.Problem(p, G0, u, v, w, "f64", checkpoint=5)
+    try:
+        gt = prob.target(sl_t, steps)
+        _, g_sl = prob.gradient(sl, steps)
+    finally:
+        prob.close()
+    for q in range(2):
+        d = adj.fourier_field(sl.shape[::-1], 51 + q)
+        d /= np.linalg.norm(d)
+        h = 1e-6 * np.linalg.norm(sl)
+        fd = (oracle_loss(sl + h * d, gt) - oracle_loss(sl - h * d, gt)) / (2 * h)
+        ad = float(np.sum(g_sl * d))
+        print(f"oracle fd={fd:.10e} adjoint={ad:.10e}")
+        assert abs(fd - ad) <= 1e-5 * abs(fd)
+
+
+def test_gradient_independent_of_checkpoint_interval(cuda, lsgb_mod):
+    adj, p, steps, G0, u, v, w, sl, sl_t = small(lsgb_mod, 3)
+    res = []
+    for ck in (1, 3, 50):
+        prob = adj.Problem(p, G0, u, v, w, "f64", checkpoint=ck)
+        try:
+            prob.target(sl_t, steps)
+            L, g = prob.gradient(sl, steps)
+            res.append((L, g, prob.a.grad("G0"), prob.a.grad("w")))
+        finally:
+            prob.close()
+    for r in res[1:]:
+        assert r[0] == res[0][0]
+        for a, b in zip(r[1:], res[0][1:]):
+            assert np.array_equal(a, b)
+
+
+def test_f32_adjoint_close_to_f64(cuda, lsgb_mod):
+    adj, p, steps, G0, u, v, w, sl, sl_t = small(lsgb_mod, 3)
+    out = {}
+    for prec in ("f64", "f32"):
+        prob = adj.Problem(p, G0, u, v, w, prec, checkpoint=6)
+        try:
+            prob.target(sl_t, steps)
+            out[prec] = prob.gradient(sl, steps)[1]
+        finally:
+            prob.close()
+    rel = np.linalg.norm(out["f32"] - out["f64"]) / np.linalg.norm(out["f64"])
+    print(f"f32 vs f64 adjoint: rel L2 {rel:.3e}")
+    assert rel <= 1e-3
+
+
+def test_torch_rollout_gradients(cuda, lsgb_mod):
+    import torch
+    adj, p, steps, G0, u, v, w, sl, sl_t = small(lsgb_mod, 3)
+    prob = adj.Problem(p, G0, u, v, w, "f64", checkpoint=4)
+    try:
+        gt = prob.target(sl_t, steps)
+        L_native, g_native = prob.gradient(sl, steps)
+        gG0_native = prob.a.grad("G0")
+    finally:
+        prob.close()
+    T = lambda a, rg=False: torch.tensor(a, dtype=torch.float64, device="cuda").contiguous().requires_grad_(rg)
+    tG0, tsl, tu, tv, tw = T(G0, True), T(sl, True), T(u, True), T(v), T(w)
+    GT = adj.rollout(tG0, tsl, tu, tv, tw, p, steps, "f64", 4)
+    L = adj.heaviside_loss(GT, T(gt), 1.5 * p.dx, p.dx ** 3)
+    L.backward()
+    assert abs(L.item() - L_native) <= 1e-12 * L_native
+    np.testing.assert_allclose(tsl.grad.cpu().numpy(), g_native, rtol=1e-9, atol=1e-12 * np.abs(g_native).max())
+    np.testing.assert_allclose(tG0.grad.cpu().numpy(), gG0_native, rtol=1e-9,
+                               atol=1e-12 * np.abs(gG0_native).max())
+    assert tu.grad is not None and tv.grad is None
