@@ -56,6 +56,7 @@ def parse():
     ap.add_argument("--batch-steps", type=int, default=200, help="RK3 steps of the batched form (0 = skip)")
     ap.add_argument("--adjoint-steps", type=int, default=300, help="RK3 steps of the adjoint form (0 = skip)")
     ap.add_argument("--adjoint-n", type=int, default=192)
+    ap.add_argument("--sample-steps", type=int, default=10, help="steps of the sample-surface frequency sweep (0 = skip)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--json-out", default=None)
     return ap.parse_args()
@@ -342,6 +343,7 @@ def measure_adjoint(torch, lsgb, n: int, steps: int, dist: Dist):
     p, G0, u, v, w, sl, sl_t = adj.workload(n, steps)
     stream = torch.cuda.Stream()
     prob = adj.Problem(p, G0, u, v, w, "f32", checkpoint=20)
+    prob.a.set_grads(sl=True, velocity=False)  # the workload's gradient is dL/dS_L
     prob.s.set_stream(stream)
     prob.target(sl_t, steps)
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
@@ -372,6 +374,45 @@ def measure_adjoint(torch, lsgb, n: int, steps: int, dist: Dist):
             "rk3_steps": steps, "checkpoint_interval": 20,
             "workload": f"config5 {n}^3 periodic, FP32-bulk, S_L(x) = 0.15 + 0.05 f(x) (8 modes), "
                         "reinit every 10, L = 1/2 sum (H(G_T) - H(G_target))^2 dV, eps = 1.5 dx"}
+
+
+def measure_sample(torch, lsgb, steps: int, dist: Dist, cpu: bool):
+    """The reference's sample surface as its frequency sweep runs it: 30
+    Bunsen-flame instances of 800 x 800 (forcing 5..50 step 5, 55..100 step 5,
+    110..200 step 10 Hz; sample/submit_all.sh), LLF WENO-5 + RK3 with the
+    anchored/periodic boundaries, FP64 and bit-exact.  One lsgb_sample_run
+    call advances all instances `steps` steps (CUDA events on its stream).
+    The CPU figure is the oracle port of the same loop on one instance."""
+    from lsgb import sample as smp
+    freqs = list(range(5, 51, 5)) + list(range(55, 101, 5)) + list(range(110, 201, 10))
+    nx, ny = smp.NX, smp.NY
+    dx, dy = smp.spacing(nx, ny)
+    G0 = torch.tensor(smp.bunsen(nx, ny), dtype=torch.float64, device="cuda")
+    stack = G0.unsqueeze(0).repeat(len(freqs), 1, 1).contiguous()
+    stream = torch.cuda.Stream()
+    t = smp.run(stack, G0, 2, dx, dy, freqs, stream=stream)  # warm
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    ev[0].record(stream)
+    smp.run(stack, G0, steps, dx, dy, freqs, t=t, stream=stream)
+    ev[1].record(stream)
+    torch.cuda.synchronize()
+    ms = dist.max(ev[0].elapsed_time(ev[1]))
+    cells = len(freqs) * nx * ny
+    out = {"value": dist.world * cells * steps / (ms * 1e-3) / 1e9, "unit": "Gcell-updates/s", "instances": len(freqs),
+           "grid": [nx, ny], "steps": steps, "ms": ms, "dtype": "f64",
+           "workload": "sample/main.cpp Bunsen flame, 30 forcing frequencies 5-200 Hz, 800x800, DT 2.5e-6, S_L 0.4"}
+    if cpu:
+        from oracle import SampleOracle
+        so = SampleOracle("port")
+        g0 = smp.bunsen(nx, ny)
+        n_cpu = 2
+        a = time.perf_counter()
+        so.run(g0, g0, n_cpu, dx, dy, smp.DT, smp.SL, smp.U0, smp.V0, smp.EPS_U, smp.EPS_V, 5)
+        el = time.perf_counter() - a
+        out["cpu_baseline"] = {"value": nx * ny * n_cpu / el / 1e9, "unit": "Gcell-updates/s",
+                               "cores": os.cpu_count(), "kind": "port",
+                               "sample": f"one instance, {n_cpu} steps, {el:.2f} s"}
+    return out
 
 
 def run_ours(args, dist: Dist):
@@ -477,6 +518,11 @@ def run_ours(args, dist: Dist):
     if args.batch_steps > 0:
         batched = measure_batched(torch, lsgb, syn, args.batch_steps, dist)
 
+    sample = None
+    if args.sample_steps > 0:
+        sample = measure_sample(torch, lsgb, args.sample_steps, dist,
+                                cpu=not args.no_cpu_baseline and dist.rank == 0 and dist.world == 1)
+
     adjoint = None
     if args.adjoint_steps > 0:
         adjoint = measure_adjoint(torch, lsgb, args.adjoint_n, args.adjoint_steps, dist)
@@ -510,6 +556,7 @@ def run_ours(args, dist: Dist):
             "reinit_avg_launch_ms": re_ms / max(re_n, 1),
             "batched": batched,
             "adjoint": adjoint,
+            "sample_sweep": sample,
         }
         s = json.dumps(line)
         print(s, flush=True)

@@ -306,6 +306,11 @@ LSGB_API int lsgb_batch_stream(lsgb_batch* b, void** stream);
 typedef struct lsgb_adjoint lsgb_adjoint;
 LSGB_API int lsgb_adjoint_create(lsgb_solver* s, int checkpoint_interval, lsgb_adjoint** out);
 LSGB_API int lsgb_adjoint_destroy(lsgb_adjoint* a);
+/* Parameter gradients the backward accumulates (default: both).  dL/dG_0 is
+ * always formed. */
+#define LSGB_GRAD_SL 1
+#define LSGB_GRAD_VELOCITY 2
+LSGB_API int lsgb_adjoint_set_grads(lsgb_adjoint* a, int mask);
 /* Advance the solver n_steps steps (same results as lsgb_solver_advance),
  * recording checkpoints; the solver ends at G_T. */
 LSGB_API int lsgb_adjoint_forward(lsgb_adjoint* a, int n_steps);
@@ -329,6 +334,75 @@ LSGB_API int lsgb_adjoint_get_grad(lsgb_adjoint* a, int which, double* out, int 
  * computeDeformationVelocity / updateDeformationVelocity
  * (Local_code/level-set_MPI_3D/include/initial_conditions.h:232-282). */
 LSGB_API int lsgb_solver_set_velocity_deformation(lsgb_solver* s, double t, double T);
+
+/* ------------------------------------------------------------------------
+ * Binary G dumps in the reference's .bin format: int32 {nx, ny, nz, nghost}
+ * (3D) or {nx, ny, nghost} (2D), then the whole ghosted FP64 array, whose x
+ * (and z) ghosts are what the boundary fill leaves and whose y ghosts copy the
+ * first / last interior row.  Replaces saveFieldBinary3D
+ * (Local_code/level-set_MPI_3D/include/io.h:33-131) and saveFieldBinary
+ * (Local_code/level-set_MPI_2D/include/io.h:26-109); the reference's doc
+ * comment promises a double[4] {time, dx, dy, dz} header block that its code
+ * never writes, and neither does this.
+ * ------------------------------------------------------------------------ */
+/* Bytes of one dump image (header + array). */
+LSGB_API int lsgb_dump_bytes(const lsgb_params* p, size_t* bytes);
+/* Image of a ghosted FP64 device array G into out (lsgb_dump_bytes bytes,
+ * host or device memory).  Synchronises the stream. */
+LSGB_API int lsgb_dump_f64(const lsgb_params* p, const double* G, void* out, int memory, void* stream);
+/* Image of a solver's current G (either precision; FP32 values widened). */
+LSGB_API int lsgb_solver_dump(lsgb_solver* s, void* out, int memory);
+/* Write the current G's image to the file `path` without stopping the time
+ * loop: the image is packed on the solver's stream, copied to pinned host
+ * memory on a second stream and written by a background thread (two images
+ * in flight; a third call waits for the older one).  Later steps may run
+ * while the file is written.  lsgb_solver_snapshot_wait waits for every
+ * pending file and reports the first failure. */
+LSGB_API int lsgb_solver_snapshot(lsgb_solver* s, const char* path);
+LSGB_API int lsgb_solver_snapshot_wait(lsgb_solver* s);
+
+/* ------------------------------------------------------------------------
+ * Sample surface: the reference's 2D Field2D solver (sample/field.hpp,
+ * sample/weno5_rk3.hpp).  Arrays are FP64 device buffers in Field2D's element
+ * order, row-major [ny+6][nx+6] with 3 ghost cells per side (the same map as
+ * LSGB_LAYOUT_GHOSTED in 2D), owned by the caller.  Results equal the
+ * reference's compiled sources bit for bit.  Calls are stream-ordered on
+ * `stream` (NULL = legacy default stream); `work` arguments are optional
+ * device scratch (NULL = stream-ordered allocation inside the call).
+ * ------------------------------------------------------------------------ */
+/* compute_geqn_rhs (sample/weno5_rk3.hpp:10-16, weno5_rk3.cpp:91-145): the
+ * local Lax-Friedrichs rhs = -H on the interior; ghost cells of rhs = 0. */
+LSGB_API int lsgb_sample_rhs(int nx, int ny, const double* G, const double* u, const double* v, double* rhs,
+                             double dx, double dy, double S_L, void* stream);
+/* RK3_step (sample/weno5_rk3.hpp:20-25, weno5_rk3.cpp:148-188): in place on
+ * G; work = 2 arrays. */
+LSGB_API int lsgb_sample_rk3_step(int nx, int ny, double* G, const double* u, const double* v, double dx,
+                                  double dy, double dt, double S_L, const double* G_initial, double* work,
+                                  void* stream);
+/* Field2D::apply_periodic / apply_anchored_bc (sample/field.hpp:15-18,
+ * field.cpp:16-63). */
+LSGB_API int lsgb_sample_apply_periodic(int nx, int ny, double* G, void* stream);
+LSGB_API int lsgb_sample_apply_anchored_bc(int nx, int ny, double* G, const double* G_initial, void* stream);
+/* Field2D::reinitialize (sample/field.hpp:20, field.cpp:66-129); work = 1 array. */
+LSGB_API int lsgb_sample_reinitialize(int nx, int ny, double* G, const double* G_initial, double dx, double dy,
+                                      int num_iters, double* work, void* stream);
+
+/* The forced time loop of sample/main.cpp:126-148 for n_steps steps, over
+ * n_inst instances at once (the reference runs one process per forcing
+ * frequency, sample/submit_all.sh): instance q is the array G + q (nx+6)(ny+6)
+ * with the spatially uniform velocity
+ *   u = u0 + eps_u v0 cos(2 pi freq[q] t),  v = v0 + eps_v v0 cos(2 pi freq[q] t)
+ * evaluated at its own time t[q], which advances by dt per step (host arrays
+ * freq and t; t is updated).  G_initial is one array shared by all instances
+ * (shared_initial != 0) or n_inst arrays.  work = 2 n_inst arrays.
+ * Synchronises the stream before returning. */
+typedef struct lsgb_sample_forcing {
+    double u0, v0, eps_u, eps_v;
+} lsgb_sample_forcing;
+LSGB_API int lsgb_sample_run(int n_inst, int nx, int ny, int n_steps, double* G, const double* G_initial,
+                             int shared_initial, double dx, double dy, double dt, double S_L,
+                             const lsgb_sample_forcing* forcing, const int* freq, double* t, double* work,
+                             void* stream);
 
 /* ------------------------------------------------------------------------
  * Synthetic benchmark fields, generated on the device (FP64 arithmetic).

@@ -14,9 +14,10 @@
 //   computeInterfaceVolume io.h:263                    lsgb::computeInterfaceVolume
 //   computeL2Error3D     io.h:229                      lsgb::computeL2Error3D
 //   calculateTimeStep    config.h:272                  lsgb::calculateTimeStep (field max)
+//   saveFieldBinary3D    io.h:33                       lsgb::saveFieldBinary3D (device array)
 //   2D: rk3TimeStep (2D rk3.h:168), reinitializeWithSwap (2D reinitialization.h:321),
 //       applyBoundaryConditions (2D boundary.h:217), computeInterfaceArea (2D io.h:225),
-//       computeL2Error (2D io.h:194)
+//       computeL2Error (2D io.h:194), saveFieldBinary (2D io.h:26)
 //
 // The caller's own SimParams type is read field by field (any struct with the
 // reference's member names works).  Arrays are CUDA device arrays in the
@@ -25,6 +26,7 @@
 // wrappers throw lsgb::Error with the library's message.
 #pragma once
 
+#include <cstdio>
 #include <stdexcept>
 #include <string>
 
@@ -32,6 +34,8 @@
 
 namespace lsgb {
 
+#ifndef LSGB_ERROR_DEFINED
+#define LSGB_ERROR_DEFINED
 struct Error : std::runtime_error {
     int code;
     Error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
@@ -40,6 +44,7 @@ struct Error : std::runtime_error {
 inline void check(int rc) {
     if (rc != LSGB_OK) throw Error(rc, std::string("lsgb: ") + lsgb_last_error());
 }
+#endif
 
 // Reference SimParams (3D, Local_code/level-set_MPI_3D/include/config.h:134-175)
 // -> lsgb_params.  Periodic on every axis, as applyBoundaryConditions3D.
@@ -179,6 +184,32 @@ inline double computeL2Error(const double* G, const double* G_ref, SimParams& pa
 }
 
 // ---- RAII handle over the device-resident fast path ---------------------------
+// The reference's binary dump of a ghosted device array: int32 header, then
+// the array with its y ghosts copied from the nearest interior row
+// (saveFieldBinary3D, io.h:33-131; the 2D saveFieldBinary, 2D io.h:26-109).
+// current_time is accepted for the signature; the reference does not write it.
+inline bool write_dump_file(const char* filename, const lsgb_params& p, const double* G) {
+    size_t n = 0;
+    check(lsgb_dump_bytes(&p, &n));
+    std::string buf(n, '\0');
+    check(lsgb_dump_f64(&p, G, &buf[0], LSGB_MEM_HOST, nullptr));
+    FILE* fp = std::fopen(filename, "wb");
+    if (!fp) return false;
+    const bool ok = std::fwrite(buf.data(), 1, n, fp) == n;
+    return std::fclose(fp) == 0 && ok;
+}
+
+template <class SimParams>
+inline bool saveFieldBinary3D(const char* filename, const double* G, SimParams& params, double current_time = 0.0) {
+    (void)current_time;
+    return write_dump_file(filename, params3d(params), G);
+}
+
+template <class SimParams>
+inline bool saveFieldBinary(const char* filename, const double* G, SimParams& params, bool periodic_y = true) {
+    return write_dump_file(filename, params2d(params, periodic_y), G);
+}
+
 class Solver {
   public:
     Solver(const lsgb_params& p, int precision = LSGB_PREC_F64) { check(lsgb_solver_create(&p, precision, &h_)); }

@@ -26,9 +26,12 @@ COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler",
 # per-file extra flags
 EXTRA = {
     "f64_kernels.cu": ["--fmad=false"],
+    "sample_kernels.cu": ["--fmad=false"],
+    # host arithmetic of the forced velocity must not contract (aarch64 gcc would)
+    "sample_api.cu": ["-Xcompiler", "-ffp-contract=off"],
 }
 SOURCES = ["api.cu", "f64_kernels.cu", "f32_kernels.cu", "reduce.cu", "synth.cu", "noalloc.cu", "stage3d_f32.cu",
-           "adjoint.cu"]
+           "adjoint.cu", "sample_kernels.cu", "sample_api.cu", "dump.cu"]
 
 
 def _nvcc() -> str:

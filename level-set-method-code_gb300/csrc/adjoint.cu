@@ -37,6 +37,16 @@ struct Idx {
 
 __device__ __forceinline__ int wrap(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
 
+// Reciprocal: IEEE in the FP64 adjoint; the approximate MUFU reciprocal in
+// the FP32 adjoint (its relative error, ~1e-7, is below FP32 rounding of the
+// sums it feeds).
+__device__ __forceinline__ double rcpx(double x) { return 1.0 / x; }
+__device__ __forceinline__ float rcpx(float x) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
 // WENO reconstruction f = sum_k w_k p_k over the candidate stencils of
 // (a0..a4) with linear weights (d0, d1, d2), and df/da.  With
 // alpha_k = d_k / (eps + beta_k)^2 and w_k = alpha_k / sum alpha:
@@ -54,17 +64,18 @@ __device__ __forceinline__ void weno_grad(R a0, R a1, R a2, R a3, R a4, R d0, R 
     const R q0 = eps + c1312 * e0 * e0 + (R)0.25 * h0 * h0;
     const R q1 = eps + c1312 * e1 * e1 + (R)0.25 * h1 * h1;
     const R q2 = eps + c1312 * e2 * e2 + (R)0.25 * h2 * h2;
-    const R al0 = d0 / (q0 * q0), al1 = d1 / (q1 * q1), al2 = d2 / (q2 * q2);
-    const R inv = (R)1 / (al0 + al1 + al2);
+    const R r0 = rcpx(q0), r1 = rcpx(q1), r2 = rcpx(q2);
+    const R al0 = d0 * r0 * r0, al1 = d1 * r1 * r1, al2 = d2 * r2 * r2;
+    const R inv = rcpx(al0 + al1 + al2);
     const R w0 = al0 * inv, w1 = al1 * inv, w2 = al2 * inv;
     const R sixth = (R)(1.0 / 6.0);
     const R p0 = ((R)2 * a0 - (R)7 * a1 + (R)11 * a2) * sixth;
     const R p1 = (-a1 + (R)5 * a2 + (R)2 * a3) * sixth;
     const R p2 = ((R)2 * a2 + (R)5 * a3 - a4) * sixth;
     f = w0 * p0 + w1 * p1 + w2 * p2;
-    const R c0 = (R)-2 * (p0 - f) * w0 / q0;
-    const R cc1 = (R)-2 * (p1 - f) * w1 / q1;
-    const R c2 = (R)-2 * (p2 - f) * w2 / q2;
+    const R c0 = (R)-2 * (p0 - f) * w0 * r0;
+    const R cc1 = (R)-2 * (p1 - f) * w1 * r1;
+    const R c2 = (R)-2 * (p2 - f) * w2 * r2;
     // dbeta_k / d(a_k, a_{k+1}, a_{k+2})
     const R b0l = c136 * e0 - (R)0.5 * h0, b0m = -c133 * e0, b0r = c136 * e0 + (R)0.5 * h0;
     const R b1l = c136 * e1 - (R)0.5 * h1, b1m = -c133 * e1, b1r = c136 * e1 + (R)0.5 * h1;
@@ -129,7 +140,7 @@ __global__ void __launch_bounds__(256) stage_adj_coef_kernel(AdjStageArgs a) {
         if (DIM == 3) s[2][d + 3] = G[ix.at(i, j, wrap(k + d, g.nz))];
     }
     const R S = a.sl ? ((const T*)a.sl)[c] : (R)a.s_l;
-    const R h[3] = {(R)a.dx, (R)a.dy, (R)a.dz};
+    const R ih[3] = {(R)(1.0 / a.dx), (R)(1.0 / a.dy), (R)(1.0 / a.dz)};
     R gr[3] = {(R)0, (R)0, (R)0};
     R gm = (R)1;
     const bool active = (double)S > a.eps;
@@ -137,17 +148,18 @@ __global__ void __launch_bounds__(256) stage_adj_coef_kernel(AdjStageArgs a) {
         R q = (R)0;
 #pragma unroll
         for (int ax = 0; ax < DIM; ++ax) {
-            gr[ax] = (s[ax][4] - s[ax][2]) / ((R)2 * h[ax]);
+            gr[ax] = (s[ax][4] - s[ax][2]) * ((R)0.5 * ih[ax]);
             q += gr[ax] * gr[ax];
         }
         gm = sqrt(q + (R)a.eps);
     }
+    const R igm = rcpx(gm);
     const T* vel[3] = {(const T*)a.u, (const T*)a.v, (const T*)a.w};
     R ue[3], D[3], dD[3][7];
 #pragma unroll
     for (int ax = 0; ax < DIM; ++ax) {
-        ue[ax] = vel[ax][c] - S * gr[ax] / gm;
-        axis_grad(s[ax], ue[ax], (R)1 / h[ax], D[ax], dD[ax]);
+        ue[ax] = vel[ax][c] - S * gr[ax] * igm;
+        axis_grad(s[ax], ue[ax], ih[ax], D[ax], dD[ax]);
     }
     // R = -(sum_a ue_a D_a);  dR/dg_b = S (D_b / gm - (D . g) g_b / gm^3);  dR/dS = (D . g) / gm
     R dg = (R)0;
@@ -160,8 +172,8 @@ __global__ void __launch_bounds__(256) stage_adj_coef_kernel(AdjStageArgs a) {
 #pragma unroll
     for (int ax = 0; ax < DIM; ++ax) {
         R dRg = (R)0;
-        if (active) dRg = S * (D[ax] / gm - dg * gr[ax] / (gm * gm * gm));
-        const R half = dRg / ((R)2 * h[ax]);
+        if (active) dRg = S * igm * (D[ax] - dg * gr[ax] * igm * igm);
+        const R half = dRg * ((R)0.5 * ih[ax]);
         centre += -ue[ax] * dD[ax][3];
 #pragma unroll
         for (int q = 0; q < 6; ++q) {
@@ -173,7 +185,7 @@ __global__ void __launch_bounds__(256) stage_adj_coef_kernel(AdjStageArgs a) {
         }
     }
     coef[c] = (T)(wc * centre);
-    if (a.gS) a.gS[c] += (double)(wc * (active ? dg / gm : (R)0));
+    if (a.gS) a.gS[c] += (double)(wc * (active ? dg * igm : (R)0));
     if (a.gu) {
         a.gu[c] += (double)(-wc * D[0]);
         a.gv[c] += (double)(-wc * D[1]);

@@ -5,9 +5,14 @@
 // keeps compact device-resident fields and sequences the kernels of
 // f64_kernels.cu / f32_kernels.cu / reduce.cu / synth.cu on one stream.
 #include "common.cuh"
+#include "host.hpp"
 
 #include <algorithm>
 #include <atomic>
+#include <condition_variable>
+#include <deque>
+#include <mutex>
+#include <thread>
 #include <cmath>
 #include <cstdarg>
 #include <cstring>
@@ -22,7 +27,7 @@ void count_launches(uint64_t n) { g_launches.fetch_add(n, std::memory_order_rela
 // launches recorded into a graph during capture run only when the graph does
 void uncount_launches(uint64_t n) { g_launches.fetch_sub(n, std::memory_order_relaxed); }
 
-namespace {
+// Host helpers shared with the other host-side translation units (host.hpp).
 
 thread_local std::string g_err;
 
@@ -36,19 +41,6 @@ int fail(int code, const char* fmt, ...) {
     return code;
 }
 
-#define LSGB_CUDA(call)                                                                  \
-    do {                                                                                 \
-        cudaError_t e_ = (call);                                                         \
-        if (e_ != cudaSuccess)                                                           \
-            return fail(LSGB_ERR_CUDA, "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), \
-                        __FILE__, __LINE__);                                             \
-    } while (0)
-
-#define LSGB_TRY(call)             \
-    do {                           \
-        int rc_ = (call);          \
-        if (rc_ != LSGB_OK) return rc_; \
-    } while (0)
 
 Geo geo_of(const lsgb_params& p) {
     Geo g;
@@ -144,7 +136,6 @@ int read_result(const double* dev, double* host2, cudaStream_t st) {
     return LSGB_OK;
 }
 
-}  // namespace
 }  // namespace lsgb
 
 using namespace lsgb;
@@ -359,6 +350,27 @@ struct lsgb_solver {
     std::vector<cudaEvent_t> ev_pool;
     size_t ev_used = 0;
     std::vector<std::pair<size_t, int>> ev_marks;  // (first event index, kind 0 stage / 1 reinit)
+    struct Snapshots* snap = nullptr;  // asynchronous dump writer (lsgb_solver_snapshot)
+};
+
+// Asynchronous dump files: the image is packed on the solver's stream into
+// one of two device slots, copied to a pinned host slot on a copy stream, and
+// written to its file by a writer thread, so the time loop keeps running.
+struct Snapshots {
+    int device = 0;
+    size_t hdr = 0, data = 0;          // header / array bytes of one image
+    double* dev[2] = {nullptr, nullptr};
+    char* host[2] = {nullptr, nullptr};
+    cudaEvent_t packed[2] = {nullptr, nullptr}, copied[2] = {nullptr, nullptr};
+    cudaStream_t cs = nullptr;
+    bool busy[2] = {false, false};
+    int next = 0;
+    std::mutex m;
+    std::condition_variable cv;
+    std::deque<std::pair<int, std::string>> jobs;
+    bool stop = false;
+    std::string err;                   // first failure, reported by lsgb_solver_snapshot_wait
+    std::thread th;
 };
 
 namespace {
@@ -561,9 +573,12 @@ extern "C" int lsgb_solver_create(const lsgb_params* p, int precision, lsgb_solv
     return LSGB_OK;
 }
 
+void snapshots_close(lsgb_solver* s);
+
 extern "C" int lsgb_solver_destroy(lsgb_solver* s) {
     if (!s) return LSGB_OK;
     if (s->st) cudaStreamSynchronize(s->st);
+    snapshots_close(s);
     void* ptrs[9] = {s->G, s->A, s->B, s->u, s->v, s->w, s->sl, s->stage64, s->scratch};
     for (void* q : ptrs)
         if (q) cudaFree(q);
@@ -1191,6 +1206,7 @@ struct lsgb_adjoint {
     int step0 = 0;             // solver step when that forward started
     bool have_fwd = false, have_seed = false, have_target = false, have_grad = false;
     double eps = 0.0;          // Heaviside width
+    int grads = LSGB_GRAD_SL | LSGB_GRAD_VELOCITY;  // parameter gradients accumulated
     size_t slot = 0;           // bytes per field slot (multiple of 256)
     int tape_slots = 0, ckpt_slots = 0;
     char* tape = nullptr;      // recompute tape of one segment
@@ -1335,10 +1351,11 @@ int adj_reverse_step(lsgb_adjoint* a, const TapeStep& t, void** L) {
     c.dy = s->p.dy;
     c.dz = s->p.dim == 3 ? s->p.dz : s->p.dx;
     c.coef = a->coef;
-    c.gS = a->grad[0];
-    c.gu = a->grad[1];
-    c.gv = a->grad[2];
-    c.gw = s->p.dim == 3 ? a->grad[3] : nullptr;
+    c.gS = (a->grads & LSGB_GRAD_SL) ? a->grad[0] : nullptr;
+    const bool vel = (a->grads & LSGB_GRAD_VELOCITY) != 0;
+    c.gu = vel ? a->grad[1] : nullptr;
+    c.gv = vel ? a->grad[2] : nullptr;
+    c.gw = vel && s->p.dim == 3 ? a->grad[3] : nullptr;
     AdjGatherArgs gt;
     std::memset(&gt, 0, sizeof(gt));
     gt.g = g;
@@ -1436,6 +1453,14 @@ extern "C" int lsgb_adjoint_destroy(lsgb_adjoint* a) {
     return LSGB_OK;
 }
 
+extern "C" int lsgb_adjoint_set_grads(lsgb_adjoint* a, int mask) {
+    LSGB_TRY(adj_ok(a));
+    if (mask & ~(LSGB_GRAD_SL | LSGB_GRAD_VELOCITY)) return fail(LSGB_ERR_INVALID, "unknown gradient bits 0x%x", mask);
+    a->grads = mask;
+    a->have_grad = false;
+    return LSGB_OK;
+}
+
 extern "C" int lsgb_adjoint_forward(lsgb_adjoint* a, int n_steps) {
     LSGB_TRY(adj_ok(a));
     lsgb_solver* s = a->s;
@@ -1530,7 +1555,8 @@ extern "C" int lsgb_adjoint_backward(lsgb_adjoint* a, const double* dL_dGT, int 
         a->tape_slots = need;
     }
     for (int b = 0; b < 4; ++b)
-        LSGB_CUDA(cudaMemsetAsync(a->grad[b], 0, sizeof(double) * (size_t)s->g.cells(), s->st));
+        if ((b == 0 && (a->grads & LSGB_GRAD_SL)) || (b > 0 && (a->grads & LSGB_GRAD_VELOCITY)))
+            LSGB_CUDA(cudaMemsetAsync(a->grad[b], 0, sizeof(double) * (size_t)s->g.cells(), s->st));
     // the current adjoint field lives in one of the four buffers
     void* L = a->lam[0];
     for (int seg = nseg - 1; seg >= 0; --seg) {
@@ -1566,12 +1592,226 @@ extern "C" int lsgb_adjoint_get_grad(lsgb_adjoint* a, int which, double* out, in
         return fail(LSGB_ERR_INVALID, "unknown memory kind %d", memory);
     switch (which) {
         case LSGB_FIELD_G: return store_compact(s, a->lam[0], s->prec == LSGB_PREC_F64, out, layout, memory);
-        case LSGB_FIELD_SL: return store_compact(s, a->grad[0], true, out, layout, memory);
-        case LSGB_FIELD_U: return store_compact(s, a->grad[1], true, out, layout, memory);
-        case LSGB_FIELD_V: return store_compact(s, a->grad[2], true, out, layout, memory);
+        case LSGB_FIELD_SL:
+            if (!(a->grads & LSGB_GRAD_SL)) return fail(LSGB_ERR_STATE, "dL/dS_L was not requested");
+            return store_compact(s, a->grad[0], true, out, layout, memory);
+        case LSGB_FIELD_U:
+        case LSGB_FIELD_V:
         case LSGB_FIELD_W:
-            if (s->p.dim != 3) return fail(LSGB_ERR_INVALID, "no w in 2D");
-            return store_compact(s, a->grad[3], true, out, layout, memory);
+            if (!(a->grads & LSGB_GRAD_VELOCITY)) return fail(LSGB_ERR_STATE, "velocity gradients were not requested");
+            if (which == LSGB_FIELD_W && s->p.dim != 3) return fail(LSGB_ERR_INVALID, "no w in 2D");
+            return store_compact(s, a->grad[which == LSGB_FIELD_U ? 1 : which == LSGB_FIELD_V ? 2 : 3], true, out,
+                                 layout, memory);
         default: return fail(LSGB_ERR_INVALID, "unknown field %d", which);
     }
+}
+
+// ---------------------------------------------------------------------------
+// binary dumps (dump.cu kernels)
+// ---------------------------------------------------------------------------
+
+namespace {
+
+// int32 header of saveFieldBinary3D (io.h:86-88) / 2D saveFieldBinary (2D io.h:86-88)
+size_t dump_header(const lsgb_params& p, int32_t* h) {
+    if (p.dim == 3) {
+        h[0] = p.nx; h[1] = p.ny; h[2] = p.nz; h[3] = p.nghost;
+        return 4 * sizeof(int32_t);
+    }
+    h[0] = p.nx; h[1] = p.ny; h[2] = p.nghost;
+    return 3 * sizeof(int32_t);
+}
+
+size_t dump_data_bytes(const Geo& g) { return sizeof(double) * (size_t)layout_elems(g, 1); }
+
+// the image's array part from the solver state into dst (device, aligned)
+int dump_pack_state(lsgb_solver* s, double* dst, cudaStream_t st) {
+    if (s->prec == LSGB_PREC_F64) LSGB_CUDA(launch_dump_compact<double>(s->g, (const double*)s->G, dst, st));
+    else LSGB_CUDA(launch_dump_compact<float>(s->g, (const float*)s->G, dst, st));
+    return LSGB_OK;
+}
+
+void snapshot_writer(Snapshots* sn) {
+    cudaSetDevice(sn->device);
+    for (;;) {
+        std::pair<int, std::string> job;
+        {
+            std::unique_lock<std::mutex> lk(sn->m);
+            sn->cv.wait(lk, [&] { return sn->stop || !sn->jobs.empty(); });
+            if (sn->jobs.empty()) return;
+            job = sn->jobs.front();
+            sn->jobs.pop_front();
+        }
+        std::string msg;
+        cudaError_t e = cudaEventSynchronize(sn->copied[job.first]);
+        if (e != cudaSuccess) {
+            msg = std::string("snapshot copy: ") + cudaGetErrorString(e);
+        } else {
+            FILE* f = std::fopen(job.second.c_str(), "wb");
+            const size_t n = sn->hdr + sn->data;
+            if (!f) msg = "cannot open " + job.second;
+            else {
+                if (std::fwrite(sn->host[job.first], 1, n, f) != n) msg = "short write to " + job.second;
+                if (std::fclose(f) != 0 && msg.empty()) msg = "close failed for " + job.second;
+            }
+        }
+        std::lock_guard<std::mutex> lk(sn->m);
+        if (!msg.empty() && sn->err.empty()) sn->err = msg;
+        sn->busy[job.first] = false;
+        sn->cv.notify_all();
+    }
+}
+
+int snapshots_open(lsgb_solver* s) {
+    if (s->snap) return LSGB_OK;
+    Snapshots* sn = new Snapshots();
+    int32_t h[4];
+    sn->hdr = dump_header(s->p, h);
+    sn->data = dump_data_bytes(s->g);
+    cudaGetDevice(&sn->device);
+    cudaError_t e = cudaStreamCreateWithFlags(&sn->cs, cudaStreamNonBlocking);
+    for (int k = 0; k < 2 && e == cudaSuccess; ++k) {
+        e = cudaMalloc((void**)&sn->dev[k], sn->data);
+        if (e == cudaSuccess) e = cudaMallocHost((void**)&sn->host[k], sn->hdr + sn->data);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&sn->packed[k], cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&sn->copied[k], cudaEventDisableTiming);
+    }
+    s->snap = sn;
+    if (e != cudaSuccess) {
+        std::string why = cudaGetErrorString(e);
+        snapshots_close(s);
+        return fail(LSGB_ERR_ALLOC, "snapshot buffers: %s", why.c_str());
+    }
+    sn->th = std::thread(snapshot_writer, sn);
+    return LSGB_OK;
+}
+
+}  // namespace
+
+void snapshots_close(lsgb_solver* s) {
+    Snapshots* sn = s->snap;
+    if (!sn) return;
+    if (sn->th.joinable()) {
+        {
+            std::lock_guard<std::mutex> lk(sn->m);
+            sn->stop = true;
+        }
+        sn->cv.notify_all();
+        sn->th.join();  // the writer drains the queue before it stops
+    }
+    for (int k = 0; k < 2; ++k) {
+        if (sn->dev[k]) cudaFree(sn->dev[k]);
+        if (sn->host[k]) cudaFreeHost(sn->host[k]);
+        if (sn->packed[k]) cudaEventDestroy(sn->packed[k]);
+        if (sn->copied[k]) cudaEventDestroy(sn->copied[k]);
+    }
+    if (sn->cs) cudaStreamDestroy(sn->cs);
+    delete sn;
+    s->snap = nullptr;
+}
+
+extern "C" int lsgb_dump_bytes(const lsgb_params* p, size_t* bytes) {
+    LSGB_TRY(check_params(p));
+    if (!bytes) return fail(LSGB_ERR_INVALID, "bytes is NULL");
+    int32_t h[4];
+    *bytes = dump_header(*p, h) + dump_data_bytes(geo_of(*p));
+    return LSGB_OK;
+}
+
+extern "C" int lsgb_dump_f64(const lsgb_params* p, const double* G, void* out, int memory, void* stream) {
+    LSGB_TRY(check_params(p));
+    LSGB_TRY(check_dev(G, "G"));
+    if (!out) return fail(LSGB_ERR_INVALID, "out is NULL");
+    if (memory != LSGB_MEM_HOST && memory != LSGB_MEM_DEVICE)
+        return fail(LSGB_ERR_INVALID, "unknown memory kind %d", memory);
+    if (memory == LSGB_MEM_DEVICE) LSGB_TRY(check_dev(out, "out"));
+    cudaStream_t st = (cudaStream_t)stream;
+    const Geo g = geo_of(*p);
+    int32_t h[4];
+    const size_t hb = dump_header(*p, h), db = dump_data_bytes(g);
+    double* tmp = nullptr;
+    cudaError_t e = cudaMallocAsync((void**)&tmp, db, st);
+    if (e != cudaSuccess) return fail(LSGB_ERR_ALLOC, "dump staging (%zu B): %s", db, cudaGetErrorString(e));
+    int rc = LSGB_OK;
+    e = launch_dump_ghosted(g, G, tmp, st);
+    if (e == cudaSuccess) {
+        char* o = (char*)out;
+        if (memory == LSGB_MEM_HOST) {
+            std::memcpy(o, h, hb);
+            e = cudaMemcpyAsync(o + hb, tmp, db, cudaMemcpyDeviceToHost, st);
+        } else {
+            e = cudaMemcpyAsync(o, h, hb, cudaMemcpyHostToDevice, st);
+            if (e == cudaSuccess) e = cudaMemcpyAsync(o + hb, tmp, db, cudaMemcpyDeviceToDevice, st);
+        }
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) rc = fail(LSGB_ERR_CUDA, "dump: %s", cudaGetErrorString(e));
+    cudaFreeAsync(tmp, st);
+    return rc;
+}
+
+extern "C" int lsgb_solver_dump(lsgb_solver* s, void* out, int memory) {
+    LSGB_TRY(solver_ok(s));
+    if (!out) return fail(LSGB_ERR_INVALID, "out is NULL");
+    if (!s->have_G) return fail(LSGB_ERR_STATE, "G has not been set");
+    if (memory != LSGB_MEM_HOST && memory != LSGB_MEM_DEVICE)
+        return fail(LSGB_ERR_INVALID, "unknown memory kind %d", memory);
+    if (memory == LSGB_MEM_DEVICE) LSGB_TRY(check_dev(out, "out"));
+    LSGB_TRY(ensure_stage(s));
+    int32_t h[4];
+    const size_t hb = dump_header(s->p, h), db = dump_data_bytes(s->g);
+    LSGB_TRY(dump_pack_state(s, s->stage64, s->st));
+    char* o = (char*)out;
+    if (memory == LSGB_MEM_HOST) {
+        std::memcpy(o, h, hb);
+        LSGB_CUDA(cudaMemcpyAsync(o + hb, s->stage64, db, cudaMemcpyDeviceToHost, s->st));
+    } else {
+        LSGB_CUDA(cudaMemcpyAsync(o, h, hb, cudaMemcpyHostToDevice, s->st));
+        LSGB_CUDA(cudaMemcpyAsync(o + hb, s->stage64, db, cudaMemcpyDeviceToDevice, s->st));
+    }
+    LSGB_CUDA(cudaStreamSynchronize(s->st));
+    return check_flag(s);
+}
+
+extern "C" int lsgb_solver_snapshot(lsgb_solver* s, const char* path) {
+    LSGB_TRY(solver_ok(s));
+    if (!path || !*path) return fail(LSGB_ERR_INVALID, "path is empty");
+    if (!s->have_G) return fail(LSGB_ERR_STATE, "G has not been set");
+    LSGB_TRY(snapshots_open(s));
+    Snapshots* sn = s->snap;
+    const int k = sn->next;
+    {
+        std::unique_lock<std::mutex> lk(sn->m);
+        sn->cv.wait(lk, [&] { return !sn->busy[k]; });  // the slot's previous file is written
+    }
+    LSGB_TRY(dump_pack_state(s, sn->dev[k], s->st));
+    LSGB_CUDA(cudaEventRecord(sn->packed[k], s->st));
+    LSGB_CUDA(cudaStreamWaitEvent(sn->cs, sn->packed[k], 0));
+    int32_t h[4];
+    dump_header(s->p, h);
+    std::memcpy(sn->host[k], h, sn->hdr);
+    LSGB_CUDA(cudaMemcpyAsync(sn->host[k] + sn->hdr, sn->dev[k], sn->data, cudaMemcpyDeviceToHost, sn->cs));
+    LSGB_CUDA(cudaEventRecord(sn->copied[k], sn->cs));
+    {
+        std::lock_guard<std::mutex> lk(sn->m);
+        sn->busy[k] = true;
+        sn->jobs.emplace_back(k, std::string(path));
+    }
+    sn->cv.notify_all();
+    sn->next = k ^ 1;
+    return LSGB_OK;
+}
+
+extern "C" int lsgb_solver_snapshot_wait(lsgb_solver* s) {
+    LSGB_TRY(solver_ok(s));
+    Snapshots* sn = s->snap;
+    if (!sn) return LSGB_OK;
+    std::unique_lock<std::mutex> lk(sn->m);
+    sn->cv.wait(lk, [&] { return sn->jobs.empty() && !sn->busy[0] && !sn->busy[1]; });
+    if (!sn->err.empty()) {
+        std::string e = sn->err;
+        sn->err.clear();
+        return fail(LSGB_ERR_INVALID, "snapshot: %s", e.c_str());
+    }
+    return LSGB_OK;
 }

@@ -218,6 +218,38 @@ template <typename T>
 cudaError_t launch_heaviside(const Geo& g, const T* G, const double* Gt, double eps, double dv, T* lam,
                              double* partials, double* out, cudaStream_t st);
 
+// Sample surface (sample_kernels.cu): n_inst Field2D arrays [ny+6][nx+6]
+// back to back.  Velocity: the ghosted fields u, v (same stride) or, when u
+// is NULL, the uniform pairs vel[2 (step n_inst + inst) + {0,1}] at
+// step = *ctr.  init: the anchoring field (init_stride 0 = shared).
+struct SampleArgs {
+    int nx, ny, n_inst;
+    const double* u;
+    const double* v;
+    const double* vel;
+    int* ctr;
+    const double* init;
+    long long init_stride;
+    double dx, dy, dt, S_L;
+};
+// stage 0 = the right-hand side alone (out = L(Gin)); 1..3 = RK3 stages
+cudaError_t sample_launch_stage(const SampleArgs& a, int stage, const double* Gin, const double* Gn, double* out,
+                                cudaStream_t st);
+// anchored + periodic pair after a stage; bump advances *ctr
+cudaError_t sample_launch_stage_bc(const SampleArgs& a, double* G, bool bump, cudaStream_t st);
+cudaError_t sample_launch_anchored(const SampleArgs& a, double* G, cudaStream_t st);
+cudaError_t sample_launch_periodic(const SampleArgs& a, double* G, cudaStream_t st);
+cudaError_t sample_launch_reinit_step(const SampleArgs& a, const double* phi, double* out, double dtau,
+                                      cudaStream_t st);
+cudaError_t sample_launch_zero_ghosts(const SampleArgs& a, double* G, cudaStream_t st);
+
+// The FP64 array part of the reference's binary dump (dump.cu): from a
+// compact state (x/z ghosts as the boundary fill leaves them, y ghosts =
+// nearest interior row) or from a caller's ghosted array (y ghosts replaced).
+template <typename T>
+cudaError_t launch_dump_compact(const Geo& g, const T* G, double* out, cudaStream_t st);
+cudaError_t launch_dump_ghosted(const Geo& g, const double* G, double* out, cudaStream_t st);
+
 // Bookkeeping of kernel launches (lsgb_launch_count).
 void count_launches(uint64_t n);
 

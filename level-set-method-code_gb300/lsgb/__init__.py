@@ -468,6 +468,10 @@ class Adjoint:
     def __exit__(self, *a):
         self.close()
 
+    def set_grads(self, sl: bool = True, velocity: bool = True):
+        """Which parameter gradients the backward accumulates (dL/dG0 always)."""
+        _check(lib().lsgb_adjoint_set_grads(self._h, (1 if sl else 0) | (2 if velocity else 0)))
+
     def forward(self, n_steps: int):
         _check(lib().lsgb_adjoint_forward(self._h, int(n_steps)))
 
@@ -489,3 +493,51 @@ class Adjoint:
             out = np.empty(p.shape(layout), dtype=np.float64)
         _check(lib().lsgb_adjoint_get_grad(self._h, self._CODES[which], _ptr(out), _layout(layout), _mem(out)))
         return out
+
+
+# -- binary dumps (the reference's .bin format) --------------------------------
+def dump_bytes(p: Params) -> int:
+    n = C.c_size_t()
+    _check(lib().lsgb_dump_bytes(C.byref(p), C.byref(n)))
+    return n.value
+
+
+def dump_f64(p: Params, G, stream=None) -> bytes:
+    """Image of a ghosted FP64 device array (saveFieldBinary3D / saveFieldBinary)."""
+    buf = np.empty(dump_bytes(p), dtype=np.uint8)
+    _check(lib().lsgb_dump_f64(C.byref(p), _ptr(G), C.c_void_p(buf.ctypes.data), MEM_HOST, _stream(stream)))
+    return buf.tobytes()
+
+
+def read_dump(data, dim: int):
+    """(header ints, ghosted array) of a dump image or file (3D header
+    {nx, ny, nz, nghost}, 2D {nx, ny, nghost})."""
+    if isinstance(data, (str, os.PathLike)):
+        with open(data, "rb") as f:
+            data = f.read()
+    nh = 4 if dim == 3 else 3
+    h = np.frombuffer(data, dtype=np.int32, count=nh)
+    g = int(h[-1])
+    shape = (int(h[2]) + 2 * g, int(h[1]) + 2 * g, int(h[0]) + 2 * g) if dim == 3 else (int(h[1]) + 2 * g, int(h[0]) + 2 * g)
+    arr = np.frombuffer(data, dtype=np.float64, offset=4 * nh).reshape(shape)
+    return [int(x) for x in h], arr
+
+
+def _solver_dump(self) -> bytes:
+    buf = np.empty(dump_bytes(self.params()), dtype=np.uint8)
+    _check(lib().lsgb_solver_dump(self._h, C.c_void_p(buf.ctypes.data), MEM_HOST))
+    return buf.tobytes()
+
+
+def _solver_snapshot(self, path: str):
+    """Write the current G's dump to `path` in the background."""
+    _check(lib().lsgb_solver_snapshot(self._h, os.fsencode(path)))
+
+
+def _solver_snapshot_wait(self):
+    _check(lib().lsgb_solver_snapshot_wait(self._h))
+
+
+Solver.dump = _solver_dump
+Solver.snapshot = _solver_snapshot
+Solver.snapshot_wait = _solver_snapshot_wait

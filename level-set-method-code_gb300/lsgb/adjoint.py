@@ -64,7 +64,7 @@ def sl_field(n, seed: int) -> np.ndarray:
 
 
 def workload(n: int = 192, steps: int = 300, dim: int = 3, cfl: float = 0.5, reinit_interval: int = 10,
-             reinit_iterations: int = 2):
+             reinit_iterations: int = 2, reinit: bool = True):
     """(params, G0, u, v, w, sl, sl_target) of the adjoint workload; fields in
     the compact layout, FP64 host arrays."""
     if dim == 3:
@@ -83,7 +83,7 @@ def workload(n: int = 192, steps: int = 300, dim: int = 3, cfl: float = 0.5, rei
     speed = np.abs(u) + np.abs(v) + (np.abs(w) if dim == 3 else 0.0)
     dt = cfl * (1.0 / n) / (float(speed.max()) + float(max(sl.max(), sl_t.max())))
     p = lsgb.params(dim, n, n, n if dim == 3 else 1, dx=1.0 / n, dy=1.0 / n, dz=1.0 / n, s_l=0.15, dt=dt,
-                    enable_reinit=True, reinit_interval=reinit_interval, reinit_iterations=reinit_iterations)
+                    enable_reinit=reinit, reinit_interval=reinit_interval, reinit_iterations=reinit_iterations)
     return p, G, u, v, w, sl, sl_t
 
 
@@ -126,21 +126,24 @@ class Problem:
         return L, self.a.grad("sl")
 
 
-def fd_check(prob: Problem, sl, n_steps: int, n_dirs: int, rel_step: float = 1e-3, seed: int = 7):
+def fd_check(prob: Problem, sl, n_steps: int, n_dirs: int, rel_step=1e-3, seed: int = 7):
     """Central differences of L along n_dirs random smooth unit directions d
-    (||d||_2 = 1 over the cells), step h = rel_step * ||S_L||_2, against
-    <dL/dS_L, d> of the adjoint."""
+    (||d||_2 = 1 over the cells), step h = rel_step * ||S_L||_2 (one step or a
+    list of steps), against <dL/dS_L, d> of the adjoint."""
     L, g = prob.gradient(sl, n_steps)
-    h = rel_step * float(np.linalg.norm(sl))
+    steps = [rel_step] if np.isscalar(rel_step) else list(rel_step)
     rows = []
     for q in range(n_dirs):
         d = fourier_field(sl.shape[::-1], seed * 1000 + q)
         d /= np.linalg.norm(d)
-        lp = prob.loss(sl + h * d, n_steps)
-        lm = prob.loss(sl - h * d, n_steps)
-        fd = (lp - lm) / (2 * h)
         ad = float(np.sum(g * d))
-        rows.append({"fd": fd, "adjoint": ad, "rel_err": abs(fd - ad) / max(abs(fd), 1e-300)})
+        for rs in steps:
+            h = rs * float(np.linalg.norm(sl))
+            lp = prob.loss(sl + h * d, n_steps)
+            lm = prob.loss(sl - h * d, n_steps)
+            fd = (lp - lm) / (2 * h)
+            rows.append({"dir": q, "rel_step": rs, "fd": fd, "adjoint": ad,
+                         "rel_err": abs(fd - ad) / max(abs(fd), 1e-300)})
     return L, g, rows
 
 
@@ -167,6 +170,7 @@ def _make_rollout():
             s.set_fields(G0, u, v, w if p.dim == 3 else None, layout="compact")
             s.set_sl_field(sl, layout="compact")
             a = lsgb.Adjoint(s, ckpt)
+            a.set_grads(sl=ctx.needs_input_grad[1], velocity=any(ctx.needs_input_grad[2:5]))
             a.forward(n_steps)
             out = torch.empty_like(G0)
             s.get_G(layout="compact", out=out)
@@ -219,12 +223,15 @@ def heaviside_loss(G, G_target, eps: float, dv: float):
 
 
 # -- report -------------------------------------------------------------------
-def report(n: int = 192, steps: int = 300, dirs: int = 32, checkpoint: int = 20, rel_step: float = 1e-3) -> dict:
+def report(n: int = 192, steps: int = 300, dirs: int = 32, checkpoint: int = 20, rel_step=1e-3,
+           reinit: bool = True) -> dict:
     import torch  # noqa: F401  (CUDA context for the timing events)
-    p, G0, u, v, w, sl, sl_t = workload(n, steps)
-    out = {"n": n, "steps": steps, "checkpoint": checkpoint, "dt": p.dt, "dirs": dirs, "rel_step": rel_step}
+    p, G0, u, v, w, sl, sl_t = workload(n, steps, reinit=reinit)
+    out = {"n": n, "steps": steps, "checkpoint": checkpoint, "dt": p.dt, "dirs": dirs, "rel_step": rel_step,
+           "reinit": reinit}
     # FP32 adjoint (the product form) and its cost against one plain forward
     p32 = Problem(p, G0, u, v, w, "f32", checkpoint)
+    p32.a.set_grads(sl=True, velocity=False)
     p32.target(sl_t, steps)
     p32.run(sl, steps)
     p32.s.volume()
@@ -240,15 +247,18 @@ def report(n: int = 192, steps: int = 300, dirs: int = 32, checkpoint: int = 20,
     p32.close()
     # FP64 adjoint and the finite differences of the FP64 forward
     p64 = Problem(p, G0, u, v, w, "f64", checkpoint)
+    p64.a.set_grads(sl=True, velocity=False)
     p64.target(sl_t, steps)
     t = time.perf_counter()
     L64, g64, rows = fd_check(p64, sl, steps, dirs, rel_step)
     out["seconds_fd_f64"] = time.perf_counter() - t
     p64.close()
-    rel = [r["rel_err"] for r in rows]
     out.update({"loss_f64": L64,
-                "grad_f32_vs_f64_rel_l2": float(np.linalg.norm(g32 - g64) / np.linalg.norm(g64)),
-                "fd_rel_err_max": max(rel), "fd_rel_err_median": float(np.median(rel)), "fd": rows})
+                "grad_f32_vs_f64_rel_l2": float(np.linalg.norm(g32 - g64) / np.linalg.norm(g64)), "fd": rows})
+    for rs in sorted({r["rel_step"] for r in rows}, reverse=True):
+        rel = [r["rel_err"] for r in rows if r["rel_step"] == rs]
+        out[f"fd_rel_err_max@{rs:g}"] = max(rel)
+        out[f"fd_rel_err_median@{rs:g}"] = float(np.median(rel))
     return out
 
 
@@ -258,12 +268,15 @@ def main():
     ap.add_argument("--steps", type=int, default=300)
     ap.add_argument("--dirs", type=int, default=32)
     ap.add_argument("--checkpoint", type=int, default=20)
-    ap.add_argument("--rel-step", type=float, default=1e-3)
+    ap.add_argument("--rel-step", type=float, nargs="+", default=[1e-3])
+    ap.add_argument("--no-reinit", action="store_true", help="drop HCR-2 (its crossing flags and stability "
+                    "mask make the forward map discontinuous)")
     ap.add_argument("--json", default=None)
     a = ap.parse_args()
     import __graft_entry__
     __graft_entry__.build_library()
-    r = report(a.n, a.steps, a.dirs, a.checkpoint, a.rel_step)
+    r = report(a.n, a.steps, a.dirs, a.checkpoint, a.rel_step if len(a.rel_step) > 1 else a.rel_step[0],
+               reinit=not a.no_reinit)
     if a.json:
         with open(a.json, "w") as f:
             json.dump(r, f, indent=2)

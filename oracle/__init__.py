@@ -1,2 +1,2 @@
 """CPU oracle of the level-set hot path (test infrastructure only; see oracle.py)."""
-from .oracle import Oracle, Problem, build_port, build_ref, ref_available  # noqa: F401
+from .oracle import Oracle, Problem, SampleOracle, build_port, build_ref, ref_available  # noqa: F401

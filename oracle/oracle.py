@@ -91,17 +91,17 @@ class Problem:
 
 
 def build_port(force: bool = False) -> str:
-    """Compile oracle/ls_oracle.c into oracle/_build/liboracle.so (gcc, OpenMP,
-    no FP contraction so every operation is the plain IEEE double op)."""
-    src = os.path.join(HERE, "ls_oracle.c")
+    """Compile oracle/ls_oracle.c and oracle/ls_oracle_sample.c into
+    oracle/_build/liboracle.so (gcc, OpenMP, no FP contraction so every
+    operation is the plain IEEE double op)."""
+    srcs = [os.path.join(HERE, "ls_oracle.c"), os.path.join(HERE, "ls_oracle_sample.c")]
     os.makedirs(BUILD_DIR, exist_ok=True)
-    if (not force and os.path.exists(PORT_LIB)
-            and os.path.getmtime(PORT_LIB) >= os.path.getmtime(src)
-            and os.path.getmtime(PORT_LIB) >= os.path.getmtime(os.path.join(HERE, "oracle_params.h"))):
+    deps = srcs + [os.path.join(HERE, "oracle_params.h")]
+    if not force and os.path.exists(PORT_LIB) and all(os.path.getmtime(PORT_LIB) >= os.path.getmtime(d) for d in deps):
         return PORT_LIB
     tmp = PORT_LIB + f".tmp{os.getpid()}"
     cmd = ["gcc", "-O2", "-std=c11", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off",
-           "-fno-fast-math", "-I", HERE, src, "-o", tmp, "-lm"]
+           "-fno-fast-math", "-I", HERE, *srcs, "-o", tmp, "-lm"]
     subprocess.run(cmd, check=True)
     os.replace(tmp, PORT_LIB)
     return PORT_LIB
@@ -283,6 +283,14 @@ class Oracle:
         assert self.kind == "port"
         return self._l3.orc_cfl_dt(C.byref(pb.c()), pb.dim, C.c_double(cfl), C.c_double(max_speed))
 
+    def save_binary(self, pb: Problem, G, path: str):
+        """The reference's own dump writer, saveFieldBinary3D / saveFieldBinary
+        (io.h), on a ghosted array (ref only)."""
+        assert self.kind == "ref"
+        self._chk(pb, G)
+        rc = self._f(pb, "save_binary")(C.byref(pb.c()), _ptr(G), path.encode())
+        assert rc == 0, "reference dump writer failed"
+
     # -- reference-only end-to-end case ------------------------------------
     def deformation_test(self):
         """The reference's default 64^3 sphere-deformation run (ref only)."""
@@ -291,3 +299,76 @@ class Oracle:
         st = C.c_int()
         self._l3.ref3d_deformation_test(C.byref(l2), C.byref(v0), C.byref(v1), C.byref(st), None)
         return l2.value, v0.value, v1.value, st.value
+
+
+class SampleOracle:
+    """The sample surface (sample/field.cpp, sample/weno5_rk3.cpp): 2D
+    Field2D arrays as float64 numpy arrays of shape (ny+6, nx+6).
+
+    ``kind="port"``: oracle/ls_oracle_sample.c (in liboracle.so);
+    ``kind="ref"``: the reference's own sources compiled by build_ref.sh
+    into oracle/_ref/libref_sample.so."""
+
+    def __init__(self, kind: str = "port"):
+        self.kind = kind
+        if kind == "port":
+            self._l = C.CDLL(build_port())
+            self._p = "orcs_"
+        elif kind == "ref":
+            path = os.path.join(REF_DIR, "libref_sample.so")
+            if not os.path.exists(path):
+                raise RuntimeError("oracle/_ref/libref_sample.so not built (reference tree absent?)")
+            self._l = C.CDLL(path)
+            self._p = "refs_"
+        else:
+            raise ValueError(kind)
+
+    def _fn(self, name):
+        return getattr(self._l, self._p + name)
+
+    @staticmethod
+    def _dims(G):
+        assert G.dtype == np.float64 and G.flags.c_contiguous and G.ndim == 2
+        return G.shape[1] - 6, G.shape[0] - 6
+
+    def rhs(self, G, u, v, dx, dy, S_L):
+        nx, ny = self._dims(G)
+        out = np.zeros_like(G)
+        self._fn("rhs")(nx, ny, _ptr(G), _ptr(u), _ptr(v), _ptr(out), C.c_double(dx), C.c_double(dy),
+                        C.c_double(S_L))
+        return out
+
+    def rk3_step(self, G, u, v, dx, dy, dt, S_L, G_initial):
+        nx, ny = self._dims(G)
+        out = G.copy()
+        self._fn("rk3_step")(nx, ny, _ptr(out), _ptr(u), _ptr(v), C.c_double(dx), C.c_double(dy), C.c_double(dt),
+                             C.c_double(S_L), _ptr(G_initial))
+        return out
+
+    def apply_periodic(self, G):
+        nx, ny = self._dims(G)
+        out = G.copy()
+        self._fn("apply_periodic")(nx, ny, _ptr(out))
+        return out
+
+    def apply_anchored_bc(self, G, G_initial):
+        nx, ny = self._dims(G)
+        out = G.copy()
+        self._fn("apply_anchored_bc")(nx, ny, _ptr(out), _ptr(G_initial))
+        return out
+
+    def reinitialize(self, G, G_initial, dx, dy, iters):
+        nx, ny = self._dims(G)
+        out = G.copy()
+        self._fn("reinitialize")(nx, ny, _ptr(out), _ptr(G_initial), C.c_double(dx), C.c_double(dy), int(iters))
+        return out
+
+    def run(self, G, G_initial, n_steps, dx, dy, dt, S_L, u0, v0, eps_u, eps_v, freq, t0=0.0):
+        """sample/main.cpp's time loop; returns (G, t)."""
+        nx, ny = self._dims(G)
+        out = G.copy()
+        t = C.c_double(t0)
+        self._fn("run")(nx, ny, int(n_steps), _ptr(out), _ptr(G_initial), C.c_double(dx), C.c_double(dy),
+                        C.c_double(dt), C.c_double(S_L), C.c_double(u0), C.c_double(v0), C.c_double(eps_u),
+                        C.c_double(eps_v), int(freq), C.byref(t))
+        return out, t.value

@@ -121,4 +121,11 @@ void ref2d_run(const orc_params* p, int n_steps, double* G, const double* u_in,
     std::memcpy(G, pG, sizeof(double) * n);
 }
 
+
+/* the reference's binary dump writer on a ghosted array (io.h) */
+int ref2d_save_binary(const orc_params* p, const double* G, const char* path) {
+    SimParams s = to_sim(p);
+    return saveFieldBinary(path, G, s) ? 0 : 1;
+}
+
 }  // extern "C"

@@ -173,4 +173,11 @@ void ref3d_deformation_velocity(double t, double* u, double* v, double* w) {
     initDeformationVelocity3D(u, v, w, params);
 }
 
+
+/* the reference's binary dump writer on a ghosted array (io.h) */
+int ref3d_save_binary(const orc_params* p, const double* G, const char* path) {
+    SimParams s = to_sim(p);
+    return saveFieldBinary3D(path, G, s, 0.0) ? 0 : 1;
+}
+
 }  // extern "C"

@@ -77,6 +77,8 @@ int main(int argc, char** argv) {
         std::fwrite(out.data(), sizeof(double), n, f);
         std::fclose(f);
         std::printf("volume %.17g\n", vol);
+        // the reference's end-of-run dump (src/main.cpp:378)
+        if (argc > 12 && !lsgb::saveFieldBinary3D(argv[12], G, sp, 0.0)) return 3;
     } catch (const lsgb::Error& e) {
         std::fprintf(stderr, "%s\n", e.what());
         return 1;

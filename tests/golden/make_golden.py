@@ -19,7 +19,8 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.join(ROOT, "level-set-method-code_gb300"))
 
-from oracle import Oracle, Problem, build_ref  # noqa: E402
+from oracle import Oracle, Problem, SampleOracle, build_ref  # noqa: E402
+from lsgb import sample as smp  # noqa: E402
 from lsgb import synthetic as syn  # noqa: E402
 
 
@@ -55,6 +56,7 @@ def main():
                         rk3_sl0=ref.rk3_step(Problem(**{**pb3.__dict__, "s_l": 0.0}), G, u, v, w),
                         reinit_phi=phi, reinit_phi0=phi0, reinit_rt=rt, reinit_flag=flag,
                         run10=run, vol_run10=ref.volume(pb3, run), l2_run10=ref.l2(pb3, run, G))
+    ref.save_binary(pb3, run, os.path.join(HERE, "dump_3d_small_run10.bin"))
 
     # 2D, periodic Y and zero-gradient Y
     for tag, per in (("periodic", True), ("zerograd", False)):
@@ -68,6 +70,7 @@ def main():
                             rk3=ref.rk3_step(pb2, G, u, v),
                             reinit_phi=phi, reinit_phi0=phi0, reinit_rt=rt, reinit_flag=flag,
                             run9=run, area_run9=ref.volume(pb2, run), l2_run9=ref.l2(pb2, run, G))
+        ref.save_binary(pb2, run, os.path.join(HERE, f"dump_2d_{tag}_run9.bin"))
 
     # configuration 1: 2D 128^2 circle, u = (1, 0), S_L = 0.1, CFL 0.5,
     # 400 steps, HCR-2 every 10 steps with 5 pseudo-steps
@@ -81,6 +84,27 @@ def main():
                         G_final=np.ascontiguousarray(fin[3:-3, 3:-3]), dt=dt,
                         area0=ref.volume(pb, G), area_final=ref.volume(pb, fin),
                         l2_final=ref.l2(pb, fin, G))
+
+    # sample surface (sample/field.cpp, sample/weno5_rk3.cpp): a Bunsen cone
+    # with noise, random velocity fields, the config.hpp physics
+    sref = SampleOracle("ref")
+    for tag, (nx, ny) in (("24x20", (24, 20)), ("3x3", (3, 3))):
+        rng = np.random.default_rng(syn.seed_for(92, nx))
+        G0 = smp.bunsen(nx, ny)
+        dx, dy = smp.spacing(nx, ny)
+        G = np.ascontiguousarray(G0 + 2e-4 * rng.standard_normal(G0.shape))
+        u = np.ascontiguousarray(0.3 * rng.standard_normal(G0.shape))
+        v = np.ascontiguousarray(0.8 + 0.3 * rng.standard_normal(G0.shape))
+        dt = 1e-4
+        run_f0, t_f0 = sref.run(G, G0, 25, dx, dy, dt, smp.SL, smp.U0, smp.V0, smp.EPS_U, smp.EPS_V, 0)
+        run_f50, t_f50 = sref.run(G, G0, 25, dx, dy, dt, smp.SL, smp.U0, smp.V0, smp.EPS_U, smp.EPS_V, 50)
+        np.savez_compressed(os.path.join(HERE, f"golden_sample_{tag}.npz"),
+                            G=G, G0=G0, u=u, v=v, dx=dx, dy=dy, dt=dt, S_L=smp.SL,
+                            rhs=sref.rhs(G, u, v, dx, dy, smp.SL),
+                            rk3=sref.rk3_step(G, u, v, dx, dy, dt, smp.SL, G0),
+                            periodic=sref.apply_periodic(G), anchored=sref.apply_anchored_bc(G, G0),
+                            reinit10=sref.reinitialize(G, G0, dx, dy, 10),
+                            run25_f0=run_f0, t25_f0=t_f0, run25_f50=run_f50, t25_f50=t_f50)
 
     # the reference's default 3D case end to end (its committed log pins it)
     l2, v0, v1, steps = ref.deformation_test()
