@@ -335,6 +335,23 @@ LSGB_API int lsgb_adjoint_get_grad(lsgb_adjoint* a, int which, double* out, int 
  * (Local_code/level-set_MPI_3D/include/initial_conditions.h:232-282). */
 LSGB_API int lsgb_solver_set_velocity_deformation(lsgb_solver* s, double t, double T);
 
+/* Error and conservation diagnostics of the reference's analysis script
+ * (Local_code/level-set_MPI_3D/scripts/analyze_error.m) between the solver's
+ * G and a reference field G_ref (FP64, given layout / memory), as one device
+ * reduction.  Synchronises. */
+typedef struct lsgb_diagnostics {
+    double l2, linf, l2_rel;        /* RMS and max of G - G_ref; l2 / RMS(G_ref)   (:33-44) */
+    double volume, volume_ref;      /* cells with G < 0 times the cell volume      (:88-98) */
+    double volume_smooth, volume_smooth_ref;  /* smoothed Heaviside of -G, eps = dx (:100-107, :264-271) */
+    double grad_mean, grad_std;     /* |grad G| (central differences) where |G| < 3 dx (:109-133) */
+    double iface_mean, iface_max;   /* interface distance: crossing points of each zero set
+                                       against the other, |G(p)| / |grad G(p)| (first order);
+                                       mean and max stand in for the contour mean / Hausdorff (:51-84) */
+    int64_t band_cells, iface_points;
+} lsgb_diagnostics;
+LSGB_API int lsgb_solver_diagnostics(lsgb_solver* s, const double* G_ref, int layout, int memory,
+                                     lsgb_diagnostics* out);
+
 /* ------------------------------------------------------------------------
  * Binary G dumps in the reference's .bin format: int32 {nx, ny, nz, nghost}
  * (3D) or {nx, ny, nghost} (2D), then the whole ghosted FP64 array, whose x

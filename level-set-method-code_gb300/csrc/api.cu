@@ -1815,3 +1815,58 @@ extern "C" int lsgb_solver_snapshot_wait(lsgb_solver* s) {
     }
     return LSGB_OK;
 }
+
+// ---------------------------------------------------------------------------
+// analyze_error.m diagnostics (diag.cu)
+// ---------------------------------------------------------------------------
+extern "C" int lsgb_solver_diagnostics(lsgb_solver* s, const double* G_ref, int layout, int memory,
+                                       lsgb_diagnostics* out) {
+    LSGB_TRY(solver_ok(s));
+    if (!G_ref || !out) return fail(LSGB_ERR_INVALID, "G_ref and out must be given");
+    if (!s->have_G) return fail(LSGB_ERR_STATE, "G has not been set");
+    if (layout != LSGB_LAYOUT_GHOSTED && layout != LSGB_LAYOUT_COMPACT)
+        return fail(LSGB_ERR_INVALID, "unknown layout %d", layout);
+    if (memory != LSGB_MEM_HOST && memory != LSGB_MEM_DEVICE)
+        return fail(LSGB_ERR_INVALID, "unknown memory kind %d", memory);
+    double* ref = nullptr;
+    double* scr = nullptr;
+    const size_t rb = sizeof(double) * (size_t)s->g.cells();
+    cudaError_t e = cudaMallocAsync((void**)&ref, rb, s->st);
+    if (e == cudaSuccess) e = cudaMallocAsync((void**)&scr, diag_scratch_bytes(), s->st);
+    if (e != cudaSuccess) {
+        if (ref) cudaFreeAsync(ref, s->st);
+        return fail(LSGB_ERR_ALLOC, "diagnostics scratch: %s", cudaGetErrorString(e));
+    }
+    int rc = load_f64_compact(s, ref, G_ref, layout, memory);
+    double r[14];
+    if (rc == LSGB_OK) {
+        const double dz = s->p.dim == 3 ? s->p.dz : s->p.dx;
+        e = s->prec == LSGB_PREC_F64
+                ? launch_diagnostics<double>(s->g, (const double*)s->G, ref, s->p.dx, s->p.dy, dz, scr, s->st)
+                : launch_diagnostics<float>(s->g, (const float*)s->G, ref, s->p.dx, s->p.dy, dz, scr, s->st);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(r, scr + (diag_scratch_bytes() / sizeof(double) - 14), sizeof(r),
+                                cudaMemcpyDeviceToHost, s->st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
+        if (e != cudaSuccess) rc = fail(LSGB_ERR_CUDA, "diagnostics: %s", cudaGetErrorString(e));
+    }
+    cudaFreeAsync(ref, s->st);
+    cudaFreeAsync(scr, s->st);
+    if (rc != LSGB_OK) return rc;
+    const double N = (double)s->g.cells(), dv = cell_volume(s->p);
+    out->l2 = std::sqrt(r[0] / N);
+    out->linf = r[1];
+    const double ref_rms = std::sqrt(r[2] / N);
+    out->l2_rel = ref_rms > 0.0 ? out->l2 / ref_rms : 0.0;
+    out->volume = r[3] * dv;
+    out->volume_ref = r[4] * dv;
+    out->volume_smooth = r[5] * dv;
+    out->volume_smooth_ref = r[6] * dv;
+    out->band_cells = (int64_t)r[7];
+    out->grad_mean = r[7] > 0.0 ? r[8] / r[7] : 0.0;
+    out->grad_std = r[7] > 1.0 ? std::sqrt(std::max(0.0, (r[9] - r[7] * out->grad_mean * out->grad_mean) / (r[7] - 1.0))) : 0.0;
+    out->iface_points = (int64_t)r[12];
+    out->iface_mean = r[12] > 0.0 ? r[10] / r[12] : 0.0;
+    out->iface_max = r[11];
+    return check_flag(s);
+}

@@ -250,6 +250,13 @@ template <typename T>
 cudaError_t launch_dump_compact(const Geo& g, const T* G, double* out, cudaStream_t st);
 cudaError_t launch_dump_ghosted(const Geo& g, const double* G, double* out, cudaStream_t st);
 
+// analyze_error.m diagnostics (diag.cu): 14 reduced values at
+// scratch + 14 * RED_BLOCKS (see diag.cu for their meaning).
+size_t diag_scratch_bytes();
+template <typename T>
+cudaError_t launch_diagnostics(const Geo& g, const T* G, const double* Gr, double dx, double dy, double dz,
+                               double* scratch, cudaStream_t st);
+
 // Bookkeeping of kernel launches (lsgb_launch_count).
 void count_launches(uint64_t n);
 

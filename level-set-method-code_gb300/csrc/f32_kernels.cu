@@ -73,7 +73,7 @@ struct F32Coef {
 
 // Fused RK3 stage on compact FP32 arrays, one thread per cell, periodic or
 // zero-gradient index mapping at the domain edges.
-template <int DIM, int STAGE>
+template <int DIM, int STAGE, typename IDX>
 __global__ void __launch_bounds__(256) stage_f32_kernel(Geo g, const float* __restrict__ Gin,
                                                         const float* __restrict__ Gn,
                                                         float* __restrict__ Gout,
@@ -85,17 +85,18 @@ __global__ void __launch_bounds__(256) stage_f32_kernel(Geo g, const float* __re
     int j = blockIdx.y * blockDim.y + threadIdx.y;
     int k = DIM == 3 ? blockIdx.z * blockDim.z + threadIdx.z : 0;
     if (i >= g.nx || j >= g.ny || k >= g.nz) return;
-    const long long sy = g.nx;
-    const long long sz = (long long)g.nx * g.ny;
-    const long long row = j * sy + k * sz;
-    const long long id = row + i;
+    const IDX sy = g.nx;
+    const IDX sz = (IDX)g.nx * g.ny;
+    const IDX plane = (IDX)k * sz;
+    const IDX row = (IDX)j * sy + plane;
+    const IDX id = row + i;
 
     float sx[7], syv[7], szv[7];
 #pragma unroll
     for (int d = -3; d <= 3; ++d) {
-        sx[d + 3] = __ldg(Gin + row + map_axis(i + d, g.nx, g.bcx));
-        syv[d + 3] = __ldg(Gin + (long long)map_axis(j + d, g.ny, g.bcy) * sy + k * sz + i);
-        if (DIM == 3) szv[d + 3] = __ldg(Gin + (long long)map_axis(k + d, g.nz, g.bcz) * sz + j * sy + i);
+        sx[d + 3] = __ldg(Gin + (row + map_axis(i + d, g.nx, g.bcx)));
+        syv[d + 3] = __ldg(Gin + ((IDX)map_axis(j + d, g.ny, g.bcy) * sy + plane + i));
+        if (DIM == 3) szv[d + 3] = __ldg(Gin + ((IDX)map_axis(k + d, g.nz, g.bcz) * sz + (IDX)j * sy + i));
     }
     const float s_l = sl ? __ldg(sl + id) : c.s_l;
     float ue = __ldg(u + id), ve = __ldg(v + id), we = 0.0f;
@@ -134,7 +135,15 @@ __global__ void __launch_bounds__(256) stage_f32_kernel(Geo g, const float* __re
 // r~ = phi0_c / sum(phi0 of crossing neighbours) (computeInterfaceCrossings3D,
 // :46-89) are recomputed from phi0 in FP64, and on flagged cells the forcing
 // and the update are formed in FP64 before the final rounding.
-template <int DIM>
+// Neighbour offset along one axis: +-stride inside, the periodic image or
+// the clamped cell (offset 0) at the ends.
+template <typename IDX>
+__device__ __forceinline__ IDX nb_off(int c, int n, int bc, IDX stride, bool up) {
+    if (up) return c < n - 1 ? stride : (bc == LSGB_BC_PERIODIC ? -(IDX)(n - 1) * stride : (IDX)0);
+    return c > 0 ? -stride : (bc == LSGB_BC_PERIODIC ? (IDX)(n - 1) * stride : (IDX)0);
+}
+
+template <int DIM, typename IDX>
 __global__ void __launch_bounds__(256) reinit_f32_kernel(Geo g, const float* __restrict__ phin,
                                                          const float* __restrict__ phi0,
                                                          float* __restrict__ phinew, float inv_dx,
@@ -145,17 +154,17 @@ __global__ void __launch_bounds__(256) reinit_f32_kernel(Geo g, const float* __r
     int j = blockIdx.y * blockDim.y + threadIdx.y;
     int k = DIM == 3 ? blockIdx.z * blockDim.z + threadIdx.z : 0;
     if (i >= g.nx || j >= g.ny || k >= g.nz) return;
-    const long long sy = g.nx;
-    const long long sz = (long long)g.nx * g.ny;
-    const long long id = j * sy + k * sz + i;
-    long long nb[6];
-    nb[0] = j * sy + k * sz + map_axis(i - 1, g.nx, g.bcx);
-    nb[1] = j * sy + k * sz + map_axis(i + 1, g.nx, g.bcx);
-    nb[2] = (long long)map_axis(j - 1, g.ny, g.bcy) * sy + k * sz + i;
-    nb[3] = (long long)map_axis(j + 1, g.ny, g.bcy) * sy + k * sz + i;
+    const IDX sy = g.nx;
+    const IDX sz = (IDX)g.nx * g.ny;
+    const IDX id = (IDX)j * sy + (IDX)k * sz + i;
+    IDX nb[6];
+    nb[0] = id + nb_off<IDX>(i, g.nx, g.bcx, (IDX)1, false);
+    nb[1] = id + nb_off<IDX>(i, g.nx, g.bcx, (IDX)1, true);
+    nb[2] = id + nb_off<IDX>(j, g.ny, g.bcy, sy, false);
+    nb[3] = id + nb_off<IDX>(j, g.ny, g.bcy, sy, true);
     if (DIM == 3) {
-        nb[4] = (long long)map_axis(k - 1, g.nz, g.bcz) * sz + j * sy + i;
-        nb[5] = (long long)map_axis(k + 1, g.nz, g.bcz) * sz + j * sy + i;
+        nb[4] = id + nb_off<IDX>(k, g.nz, g.bcz, sz, false);
+        nb[5] = id + nb_off<IDX>(k, g.nz, g.bcz, sz, true);
     }
     const float phi = __ldg(phin + id);
     const float ph0 = __ldg(phi0 + id);
@@ -244,9 +253,15 @@ cudaError_t launch_stage_f32(const StageArgs& a, cudaStream_t st) {
     const float* v = (const float*)a.v;
     const float* w = (const float*)a.w;
     const float* sl = (const float*)a.sl;
-#define LSGB_S32(D, S) stage_f32_kernel<D, S><<<gr, b, 0, st>>>(a.g, Gin, Gn, Gout, u, v, w, sl, c)
+#define LSGB_S32(D, S, I) stage_f32_kernel<D, S, I><<<gr, b, 0, st>>>(a.g, Gin, Gn, Gout, u, v, w, sl, c)
     if (a.g.dim == 3) return launch_stage3d_f32_tiled(a, a.err, st);
-    if (a.stage == 1) LSGB_S32(2, 1); else if (a.stage == 2) LSGB_S32(2, 2); else LSGB_S32(2, 3);
+    if (a.g.cells() < (1LL << 31) - 1) {  // 32-bit element offsets
+        if (a.stage == 1) LSGB_S32(2, 1, int); else if (a.stage == 2) LSGB_S32(2, 2, int); else LSGB_S32(2, 3, int);
+    } else {
+        if (a.stage == 1) LSGB_S32(2, 1, long long);
+        else if (a.stage == 2) LSGB_S32(2, 2, long long);
+        else LSGB_S32(2, 3, long long);
+    }
 #undef LSGB_S32
     count_launches(1);
     return cudaGetLastError();
@@ -260,10 +275,15 @@ cudaError_t launch_reinit_f32(const ReinitArgs& a, cudaStream_t st) {
     float* out = (float*)a.phinew;
     const float ix = (float)(1.0 / a.dx), iy = (float)(1.0 / a.dy), iz = (float)(1.0 / a.dz);
     const float dx2 = (float)(a.dx * a.dx);
-    if (a.g.dim == 3)
-        reinit_f32_kernel<3><<<gr, b, 0, st>>>(a.g, pn, p0, out, ix, iy, iz, dx2, (float)a.dtau, a.dx, a.dtau, a.beta);
-    else
-        reinit_f32_kernel<2><<<gr, b, 0, st>>>(a.g, pn, p0, out, ix, iy, iz, dx2, (float)a.dtau, a.dx, a.dtau, a.beta);
+    const bool small = a.g.cells() < (1LL << 31) - 1;  // 32-bit element offsets
+#define LSGB_R32(D, I) reinit_f32_kernel<D, I><<<gr, b, 0, st>>>(a.g, pn, p0, out, ix, iy, iz, dx2, (float)a.dtau, \
+                                                                  a.dx, a.dtau, a.beta)
+    if (a.g.dim == 3) {
+        if (small) LSGB_R32(3, int); else LSGB_R32(3, long long);
+    } else {
+        if (small) LSGB_R32(2, int); else LSGB_R32(2, long long);
+    }
+#undef LSGB_R32
     count_launches(1);
     return cudaGetLastError();
 }

@@ -34,7 +34,9 @@
 //   Pa' = (11g3-7g4+2g5)/6.
 // (d_k / q_k weights multiplied through by q0 q1 q2; one approximate
 // reciprocal per value.)  Cell i takes (L(i) - L(i-1)) / h if u_eff >= 0 and
-// (R(i+1) - R(i)) / h otherwise.
+// (R(i+1) - R(i)) / h otherwise.  In the code the indicators carry a factor
+// 144 and the weights a factor 10 (both cancel in the ratios), and the face
+// values a factor 6 that the derivative's 1/(6h) removes.
 #include "common.cuh"
 
 #include <cuda.h>
@@ -62,9 +64,6 @@ constexpr int RING = PW * PH - TX * TY;
 constexpr int RPT = (RING + NT - 1) / NT;
 constexpr int NQ = NQX + NQY;
 constexpr int NF = NFX + NFY;
-constexpr int QPT = (NQ + NT - 1) / NT;
-constexpr int FPT = (NF + NT - 1) / NT;
-constexpr int FROT = 96;        // face-task rotation (balances per-warp work)
 constexpr int MINB = 3;         // resident CTAs per SM the register budget targets
 constexpr int NSTAGE = 3;                // TMA pipeline depth (plane pairs in flight)
 constexpr int NFIELD = 5;                // u, v, w, G^n, S_L
@@ -95,31 +94,35 @@ __device__ __forceinline__ float2 div2(float2 n, float2 d) {
     return mul2(n, make_float2(rcp_approx(d.x), rcp_approx(d.y)));
 }
 
-// (1e-6 + beta)^2 of the triple (a, b, c); beta as computeSmoothnessIndicators
-// (weno5.h:28-37): 13/12 (a - 2b + c)^2 + 1/4 (c - a)^2.
+// 144 (1e-6 + beta)^2 of the triple (a, b, c), beta as computeSmoothnessIndicators
+// (weno5.h:28-37): 13/12 (a - 2b + c)^2 + 1/4 (c - a)^2.  The WENO weights are
+// ratios of products of two indicators each, so the common factor 144 cancels.
 __device__ __forceinline__ float2 qbeta(float2 a, float2 b, float2 c) {
     const float2 t = add2(fma2(c2(-2.0f), b, a), c);
     const float2 r = sub2(c, a);
-    const float2 B = fma2(mul2(c2(13.0f / 12.0f), t), t, mul2(mul2(c2(0.25f), r), r));
-    const float2 s = add2(B, c2(1.0e-6f));
+    const float2 s = fma2(mul2(c2(13.0f), t), t, fma2(mul2(c2(3.0f), r), r, c2(12.0e-6f)));
     return mul2(s, s);
 }
 
-// Both reconstructions at the face between cells f-1 and f.
+// Both reconstructions at the face between cells f-1 and f, times 6: the 1/6
+// of the candidate polynomials is folded into the derivative's 1/(6h).  The
+// weights are the reference's linear weights over the products of the other
+// two indicators, scaled by 10 (ratios are unchanged):
+//   L: (0.1 q(f-1) q(f), 0.6 q(f-2) q(f), 0.3 q(f-2) q(f-1)) x 10
+//   R: (0.3 q(f-1) q(f), 0.6 q(f+1) q(f-1), 0.1 q(f+1) q(f)) x 10
 __device__ __forceinline__ void face(float2 g0, float2 g1, float2 g2, float2 g3, float2 g4, float2 g5,
                                      float2 qm2, float2 qm1, float2 q0, float2 qp1, float2& L, float2& R) {
-    const float2 Pa = fma2(c2(1.0f / 3.0f), g0, fma2(c2(-7.0f / 6.0f), g1, mul2(c2(11.0f / 6.0f), g2)));
-    const float2 Pb = fma2(c2(-1.0f / 6.0f), g1, fma2(c2(5.0f / 6.0f), g2, mul2(c2(1.0f / 3.0f), g3)));
-    const float2 Pc = fma2(c2(1.0f / 3.0f), g2, fma2(c2(5.0f / 6.0f), g3, mul2(c2(-1.0f / 6.0f), g4)));
-    const float2 Pr = fma2(c2(11.0f / 6.0f), g3, fma2(c2(-7.0f / 6.0f), g4, mul2(c2(1.0f / 3.0f), g5)));
+    const float2 Pa = fma2(c2(2.0f), g0, fma2(c2(-7.0f), g1, mul2(c2(11.0f), g2)));
+    const float2 Pb = fma2(c2(5.0f), g2, fma2(c2(2.0f), g3, make_float2(-g1.x, -g1.y)));
+    const float2 Pc = fma2(c2(2.0f), g2, fma2(c2(5.0f), g3, make_float2(-g4.x, -g4.y)));
+    const float2 Pr = fma2(c2(11.0f), g3, fma2(c2(-7.0f), g4, mul2(c2(2.0f), g5)));
     const float2 q12 = mul2(qm1, q0);
-    const float2 lw0 = mul2(c2(0.1f), q12);
-    const float2 lw1 = mul2(c2(0.6f), mul2(qm2, q0));
-    const float2 lw2 = mul2(c2(0.3f), mul2(qm2, qm1));
-    const float2 rw0 = mul2(c2(0.3f), q12);
-    const float2 rw1 = mul2(c2(0.6f), mul2(qp1, qm1));
-    const float2 rw2 = mul2(c2(0.1f), mul2(qp1, q0));
-    L = div2(fma2(lw0, Pa, fma2(lw1, Pb, mul2(lw2, Pc))), add2(add2(lw0, lw1), lw2));
+    const float2 lw1 = mul2(c2(6.0f), mul2(qm2, q0));
+    const float2 lw2 = mul2(c2(3.0f), mul2(qm2, qm1));
+    const float2 rw0 = mul2(c2(3.0f), q12);
+    const float2 rw1 = mul2(c2(6.0f), mul2(qp1, qm1));
+    const float2 rw2 = mul2(qp1, q0);
+    L = div2(fma2(q12, Pa, fma2(lw1, Pb, mul2(lw2, Pc))), add2(add2(q12, lw1), lw2));
     R = div2(fma2(rw0, Pr, fma2(rw1, Pc, mul2(rw2, Pb))), add2(add2(rw0, rw1), rw2));
 }
 
@@ -215,40 +218,32 @@ stage3d_f32_pair(Geo g, const float* __restrict__ Gin, const float* __restrict__
         ring_s[r] = q < RING ? ly * PW + lx : -1;
         ring_g[r] = q < RING ? (IDX)wrapg(j0 + ly - 3, g.ny, g.bcy) * g.nx + wrapg(i0 + lx - 3, g.nx, g.bcx) : 0;
     }
-    // Indicator tasks: x-indicators of tile cells x in [-2, TX+1] (NQX), then
-    // y-indicators of tile cells y in [-2, TY+1] (NQY), one list so every warp
-    // carries 2 or 3 tasks.  Encoded: sample offset | (y-axis << 30).
-    int q_src[QPT], q_dst[QPT];
-#pragma unroll
-    for (int r = 0; r < QPT; ++r) {
-        const int q = t + r * NT;
-        q_dst[r] = q < NQ ? q : -1;
-        if (q < NQX) {
-            const int row = q / QXW, cx = q % QXW;
-            q_src[r] = (row + 3) * PW + cx;                  // P2[row+3][cx..cx+2]
-        } else {
-            const int qq = q - NQX, cy = qq / TX, cl = qq % TX;
-            q_src[r] = (cy * PW + cl + 3) | (1 << 30);       // P2[cy..cy+2][cl+3]
-        }
-    }
-    // Face tasks: x-faces (NFX) then y-faces (NFY), rotated so that the warps
-    // with a third face task are not the ones with a third indicator task.
-    int f_src[FPT], f_q[FPT], f_dst[FPT];
-#pragma unroll
-    for (int r = 0; r < FPT; ++r) {
-        const int f = ((t + FROT) % NT) + r * NT;
-        f_dst[r] = f < NF ? f : -1;
-        if (f < NFX) {
-            const int row = f / (TX + 1), fc = f % (TX + 1);
-            f_src[r] = (row + 3) * PW + fc;                  // P2[row+3][fc..fc+5]
-            f_q[r] = row * QXW + fc;                         // QA[row][fc..fc+3]
-        } else {
-            const int ff = f - NFX, rr = ff / TX, cl = ff % TX;
-            f_src[r] = (rr * PW + cl + 3) | (1 << 30);       // P2[rr..rr+5][cl+3]
-            f_q[r] = NQX + rr * TX + cl;                     // QY[rr..rr+3][cl]
-        }
-    }
-
+    // Indicator and face tasks, x and y in separate lists with compile-time
+    // strides.  Every thread has one task of each kind (slot A, index t);
+    // the remainder goes to whole warps (slot B): x-indicators 256..287 to
+    // threads 224..255, y-indicators 256..383 to threads 0..127, x-faces
+    // 256..263 to threads 248..255, y-faces 256..287 to threads 128..159, so
+    // no warp carries more than 3 + 3 tasks.  Offsets in float2 elements of
+    // one staged plane (P) and of the indicator array (QA).
+    //   x-indicator q: row q / QXW, column q % QXW -> P[row+3][cx..cx+2]
+    //   y-indicator q: cy = q / TX, cl = q % TX     -> P[cy..cy+2][cl+3]
+    //   x-face f: row f / (TX+1), fc = f % (TX+1)  -> P[row+3][fc..fc+5], QA[row][fc..fc+3]
+    //   y-face f: rr = f / TX, cl = f % TX          -> P[rr..rr+5][cl+3], QY[rr..rr+3][cl]
+    const int xi_a = (t / QXW + 3) * PW + t % QXW;
+    const bool has_xi_b = t >= NT - (NQX - NT);
+    const int xi_b = ((t + NQX - NT) / QXW + 3) * PW + (t + NQX - NT) % QXW;
+    const int yi_a = ty * PW + tx + 3;
+    const bool has_yi_b = t < NQY - NT;
+    const int yi_b = (ty + NT / TX) * PW + tx + 3;
+    const int fx_a_src = (t / (TX + 1) + 3) * PW + t % (TX + 1);
+    const int fx_a_q = (t / (TX + 1)) * QXW + t % (TX + 1);
+    const bool has_fx_b = t >= NT - (NFX - NT);
+    const int fxb = t + NFX - NT;  // face index of slot B
+    const int fx_b_src = (fxb / (TX + 1) + 3) * PW + fxb % (TX + 1);
+    const int fx_b_q = (fxb / (TX + 1)) * QXW + fxb % (TX + 1);
+    const bool has_fy_b = t >= NT / 2 && t < NT / 2 + (NFY - NT);
+    // y-face slot A = face (ty, tx): P[ty..ty+5][tx+3], QY[ty..ty+3][tx]
+    // y-face slot B = face (TY, tx)
     // plane offsets of z-indices z0-3 .. z1+6 (periodic wrap or clamp), one
     // table per CTA so the loop does no index arithmetic on z
     for (int d = t; d < c.zc + 10; d += NT) {
@@ -263,8 +258,7 @@ stage3d_f32_pair(Geo g, const float* __restrict__ Gin, const float* __restrict__
     }
 
     // ---- TMA pipeline prologue ----
-    auto issue = [&](int it) {
-        const int s = it % NSTAGE;
+    auto issue = [&](int it, int s) {
         const int kz = z0 + 2 * it;
         float* base = stg + s * NFIELD * FTILE;
         const uint32_t nf = 3 + (STAGE > 1 ? 1 : 0) + (has_sl ? 1 : 0);
@@ -281,7 +275,7 @@ stage3d_f32_pair(Geo g, const float* __restrict__ Gin, const float* __restrict__
     }
     __syncthreads();  // zoff table and barriers ready
     if (TMA && t == 0)
-        for (int it = 0; it < NSTAGE - 1 && it < niter; ++it) issue(it);
+        for (int it = 0; it < NSTAGE - 1 && it < niter; ++it) issue(it, it);
 
     // ---- z queues: G(k-3 .. k+4) and q_z(k-1 .. k+1) of the own column ----
     float zq[8];
@@ -306,6 +300,8 @@ stage3d_f32_pair(Geo g, const float* __restrict__ Gin, const float* __restrict__
                                    : make_float2(0.0f, 0.0f);
 
     int buf = 0;
+    int cs = 0;         // TMA stage of this iteration (it % NSTAGE)
+    uint32_t cph = 0;   // its mbarrier phase parity ((it / NSTAGE) & 1)
     for (int it = 0; it < niter; ++it) {
         const int k = z0 + 2 * it;
         const IDX* zo = zoff + 2 * it + 3;  // zo[d] = offset of plane k + d
@@ -339,21 +335,18 @@ stage3d_f32_pair(Geo g, const float* __restrict__ Gin, const float* __restrict__
             // the stage being refilled was last read in iteration it-1, which
             // every thread finished before the barrier above
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            issue(it + NSTAGE - 1);
+            issue(it + NSTAGE - 1, cs == 0 ? NSTAGE - 1 : cs - 1);
         }
 
         // ---- per-cell indicators (x, y in shared memory; z in registers) ----
-#pragma unroll
-        for (int r = 0; r < QPT; ++r)
-            if (q_dst[r] >= 0) {
-                const int st = (q_src[r] >> 30) ? PW : 1;
-                const float2* s = P + (q_src[r] & 0x3fffffff);
-                QA[q_dst[r]] = qbeta(s[0], s[st], s[2 * st]);
-            }
+        QA[t] = qbeta(P[xi_a], P[xi_a + 1], P[xi_a + 2]);
+        if (has_xi_b) QA[t + NQX - NT] = qbeta(P[xi_b], P[xi_b + 1], P[xi_b + 2]);
+        QA[NQX + t] = qbeta(P[yi_a], P[yi_a + PW], P[yi_a + 2 * PW]);
+        if (has_yi_b) QA[NQX + NT + t] = qbeta(P[yi_b], P[yi_b + PW], P[yi_b + 2 * PW]);
         // q_z(k+2), q_z(k+3): triples centred at k+2 and k+3
         const float2 qz_b = qbeta(make_float2(zq[4], zq[5]), make_float2(zq[5], zq[6]), make_float2(zq[6], zq[7]));
         if (TMA) {
-            const bool ok = mbar_wait(&mbar[it % NSTAGE], (uint32_t)((it / NSTAGE) & 1));
+            const bool ok = mbar_wait(&mbar[cs], cph);
             if (__syncthreads_or(!ok)) {
                 // a bulk copy did not arrive in time: flag it, give the copies
                 // still in flight a bounded chance to land, and leave
@@ -369,18 +362,36 @@ stage3d_f32_pair(Geo g, const float* __restrict__ Gin, const float* __restrict__
         }
 
         // ---- faces ----
-#pragma unroll
-        for (int r = 0; r < FPT; ++r)
-            if (f_dst[r] >= 0) {
-                const bool yf = f_src[r] >> 30;
-                const int st = yf ? PW : 1, qs = yf ? TX : 1;
-                const float2* s = P + (f_src[r] & 0x3fffffff);
-                const float2* q = QA + f_q[r];
-                float2 L, R;
-                face(s[0], s[st], s[2 * st], s[3 * st], s[4 * st], s[5 * st], q[0], q[qs], q[2 * qs], q[3 * qs], L, R);
-                FL[f_dst[r]] = L;
-                FR[f_dst[r]] = R;
+        {
+            float2 L, R;
+            const float2* sx = P + fx_a_src;
+            const float2* qx = QA + fx_a_q;
+            face(sx[0], sx[1], sx[2], sx[3], sx[4], sx[5], qx[0], qx[1], qx[2], qx[3], L, R);
+            FL[t] = L;
+            FR[t] = R;
+            if (has_fx_b) {
+                sx = P + fx_b_src;
+                qx = QA + fx_b_q;
+                face(sx[0], sx[1], sx[2], sx[3], sx[4], sx[5], qx[0], qx[1], qx[2], qx[3], L, R);
+                FL[fxb] = L;
+                FR[fxb] = R;
             }
+            const float2* sy = P + yi_a;  // P[ty][tx+3]
+            const float2* qy = QA + NQX + t;
+            face(sy[0], sy[PW], sy[2 * PW], sy[3 * PW], sy[4 * PW], sy[5 * PW], qy[0], qy[TX], qy[2 * TX],
+                 qy[3 * TX], L, R);
+            FL[NFX + t] = L;
+            FR[NFX + t] = R;
+            if (has_fy_b) {
+                // face row TY: P[TY..TY+5][tx+3], QY[TY..TY+3][tx]
+                sy = P + TY * PW + tx + 3;
+                qy = QA + NQX + TY * TX + tx;
+                face(sy[0], sy[PW], sy[2 * PW], sy[3 * PW], sy[4 * PW], sy[5 * PW], qy[0], qy[TX], qy[2 * TX],
+                     qy[3 * TX], L, R);
+                FL[NFX + TY * TX + tx] = L;
+                FR[NFX + TY * TX + tx] = R;
+            }
+        }
         // z faces k+1/2 and k+3/2 as one pair: samples G(k-2+m), G(k-1+m)
         float2 zL, zR;
         face(make_float2(zq[1], zq[2]), make_float2(zq[2], zq[3]), make_float2(zq[3], zq[4]),
@@ -391,7 +402,7 @@ stage3d_f32_pair(Geo g, const float* __restrict__ Gin, const float* __restrict__
 
         // ---- cell update for planes k, k+1 ----
         if (TMA) {
-            const float* sb = stg + (it % NSTAGE) * NFIELD * FTILE + ty * TX + tx;
+            const float* sb = stg + cs * NFIELD * FTILE + ty * TX + tx;
             uu = make_float2(sb[0 * FTILE], sb[0 * FTILE + TX * TY]);
             vv = make_float2(sb[1 * FTILE], sb[1 * FTILE + TX * TY]);
             ww = make_float2(sb[2 * FTILE], sb[2 * FTILE + TX * TY]);
@@ -443,6 +454,10 @@ stage3d_f32_pair(Geo g, const float* __restrict__ Gin, const float* __restrict__
         zprevL = zL.y;
         zprevR = zR.y;
         buf ^= 1;
+        if (++cs == NSTAGE) {
+            cs = 0;
+            cph ^= 1u;
+        }
     }
 }
 
@@ -504,9 +519,10 @@ cudaError_t launch_stage(const StageArgs& a, const Coef& c, const TmaMaps& tm, i
 
 cudaError_t launch_stage3d_f32_tiled(const StageArgs& a, int* err, cudaStream_t st) {
     Coef c;
-    c.inv_dx = (float)(1.0 / a.dx);
-    c.inv_dy = (float)(1.0 / a.dy);
-    c.inv_dz = (float)(1.0 / a.dz);
+    // face values carry a factor 6 (see face())
+    c.inv_dx = (float)(1.0 / (6.0 * a.dx));
+    c.inv_dy = (float)(1.0 / (6.0 * a.dy));
+    c.inv_dz = (float)(1.0 / (6.0 * a.dz));
     c.inv_2dx = (float)(1.0 / (2.0 * a.dx));
     c.inv_2dy = (float)(1.0 / (2.0 * a.dy));
     c.inv_2dz = (float)(1.0 / (2.0 * a.dz));

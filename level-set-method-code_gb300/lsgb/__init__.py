@@ -541,3 +541,24 @@ def _solver_snapshot_wait(self):
 Solver.dump = _solver_dump
 Solver.snapshot = _solver_snapshot
 Solver.snapshot_wait = _solver_snapshot_wait
+
+
+class Diagnostics(C.Structure):
+    """Mirror of ``lsgb_diagnostics`` (analyze_error.m's quantities)."""
+
+    _fields_ = [(n, C.c_double) for n in ("l2", "linf", "l2_rel", "volume", "volume_ref", "volume_smooth",
+                                          "volume_smooth_ref", "grad_mean", "grad_std", "iface_mean",
+                                          "iface_max")] + [("band_cells", C.c_int64), ("iface_points", C.c_int64)]
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
+def _solver_diagnostics(self, G_ref, layout: str = "ghosted") -> dict:
+    """Error / conservation diagnostics of G against G_ref (FP64)."""
+    d = Diagnostics()
+    _check(lib().lsgb_solver_diagnostics(self._h, _ptr(G_ref), _layout(layout), _mem(G_ref), C.byref(d)))
+    return d.as_dict()
+
+
+Solver.diagnostics = _solver_diagnostics
