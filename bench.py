@@ -48,7 +48,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--n", type=int, default=512)
+    ap.add_argument("--n", "--grid", dest="n", type=int, default=512)
     ap.add_argument("--fp64-steps", type=int, default=2, help="timed FP64 bench steps (0 = skip)")
     ap.add_argument("--e2e-steps", type=int, default=2, help="timed end-to-end calls (0 = skip)")
     ap.add_argument("--e2e-rk-steps", type=int, default=50, help="RK3 steps per end-to-end call")
@@ -405,9 +405,11 @@ def measure_sample(torch, lsgb, steps: int, dist: Dist, cpu: bool):
         from oracle import SampleOracle
         so = SampleOracle("port")
         g0 = smp.bunsen(nx, ny)
-        n_cpu = 2
+        g, tc, n_cpu = g0, 0.0, 0
         a = time.perf_counter()
-        so.run(g0, g0, n_cpu, dx, dy, smp.DT, smp.SL, smp.U0, smp.V0, smp.EPS_U, smp.EPS_V, 5)
+        while time.perf_counter() - a < 8.0:  # about 8 s of host work, whole chunks of 20 steps
+            g, tc = so.run(g, g0, 20, dx, dy, smp.DT, smp.SL, smp.U0, smp.V0, smp.EPS_U, smp.EPS_V, 5, tc)
+            n_cpu += 20
         el = time.perf_counter() - a
         out["cpu_baseline"] = {"value": nx * ny * n_cpu / el / 1e9, "unit": "Gcell-updates/s",
                                "cores": os.cpu_count(), "kind": "port",

@@ -88,29 +88,32 @@ __device__ __forceinline__ void weno_grad(R a0, R a1, R a2, R a3, R a4, R d0, R 
 }
 
 // Upwind WENO derivative D = (f_{i+1/2} - f_{i-1/2}) / h of the 7-point line
-// s[0..6] = G[i-3..i+3] (weno5_dx_3d, weno5.h:90-124) and dD/ds.
+// s[0..6] = G[i-3..i+3] (weno5_dx_3d, weno5.h:90-124) and dD/ds, without a
+// branch on the upwind direction: with w[m] = s[m] (vel >= 0) or s[6-m]
+// (vel < 0) both cases are X = f(w0..w4), Y = f(w1..w5) with linear weights
+// (0.1, 0.6, 0.3) or (0.3, 0.6, 0.1), and D = +-(Y - X) / h (weno5_left at
+// i -+ 1/2 in the first case, weno5_right on the mirrored stencils in the
+// second).  Lanes of a warp with different upwind directions follow one path.
 template <typename R>
 __device__ __forceinline__ void axis_grad(const R* s, R vel, R inv_h, R& D, R* dD) {
-    R fl, fr, tl[5], tr[5];
-    if (vel >= (R)0) {
-        weno_grad(s[0], s[1], s[2], s[3], s[4], (R)0.1, (R)0.6, (R)0.3, fl, tl);
-        weno_grad(s[1], s[2], s[3], s[4], s[5], (R)0.1, (R)0.6, (R)0.3, fr, tr);
-        dD[0] = -tl[0] * inv_h;
+    const bool p = vel >= (R)0;
+    R w[7];
 #pragma unroll
-        for (int q = 1; q <= 4; ++q) dD[q] = (tr[q - 1] - tl[q]) * inv_h;
-        dD[5] = tr[4] * inv_h;
-        dD[6] = (R)0;
-    } else {
-        // reversed stencils: f_{i-1/2} from s[5..1], f_{i+1/2} from s[6..2]
-        weno_grad(s[5], s[4], s[3], s[2], s[1], (R)0.3, (R)0.6, (R)0.1, fl, tl);
-        weno_grad(s[6], s[5], s[4], s[3], s[2], (R)0.3, (R)0.6, (R)0.1, fr, tr);
-        dD[0] = (R)0;
-        dD[1] = -tl[4] * inv_h;
+    for (int m = 0; m < 7; ++m) w[m] = p ? s[m] : s[6 - m];
+    const R d0 = p ? (R)0.1 : (R)0.3, d2 = p ? (R)0.3 : (R)0.1;
+    R X, Y, tX[5], tY[5];
+    weno_grad(w[0], w[1], w[2], w[3], w[4], d0, (R)0.6, d2, X, tX);
+    weno_grad(w[1], w[2], w[3], w[4], w[5], d0, (R)0.6, d2, Y, tY);
+    const R sg = p ? inv_h : -inv_h;
+    R dW[7];
+    dW[0] = -tX[0] * sg;
 #pragma unroll
-        for (int q = 2; q <= 5; ++q) dD[q] = (tr[6 - q] - tl[5 - q]) * inv_h;
-        dD[6] = tr[0] * inv_h;
-    }
-    D = (fr - fl) * inv_h;
+    for (int m = 1; m <= 4; ++m) dW[m] = (tY[m - 1] - tX[m]) * sg;
+    dW[5] = tY[4] * sg;
+    dW[6] = (R)0;
+#pragma unroll
+    for (int m = 0; m < 7; ++m) dD[m] = p ? dW[m] : dW[6 - m];
+    D = (Y - X) * sg;
 }
 
 // ---------------------------------------------------------------------------
@@ -129,15 +132,16 @@ __global__ void __launch_bounds__(256) stage_adj_coef_kernel(AdjStageArgs a) {
     const int k = DIM == 3 ? blockIdx.z * blockDim.z + threadIdx.z : 0;
     if (i >= g.nx || j >= g.ny || k >= g.nz) return;
     typedef T R;
-    const Idx ix{g.nx, g.ny, g.nz};
     const T* __restrict__ G = (const T*)a.Gin;
-    const long long c = ix.at(i, j, k);
+    const long long sy = g.nx, sz = (long long)g.nx * g.ny;
+    const long long c = i + sy * j + sz * k;
+    const T* Gc = G + c;
     R s[3][7];
 #pragma unroll
     for (int d = -3; d <= 3; ++d) {
-        s[0][d + 3] = G[ix.at(wrap(i + d, g.nx), j, k)];
-        s[1][d + 3] = G[ix.at(i, wrap(j + d, g.ny), k)];
-        if (DIM == 3) s[2][d + 3] = G[ix.at(i, j, wrap(k + d, g.nz))];
+        s[0][d + 3] = Gc[wrap(i + d, g.nx) - i];
+        s[1][d + 3] = Gc[(long long)(wrap(j + d, g.ny) - j) * sy];
+        if (DIM == 3) s[2][d + 3] = Gc[(long long)(wrap(k + d, g.nz) - k) * sz];
     }
     const R S = a.sl ? ((const T*)a.sl)[c] : (R)a.s_l;
     const R ih[3] = {(R)(1.0 / a.dx), (R)(1.0 / a.dy), (R)(1.0 / a.dz)};
@@ -166,8 +170,8 @@ __global__ void __launch_bounds__(256) stage_adj_coef_kernel(AdjStageArgs a) {
 #pragma unroll
     for (int ax = 0; ax < DIM; ++ax) dg += D[ax] * gr[ax];
     const R wc = (R)(a.cdt) * ((const T*)a.lam)[c];
-    T* coef = (T*)a.coef;
     const long long P = g.cells();
+    T* cp = (T*)a.coef + c;  // plane 0 of this cell; plane o at cp + o P
     R centre = (R)0;
 #pragma unroll
     for (int ax = 0; ax < DIM; ++ax) {
@@ -181,10 +185,10 @@ __global__ void __launch_bounds__(256) stage_adj_coef_kernel(AdjStageArgs a) {
             R v = -ue[ax] * dD[ax][sidx];
             if (sidx == 4) v += half;
             if (sidx == 2) v -= half;
-            coef[(long long)(1 + 6 * ax + q) * P + c] = (T)(wc * v);
+            cp[(1 + 6 * ax + q) * P] = (T)(wc * v);
         }
     }
-    coef[c] = (T)(wc * centre);
+    cp[0] = (T)(wc * centre);
     if (a.gS) a.gS[c] += (double)(wc * (active ? dg * igm : (R)0));
     if (a.gu) {
         a.gu[c] += (double)(-wc * D[0]);
@@ -202,27 +206,27 @@ __global__ void __launch_bounds__(256) stage_adj_gather_kernel(AdjGatherArgs a) 
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int k = DIM == 3 ? blockIdx.z * blockDim.z + threadIdx.z : 0;
     if (i >= g.nx || j >= g.ny || k >= g.nz) return;
-    const Idx ix{g.nx, g.ny, g.nz};
-    const long long m = ix.at(i, j, k);
+    const long long sy = g.nx, sz = (long long)g.nx * g.ny;
+    const long long m = i + sy * j + sz * k;
     const long long P = g.cells();
-    const T* __restrict__ coef = (const T*)a.coef;
+    const T* __restrict__ cm = (const T*)a.coef + m;  // plane 0 at cell m
     const T lam = ((const T*)a.lam)[m];
-    T sum = coef[m];
+    T sum = cm[0];
 #pragma unroll
     for (int q = 0; q < 6; ++q) {
         const int o = stage_off(q);
-        sum += coef[(long long)(1 + q) * P + ix.at(wrap(i - o, g.nx), j, k)];
+        sum += cm[(1 + q) * P + (wrap(i - o, g.nx) - i)];
     }
 #pragma unroll
     for (int q = 0; q < 6; ++q) {
         const int o = stage_off(q);
-        sum += coef[(long long)(7 + q) * P + ix.at(i, wrap(j - o, g.ny), k)];
+        sum += cm[(7 + q) * P + (long long)(wrap(j - o, g.ny) - j) * sy];
     }
     if (DIM == 3) {
 #pragma unroll
         for (int q = 0; q < 6; ++q) {
             const int o = stage_off(q);
-            sum += coef[(long long)(13 + q) * P + ix.at(i, j, wrap(k - o, g.nz))];
+            sum += cm[(13 + q) * P + (long long)(wrap(k - o, g.nz) - k) * sz];
         }
     }
     T out = (T)a.c_self * lam + sum;
