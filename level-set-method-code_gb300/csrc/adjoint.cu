@@ -23,6 +23,8 @@
 // bijection, so the gather is the exact transpose).
 #include "common.cuh"
 
+#include <type_traits>
+
 namespace lsgb {
 namespace {
 
@@ -194,6 +196,169 @@ __global__ void __launch_bounds__(256) stage_adj_coef_kernel(AdjStageArgs a) {
         a.gu[c] += (double)(-wc * D[0]);
         a.gv[c] += (double)(-wc * D[1]);
         if (DIM == 3) a.gw[c] += (double)(-wc * D[2]);
+    }
+}
+
+// ---- FP32 3D coefficient pass on plane pairs ---------------------------------
+// The same transpose as stage_adj_coef_kernel<float, 3>, for the cells
+// (i, j, k) and (i, j, k+1) of one thread at once: every per-cell quantity is
+// a float2 over the plane pair and the arithmetic runs as packed f32x2
+// operations (the mirrored stencil makes both cells follow one code path).
+__device__ __forceinline__ float2 f2(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 operator+(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 operator-(float2 a, float2 b) { return __ffma2_rn(f2(-1.0f), b, a); }
+__device__ __forceinline__ float2 operator*(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 operator-(float2 a) { return __fmul2_rn(f2(-1.0f), a); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 rcp2(float2 a) { return make_float2(rcpx(a.x), rcpx(a.y)); }
+__device__ __forceinline__ float2 sel2(bool px, bool py, float2 a, float2 b) {
+    return make_float2(px ? a.x : b.x, py ? a.y : b.y);
+}
+
+__device__ __forceinline__ void weno_grad2(float2 a0, float2 a1, float2 a2, float2 a3, float2 a4, float2 d0, float2 d2,
+                                           float2& f, float2* df) {
+    const float2 e0 = fma2(f2(-2.0f), a1, a0) + a2, e1 = fma2(f2(-2.0f), a2, a1) + a3, e2 = fma2(f2(-2.0f), a3, a2) + a4;
+    const float2 h0 = a2 - a0, h1 = a3 - a1, h2 = a4 - a2;
+    const float2 c1312 = f2(13.0f / 12.0f), q4 = f2(0.25f), eps = f2((float)ADJ_WENO_EPS);
+    const float2 q0 = fma2(c1312 * e0, e0, fma2(q4 * h0, h0, eps));
+    const float2 q1 = fma2(c1312 * e1, e1, fma2(q4 * h1, h1, eps));
+    const float2 q2 = fma2(c1312 * e2, e2, fma2(q4 * h2, h2, eps));
+    const float2 r0 = rcp2(q0), r1 = rcp2(q1), r2 = rcp2(q2);
+    const float2 al0 = d0 * r0 * r0, al1 = f2(0.6f) * r1 * r1, al2 = d2 * r2 * r2;
+    const float2 inv = rcp2(al0 + al1 + al2);
+    const float2 w0 = al0 * inv, w1 = al1 * inv, w2 = al2 * inv;
+    const float sixth = 1.0f / 6.0f;
+    const float2 p0 = fma2(f2(2.0f * sixth), a0, fma2(f2(-7.0f * sixth), a1, f2(11.0f * sixth) * a2));
+    const float2 p1 = fma2(f2(-sixth), a1, fma2(f2(5.0f * sixth), a2, f2(2.0f * sixth) * a3));
+    const float2 p2 = fma2(f2(2.0f * sixth), a2, fma2(f2(5.0f * sixth), a3, f2(-sixth) * a4));
+    f = fma2(w0, p0, fma2(w1, p1, w2 * p2));
+    const float2 c0 = f2(-2.0f) * (p0 - f) * w0 * r0;
+    const float2 cc1 = f2(-2.0f) * (p1 - f) * w1 * r1;
+    const float2 c2 = f2(-2.0f) * (p2 - f) * w2 * r2;
+    const float2 k136 = f2(13.0f / 6.0f), k133 = f2(-13.0f / 3.0f), hf = f2(0.5f);
+    const float2 b0l = fma2(k136, e0, -(hf * h0)), b0m = k133 * e0, b0r = fma2(k136, e0, hf * h0);
+    const float2 b1l = fma2(k136, e1, -(hf * h1)), b1m = k133 * e1, b1r = fma2(k136, e1, hf * h1);
+    const float2 b2l = fma2(k136, e2, -(hf * h2)), b2m = k133 * e2, b2r = fma2(k136, e2, hf * h2);
+    df[0] = fma2(w0, f2(2.0f * sixth), c0 * b0l);
+    df[1] = fma2(w0, f2(-7.0f * sixth), fma2(w1, f2(-sixth), fma2(c0, b0m, cc1 * b1l)));
+    df[2] = fma2(w0, f2(11.0f * sixth), fma2(w1, f2(5.0f * sixth), fma2(w2, f2(2.0f * sixth),
+                 fma2(c0, b0r, fma2(cc1, b1m, c2 * b2l)))));
+    df[3] = fma2(w1, f2(2.0f * sixth), fma2(w2, f2(5.0f * sixth), fma2(cc1, b1r, c2 * b2m)));
+    df[4] = fma2(w2, f2(-sixth), c2 * b2r);
+}
+
+__device__ __forceinline__ void axis_grad2(const float2* s, float2 vel, float inv_h, float2& D, float2* dD) {
+    const bool px = vel.x >= 0.0f, py = vel.y >= 0.0f;
+    float2 w[7];
+#pragma unroll
+    for (int m = 0; m < 7; ++m) w[m] = sel2(px, py, s[m], s[6 - m]);
+    const float2 d0 = make_float2(px ? 0.1f : 0.3f, py ? 0.1f : 0.3f);
+    const float2 d2 = make_float2(px ? 0.3f : 0.1f, py ? 0.3f : 0.1f);
+    float2 X, Y, tX[5], tY[5];
+    weno_grad2(w[0], w[1], w[2], w[3], w[4], d0, d2, X, tX);
+    weno_grad2(w[1], w[2], w[3], w[4], w[5], d0, d2, Y, tY);
+    const float2 sg = make_float2(px ? inv_h : -inv_h, py ? inv_h : -inv_h);
+    float2 dW[7];
+    dW[0] = -(tX[0] * sg);
+#pragma unroll
+    for (int m = 1; m <= 4; ++m) dW[m] = (tY[m - 1] - tX[m]) * sg;
+    dW[5] = tY[4] * sg;
+    dW[6] = f2(0.0f);
+#pragma unroll
+    for (int m = 0; m < 7; ++m) dD[m] = sel2(px, py, dW[m], dW[6 - m]);
+    D = (Y - X) * sg;
+}
+
+__global__ void __launch_bounds__(256, 2) stage_adj_coef_pair_kernel(AdjStageArgs a) {
+    const Geo g = a.g;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = 2 * (blockIdx.z * blockDim.z + threadIdx.z);
+    if (i >= g.nx || j >= g.ny || k >= g.nz) return;
+    const bool two = k + 1 < g.nz;  // an odd nz leaves the last thread one plane
+    const float* __restrict__ G = (const float*)a.Gin;
+    const long long sy = g.nx, sz = (long long)g.nx * g.ny;
+    const long long c = i + sy * j + sz * k;
+    const long long c1 = two ? c + sz : c;
+    const float* Gc = G + c;
+    float2 s[3][7];
+#pragma unroll
+    for (int d = -3; d <= 3; ++d) {
+        const int xo = wrap(i + d, g.nx) - i;
+        const long long yo = (long long)(wrap(j + d, g.ny) - j) * sy;
+        s[0][d + 3] = make_float2(Gc[xo], G[c1 + xo]);
+        s[1][d + 3] = make_float2(Gc[yo], G[c1 + yo]);
+    }
+    float zq[8];
+#pragma unroll
+    for (int d = 0; d < 8; ++d) zq[d] = Gc[(long long)(wrap(k - 3 + d, g.nz) - k) * sz];
+#pragma unroll
+    for (int d = 0; d < 7; ++d) s[2][d] = make_float2(zq[d], two ? zq[d + 1] : zq[d]);
+    const float* sl = (const float*)a.sl;
+    const float2 S = sl ? make_float2(sl[c], sl[c1]) : f2((float)a.s_l);
+    const float ih[3] = {(float)(1.0 / a.dx), (float)(1.0 / a.dy), (float)(1.0 / a.dz)};
+    const float epsf = (float)a.eps;
+    const bool actx = (double)S.x > a.eps, acty = (double)S.y > a.eps;
+    float2 gr[3], q = f2(0.0f);
+#pragma unroll
+    for (int ax = 0; ax < 3; ++ax) {
+        gr[ax] = (s[ax][4] - s[ax][2]) * f2(0.5f * ih[ax]);
+        gr[ax] = make_float2(actx ? gr[ax].x : 0.0f, acty ? gr[ax].y : 0.0f);
+        q = fma2(gr[ax], gr[ax], q);
+    }
+    const float2 gm = make_float2(actx ? sqrtf(q.x + epsf) : 1.0f, acty ? sqrtf(q.y + epsf) : 1.0f);
+    const float2 igm = rcp2(gm);
+    const float* vel[3] = {(const float*)a.u, (const float*)a.v, (const float*)a.w};
+    float2 ue[3], D[3], dD[3][7];
+#pragma unroll
+    for (int ax = 0; ax < 3; ++ax) {
+        ue[ax] = make_float2(vel[ax][c], vel[ax][c1]) - S * gr[ax] * igm;
+        axis_grad2(s[ax], ue[ax], ih[ax], D[ax], dD[ax]);
+    }
+    float2 dg = f2(0.0f);
+#pragma unroll
+    for (int ax = 0; ax < 3; ++ax) dg = fma2(D[ax], gr[ax], dg);
+    const float* lam = (const float*)a.lam;
+    const float2 wc = f2((float)a.cdt) * make_float2(lam[c], lam[c1]);
+    const long long P = g.cells();
+    float* cp0 = (float*)a.coef + c;
+    float* cp1 = (float*)a.coef + c1;
+    float2 centre = f2(0.0f);
+    const float2 igm2 = igm * igm;
+#pragma unroll
+    for (int ax = 0; ax < 3; ++ax) {
+        float2 dRg = S * igm * (D[ax] - dg * gr[ax] * igm2);
+        dRg = make_float2(actx ? dRg.x : 0.0f, acty ? dRg.y : 0.0f);
+        const float2 half = dRg * f2(0.5f * ih[ax]);
+        centre = centre - ue[ax] * dD[ax][3];
+#pragma unroll
+        for (int q6 = 0; q6 < 6; ++q6) {
+            const int sidx = stage_off(q6) + 3;
+            float2 v = -(ue[ax] * dD[ax][sidx]);
+            if (sidx == 4) v = v + half;
+            if (sidx == 2) v = v - half;
+            const float2 o = wc * v;
+            const long long po = (long long)(1 + 6 * ax + q6) * P;
+            cp0[po] = o.x;
+            if (two) cp1[po] = o.y;
+        }
+    }
+    const float2 oc = wc * centre;
+    cp0[0] = oc.x;
+    if (two) cp1[0] = oc.y;
+    if (a.gS) {
+        const float2 gs = wc * dg * igm;
+        a.gS[c] += (double)(actx ? gs.x : 0.0f);
+        if (two) a.gS[c1] += (double)(acty ? gs.y : 0.0f);
+    }
+    if (a.gu) {
+        double* gp[3] = {a.gu, a.gv, a.gw};
+#pragma unroll
+        for (int ax = 0; ax < 3; ++ax) {
+            const float2 gv = -(wc * D[ax]);
+            gp[ax][c] += (double)gv.x;
+            if (two) gp[ax][c1] += (double)gv.y;
+        }
     }
 }
 
@@ -437,7 +602,13 @@ template <typename T>
 cudaError_t launch_stage_adj(const AdjStageArgs& c, const AdjGatherArgs& gth, cudaStream_t st) {
     const dim3 b = cell_block(c.g), gr = cell_grid(c.g, b);
     if (c.g.dim == 3) {
-        stage_adj_coef_kernel<T, 3><<<gr, b, 0, st>>>(c);
+        if (std::is_same<T, float>::value) {
+            // plane pairs: half the threads along z
+            const dim3 gp(gr.x, gr.y, (unsigned)((c.g.nz + 2 * b.z - 1) / (2 * b.z)));
+            stage_adj_coef_pair_kernel<<<gp, b, 0, st>>>(c);
+        } else {
+            stage_adj_coef_kernel<T, 3><<<gr, b, 0, st>>>(c);
+        }
         stage_adj_gather_kernel<T, 3><<<gr, b, 0, st>>>(gth);
     } else {
         stage_adj_coef_kernel<T, 2><<<gr, b, 0, st>>>(c);
