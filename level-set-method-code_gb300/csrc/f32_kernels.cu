@@ -135,6 +135,60 @@ __global__ void __launch_bounds__(256) stage_f32_kernel(Geo g, const float* __re
 // r~ = phi0_c / sum(phi0 of crossing neighbours) (computeInterfaceCrossings3D,
 // :46-89) are recomputed from phi0 in FP64, and on flagged cells the forcing
 // and the update are formed in FP64 before the final rounding.
+// The pseudo-step at one cell from its value phi, phi0 and the neighbour
+// values pn / p0 in the order -x, +x, -y, +y (, -z, +z).
+template <int DIM>
+__device__ __forceinline__ float reinit_cell(float phi, float ph0, const float* pn, const float* p0, float inv_dx,
+                                             float inv_dy, float inv_dz, float dx2, float dtau_f, double dx,
+                                             double dtau, double beta) {
+    const float S = ph0 * rsqrtf(fmaf(ph0, ph0, dx2));
+    const bool pos = S > 0.0f;
+    float gsq = 0.0f;
+    const float inv[3] = {inv_dx, inv_dy, inv_dz};
+#pragma unroll
+    for (int ax = 0; ax < DIM; ++ax) {
+        const float dm = (phi - pn[2 * ax]) * inv[ax];
+        const float dp = (pn[2 * ax + 1] - phi) * inv[ax];
+        const float a = pos ? fmaxf(dm, 0.0f) : fminf(dm, 0.0f);
+        const float b = pos ? fminf(dp, 0.0f) : fmaxf(dp, 0.0f);
+        gsq += fmaxf(a * a, b * b);
+    }
+    const float term = -S * (sqrtf(gsq) - 1.0f);
+
+    // interface constraint.  The crossing test phi0_c * phi0_nb < 0 of
+    // computeInterfaceCrossings3D is a sign test: the exact product of two
+    // floats is never rounded to zero in FP64, so comparing signs in FP32
+    // decides it identically; only flagged cells go on to FP64 arithmetic.
+    int flag = 0;
+#pragma unroll
+    for (int q = 0; q < 2 * DIM; ++q)
+        if ((ph0 < 0.0f && p0[q] > 0.0f) || (ph0 > 0.0f && p0[q] < 0.0f)) flag |= 1 << q;
+    bool forced = false;
+    double outd = 0.0;
+    if (flag != 0) {
+        double sum0 = 0.0;
+        int cnt = 0;
+#pragma unroll
+        for (int q = 0; q < 2 * DIM; ++q)
+            if ((flag >> q) & 1) { sum0 += (double)p0[q]; cnt++; }
+        bool stable = (phi > 0.0f) == (ph0 > 0.0f);
+#pragma unroll
+        for (int q = 0; q < 2 * DIM; ++q)
+            if ((flag >> q) & 1) stable = stable && ((pn[q] > 0.0f) == (p0[q] > 0.0f));
+        if (stable) {
+            const double rt = (cnt > 0 && fabs(sum0) > 1e-15) ? (double)ph0 / sum0 : 0.0;
+            double sum = 0.0;
+#pragma unroll
+            for (int q = 0; q < 2 * DIM; ++q)
+                if ((flag >> q) & 1) sum += (double)pn[q];
+            const double forcing = beta * (rt * sum - (double)phi) / dx;
+            outd = (double)phi + dtau * ((double)term + forcing);
+            forced = true;
+        }
+    }
+    return forced ? (float)outd : fmaf(dtau_f, term, phi);
+}
+
 // Neighbour offset along one axis: +-stride inside, the periodic image or
 // the clamped cell (offset 0) at the ends.
 template <typename IDX>
@@ -174,54 +228,7 @@ __global__ void __launch_bounds__(256) reinit_f32_kernel(Geo g, const float* __r
         pn[q] = __ldg(phin + nb[q]);
         p0[q] = __ldg(phi0 + nb[q]);
     }
-    const float S = ph0 * rsqrtf(fmaf(ph0, ph0, dx2));
-    const bool pos = S > 0.0f;
-    float gsq = 0.0f;
-    const float inv[3] = {inv_dx, inv_dy, inv_dz};
-#pragma unroll
-    for (int ax = 0; ax < DIM; ++ax) {
-        const float dm = (phi - pn[2 * ax]) * inv[ax];
-        const float dp = (pn[2 * ax + 1] - phi) * inv[ax];
-        const float a = pos ? fmaxf(dm, 0.0f) : fminf(dm, 0.0f);
-        const float b = pos ? fminf(dp, 0.0f) : fmaxf(dp, 0.0f);
-        gsq += fmaxf(a * a, b * b);
-    }
-    const float term = -S * (sqrtf(gsq) - 1.0f);
-
-    // interface constraint.  The crossing test phi0_c * phi0_nb < 0 of
-    // computeInterfaceCrossings3D is a sign test: the exact product of two
-    // floats is never rounded to zero in FP64, so comparing signs in FP32
-    // decides it identically; only flagged cells go on to FP64 arithmetic.
-    int flag = 0;
-#pragma unroll
-    for (int q = 0; q < 2 * DIM; ++q)
-        if ((ph0 < 0.0f && p0[q] > 0.0f) || (ph0 > 0.0f && p0[q] < 0.0f)) flag |= 1 << q;
-    float out;
-    bool forced = false;
-    double outd = 0.0;
-    if (flag != 0) {
-        double sum0 = 0.0;
-        int cnt = 0;
-#pragma unroll
-        for (int q = 0; q < 2 * DIM; ++q)
-            if ((flag >> q) & 1) { sum0 += (double)p0[q]; cnt++; }
-        bool stable = (phi > 0.0f) == (ph0 > 0.0f);
-#pragma unroll
-        for (int q = 0; q < 2 * DIM; ++q)
-            if ((flag >> q) & 1) stable = stable && ((pn[q] > 0.0f) == (p0[q] > 0.0f));
-        if (stable) {
-            const double rt = (cnt > 0 && fabs(sum0) > 1e-15) ? (double)ph0 / sum0 : 0.0;
-            double sum = 0.0;
-#pragma unroll
-            for (int q = 0; q < 2 * DIM; ++q)
-                if ((flag >> q) & 1) sum += (double)pn[q];
-            const double forcing = beta * (rt * sum - (double)phi) / dx;
-            outd = (double)phi + dtau * ((double)term + forcing);
-            forced = true;
-        }
-    }
-    out = forced ? (float)outd : fmaf(dtau_f, term, phi);
-    phinew[id] = out;
+    phinew[id] = reinit_cell<DIM>(phi, ph0, pn, p0, inv_dx, inv_dy, inv_dz, dx2, dtau_f, dx, dtau, beta);
 }
 
 inline dim3 cell_block(const Geo& g) { return g.dim == 3 ? dim3(32, 4, 2) : dim3(32, 8, 1); }
