@@ -311,6 +311,11 @@ LSGB_API int lsgb_adjoint_destroy(lsgb_adjoint* a);
 #define LSGB_GRAD_SL 1
 #define LSGB_GRAD_VELOCITY 2
 LSGB_API int lsgb_adjoint_set_grads(lsgb_adjoint* a, int mask);
+/* z planes per slab of the 3D stage transpose (0 = the default, one slab for
+ * the whole domain).  Smaller slabs keep each slab's 19 coefficient planes
+ * L2-resident between the two passes at the cost of a 3-plane halo recompute
+ * and more launches.  Any slab gives bit-identical gradients. */
+LSGB_API int lsgb_adjoint_set_slab(lsgb_adjoint* a, int planes);
 /* Advance the solver n_steps steps (same results as lsgb_solver_advance),
  * recording checkpoints; the solver ends at G_T. */
 LSGB_API int lsgb_adjoint_forward(lsgb_adjoint* a, int n_steps);

@@ -38,6 +38,11 @@ struct Idx {
 };
 
 __device__ __forceinline__ int wrap(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
+// any integer onto [0, n)
+__device__ __forceinline__ int wrapn(int i, int n) {
+    i %= n;
+    return i < 0 ? i + n : i;
+}
 
 // Reciprocal: IEEE in the FP64 adjoint; the approximate MUFU reciprocal in
 // the FP32 adjoint (its relative error, ~1e-7, is below FP32 rounding of the
@@ -131,8 +136,11 @@ __global__ void __launch_bounds__(256) stage_adj_coef_kernel(AdjStageArgs a) {
     const Geo g = a.g;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
-    const int k = DIM == 3 ? blockIdx.z * blockDim.z + threadIdx.z : 0;
-    if (i >= g.nx || j >= g.ny || k >= g.nz) return;
+    const int kl = DIM == 3 ? blockIdx.z * blockDim.z + threadIdx.z : 0;  // slab-local plane
+    if (i >= g.nx || j >= g.ny || kl >= (DIM == 3 ? a.zn + 6 : 1)) return;
+    const int ku = DIM == 3 ? a.z0 - 3 + kl : 0;  // unwrapped plane
+    const int k = DIM == 3 ? wrapn(ku, g.nz) : 0;
+    const bool own = DIM == 2 || (ku >= a.z0 && ku < a.z0 + a.zn);  // parameter gradients
     typedef T R;
     const T* __restrict__ G = (const T*)a.Gin;
     const long long sy = g.nx, sz = (long long)g.nx * g.ny;
@@ -172,8 +180,8 @@ __global__ void __launch_bounds__(256) stage_adj_coef_kernel(AdjStageArgs a) {
 #pragma unroll
     for (int ax = 0; ax < DIM; ++ax) dg += D[ax] * gr[ax];
     const R wc = (R)(a.cdt) * ((const T*)a.lam)[c];
-    const long long P = g.cells();
-    T* cp = (T*)a.coef + c;  // plane 0 of this cell; plane o at cp + o P
+    const long long P = DIM == 3 ? (long long)(a.zn + 6) * sz : g.cells();
+    T* cp = (T*)a.coef + (i + sy * j + sz * kl);  // plane 0 of this cell; plane o at cp + o P
     R centre = (R)0;
 #pragma unroll
     for (int ax = 0; ax < DIM; ++ax) {
@@ -191,8 +199,8 @@ __global__ void __launch_bounds__(256) stage_adj_coef_kernel(AdjStageArgs a) {
         }
     }
     cp[0] = (T)(wc * centre);
-    if (a.gS) a.gS[c] += (double)(wc * (active ? dg * igm : (R)0));
-    if (a.gu) {
+    if (a.gS && own) a.gS[c] += (double)(wc * (active ? dg * igm : (R)0));
+    if (a.gu && own) {
         a.gu[c] += (double)(-wc * D[0]);
         a.gv[c] += (double)(-wc * D[1]);
         if (DIM == 3) a.gw[c] += (double)(-wc * D[2]);
@@ -273,13 +281,18 @@ __global__ void __launch_bounds__(256, 2) stage_adj_coef_pair_kernel(AdjStageArg
     const Geo g = a.g;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
-    const int k = 2 * (blockIdx.z * blockDim.z + threadIdx.z);
-    if (i >= g.nx || j >= g.ny || k >= g.nz) return;
-    const bool two = k + 1 < g.nz;  // an odd nz leaves the last thread one plane
+    const int kl = 2 * (blockIdx.z * blockDim.z + threadIdx.z);  // slab-local plane of the pair
+    const int nl = a.zn + 6;
+    if (i >= g.nx || j >= g.ny || kl >= nl) return;
+    const bool two = kl + 1 < nl;  // an odd slab leaves the last thread one plane
+    const int ku = a.z0 - 3 + kl;
+    const int k = wrapn(ku, g.nz), k1 = wrapn(ku + 1, g.nz);
+    const bool own0 = ku >= a.z0 && ku < a.z0 + a.zn;
+    const bool own1 = two && ku + 1 >= a.z0 && ku + 1 < a.z0 + a.zn;
     const float* __restrict__ G = (const float*)a.Gin;
     const long long sy = g.nx, sz = (long long)g.nx * g.ny;
     const long long c = i + sy * j + sz * k;
-    const long long c1 = two ? c + sz : c;
+    const long long c1 = i + sy * j + sz * k1;
     const float* Gc = G + c;
     float2 s[3][7];
 #pragma unroll
@@ -291,9 +304,9 @@ __global__ void __launch_bounds__(256, 2) stage_adj_coef_pair_kernel(AdjStageArg
     }
     float zq[8];
 #pragma unroll
-    for (int d = 0; d < 8; ++d) zq[d] = Gc[(long long)(wrap(k - 3 + d, g.nz) - k) * sz];
+    for (int d = 0; d < 8; ++d) zq[d] = G[i + sy * j + sz * wrapn(ku - 3 + d, g.nz)];
 #pragma unroll
-    for (int d = 0; d < 7; ++d) s[2][d] = make_float2(zq[d], two ? zq[d + 1] : zq[d]);
+    for (int d = 0; d < 7; ++d) s[2][d] = make_float2(zq[d], zq[d + 1]);
     const float* sl = (const float*)a.sl;
     const float2 S = sl ? make_float2(sl[c], sl[c1]) : f2((float)a.s_l);
     const float ih[3] = {(float)(1.0 / a.dx), (float)(1.0 / a.dy), (float)(1.0 / a.dz)};
@@ -320,9 +333,9 @@ __global__ void __launch_bounds__(256, 2) stage_adj_coef_pair_kernel(AdjStageArg
     for (int ax = 0; ax < 3; ++ax) dg = fma2(D[ax], gr[ax], dg);
     const float* lam = (const float*)a.lam;
     const float2 wc = f2((float)a.cdt) * make_float2(lam[c], lam[c1]);
-    const long long P = g.cells();
-    float* cp0 = (float*)a.coef + c;
-    float* cp1 = (float*)a.coef + c1;
+    const long long P = (long long)nl * sz;  // plane stride of the slab buffer
+    float* cp0 = (float*)a.coef + (i + sy * j + sz * kl);
+    float* cp1 = cp0 + sz;
     float2 centre = f2(0.0f);
     const float2 igm2 = igm * igm;
 #pragma unroll
@@ -348,16 +361,16 @@ __global__ void __launch_bounds__(256, 2) stage_adj_coef_pair_kernel(AdjStageArg
     if (two) cp1[0] = oc.y;
     if (a.gS) {
         const float2 gs = wc * dg * igm;
-        a.gS[c] += (double)(actx ? gs.x : 0.0f);
-        if (two) a.gS[c1] += (double)(acty ? gs.y : 0.0f);
+        if (own0) a.gS[c] += (double)(actx ? gs.x : 0.0f);
+        if (own1) a.gS[c1] += (double)(acty ? gs.y : 0.0f);
     }
     if (a.gu) {
         double* gp[3] = {a.gu, a.gv, a.gw};
 #pragma unroll
         for (int ax = 0; ax < 3; ++ax) {
             const float2 gv = -(wc * D[ax]);
-            gp[ax][c] += (double)gv.x;
-            if (two) gp[ax][c1] += (double)gv.y;
+            if (own0) gp[ax][c] += (double)gv.x;
+            if (own1) gp[ax][c1] += (double)gv.y;
         }
     }
 }
@@ -369,12 +382,14 @@ __global__ void __launch_bounds__(256) stage_adj_gather_kernel(AdjGatherArgs a) 
     const Geo g = a.g;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
-    const int k = DIM == 3 ? blockIdx.z * blockDim.z + threadIdx.z : 0;
-    if (i >= g.nx || j >= g.ny || k >= g.nz) return;
+    const int kk = DIM == 3 ? blockIdx.z * blockDim.z + threadIdx.z : 0;
+    if (i >= g.nx || j >= g.ny || kk >= (DIM == 3 ? a.zn : 1)) return;
+    const int k = DIM == 3 ? a.z0 + kk : 0;
     const long long sy = g.nx, sz = (long long)g.nx * g.ny;
     const long long m = i + sy * j + sz * k;
-    const long long P = g.cells();
-    const T* __restrict__ cm = (const T*)a.coef + m;  // plane 0 at cell m
+    const long long P = DIM == 3 ? (long long)(a.zn + 6) * sz : g.cells();
+    const int kl = DIM == 3 ? kk + 3 : 0;  // slab-local plane of m
+    const T* __restrict__ cm = (const T*)a.coef + (i + sy * j + sz * kl);  // plane 0 at cell m
     const T lam = ((const T*)a.lam)[m];
     T sum = cm[0];
 #pragma unroll
@@ -391,7 +406,7 @@ __global__ void __launch_bounds__(256) stage_adj_gather_kernel(AdjGatherArgs a) 
 #pragma unroll
         for (int q = 0; q < 6; ++q) {
             const int o = stage_off(q);
-            sum += cm[(13 + q) * P + (long long)(wrap(k - o, g.nz) - k) * sz];
+            sum += cm[(13 + q) * P - (long long)o * sz];  // source plane kl - o of the slab
         }
     }
     T out = (T)a.c_self * lam + sum;
@@ -602,14 +617,17 @@ template <typename T>
 cudaError_t launch_stage_adj(const AdjStageArgs& c, const AdjGatherArgs& gth, cudaStream_t st) {
     const dim3 b = cell_block(c.g), gr = cell_grid(c.g, b);
     if (c.g.dim == 3) {
+        const int nl = c.zn + 6;
         if (std::is_same<T, float>::value) {
             // plane pairs: half the threads along z
-            const dim3 gp(gr.x, gr.y, (unsigned)((c.g.nz + 2 * b.z - 1) / (2 * b.z)));
+            const dim3 gp(gr.x, gr.y, (unsigned)((nl + 2 * b.z - 1) / (2 * b.z)));
             stage_adj_coef_pair_kernel<<<gp, b, 0, st>>>(c);
         } else {
-            stage_adj_coef_kernel<T, 3><<<gr, b, 0, st>>>(c);
+            const dim3 gc(gr.x, gr.y, (unsigned)((nl + b.z - 1) / b.z));
+            stage_adj_coef_kernel<T, 3><<<gc, b, 0, st>>>(c);
         }
-        stage_adj_gather_kernel<T, 3><<<gr, b, 0, st>>>(gth);
+        const dim3 gg(gr.x, gr.y, (unsigned)((gth.zn + b.z - 1) / b.z));
+        stage_adj_gather_kernel<T, 3><<<gg, b, 0, st>>>(gth);
     } else {
         stage_adj_coef_kernel<T, 2><<<gr, b, 0, st>>>(c);
         stage_adj_gather_kernel<T, 2><<<gr, b, 0, st>>>(gth);

@@ -1211,7 +1211,10 @@ struct lsgb_adjoint {
     int tape_slots = 0, ckpt_slots = 0;
     char* tape = nullptr;      // recompute tape of one segment
     char* ckpts = nullptr;     // G at every segment start
-    void* coef = nullptr;      // ADJ_PLANES coefficient planes
+    void* coef = nullptr;      // coefficient planes (stage slab or HCR-2 full domain)
+    int slab = 1;              // z planes per coefficient slab of the stage transpose (3D)
+    int slab_auto = 1;         // the slab chosen at creation
+    size_t coef_bytes = 0;
     void* lam[4] = {nullptr, nullptr, nullptr, nullptr};  // lambda buffers (solver precision)
     double* grad[4] = {nullptr, nullptr, nullptr, nullptr};  // dL/dS_L, dL/du, dL/dv, dL/dw
     double* target = nullptr;  // FP64 compact target
@@ -1362,18 +1365,29 @@ int adj_reverse_step(lsgb_adjoint* a, const TapeStep& t, void** L) {
     gt.coef = a->coef;
     const double dt = s->p.dt;
     // stage 3: G^{n+1} = 1/3 G^n + 2/3 G2 + 2/3 dt L(G2)
+    // one stage transpose, slab by slab along z
+    auto stage = [&]() -> int {
+        const int nz = g.dim == 3 ? g.nz : 1;
+        const int step = g.dim == 3 ? a->slab : 1;
+        for (int z0 = 0; z0 < nz; z0 += step) {
+            c.z0 = gt.z0 = z0;
+            c.zn = gt.zn = std::min(step, nz - z0);
+            LSGB_CUDA(launch_stage_adj<T>(c, gt, s->st));
+        }
+        return LSGB_OK;
+    };
     c.Gin = tslot(a, t.g2); c.cdt = 2.0 / 3.0 * dt; c.lam = *L;
     gt.lam = *L; gt.out = X; gt.acc = ACC; gt.acc_init = 1; gt.c_self = 2.0 / 3.0; gt.c_n = 1.0 / 3.0;
     gt.addend = nullptr;
-    LSGB_CUDA(launch_stage_adj<T>(c, gt, s->st));
+    LSGB_TRY(stage());
     // stage 2: G2 = 3/4 G^n + 1/4 G1 + 1/4 dt L(G1)
     c.Gin = tslot(a, t.g1); c.cdt = 0.25 * dt; c.lam = X;
     gt.lam = X; gt.out = Y; gt.acc = ACC; gt.acc_init = 0; gt.c_self = 0.25; gt.c_n = 0.75;
-    LSGB_CUDA(launch_stage_adj<T>(c, gt, s->st));
+    LSGB_TRY(stage());
     // stage 1: G1 = G^n + dt L(G^n)
     c.Gin = tslot(a, t.gn); c.cdt = dt; c.lam = Y;
     gt.lam = Y; gt.out = *L; gt.acc = nullptr; gt.addend = ACC; gt.c_self = 1.0; gt.c_n = 0.0;
-    LSGB_CUDA(launch_stage_adj<T>(c, gt, s->st));
+    LSGB_TRY(stage());
     return LSGB_OK;
 }
 
@@ -1428,7 +1442,23 @@ extern "C" int lsgb_adjoint_create(lsgb_solver* s, int checkpoint_interval, lsgb
     a->s = s;
     a->ckpt = checkpoint_interval;
     a->slot = (nbytes(s) + 255) / 256 * 256;
-    int rc = adj_alloc(&a->coef, (size_t)ADJ_PLANES * nbytes(s), "adjoint coefficient planes");
+    // Stage transpose in z slabs: by default one slab spans the whole domain
+    // (measured fastest at 192^3: slabs small enough for their 19 coefficient
+    // planes to stay in L2 between the two passes lost more to the 3-plane
+    // halo recompute and the extra launches than they saved in HBM
+    // traffic).  The buffer also holds the HCR-2 transpose's 14 planes.
+    const size_t slice = (size_t)s->g.nx * s->g.ny * s->esz;  // one z plane of one coefficient
+    size_t planes_needed;
+    if (s->g.dim == 3) {
+        a->slab = s->g.nz;
+        planes_needed = std::max((size_t)ADJ_PLANES * (s->g.nz + 6), (size_t)14 * s->g.nz);
+    } else {
+        a->slab = 1;
+        planes_needed = (size_t)ADJ_PLANES;
+    }
+    a->slab_auto = a->slab;
+    a->coef_bytes = planes_needed * slice;
+    int rc = adj_alloc(&a->coef, a->coef_bytes, "adjoint coefficient planes");
     for (int b = 0; b < 4 && rc == LSGB_OK; ++b) rc = adj_alloc(&a->lam[b], a->slot, "adjoint field");
     for (int b = 0; b < 4 && rc == LSGB_OK; ++b)
         rc = adj_alloc((void**)&a->grad[b], sizeof(double) * (size_t)s->g.cells(), "gradient field");
@@ -1458,6 +1488,19 @@ extern "C" int lsgb_adjoint_set_grads(lsgb_adjoint* a, int mask) {
     if (mask & ~(LSGB_GRAD_SL | LSGB_GRAD_VELOCITY)) return fail(LSGB_ERR_INVALID, "unknown gradient bits 0x%x", mask);
     a->grads = mask;
     a->have_grad = false;
+    return LSGB_OK;
+}
+
+extern "C" int lsgb_adjoint_set_slab(lsgb_adjoint* a, int planes) {
+    LSGB_TRY(adj_ok(a));
+    const lsgb_solver* s = a->s;
+    if (s->g.dim != 3) return fail(LSGB_ERR_INVALID, "z slabs apply to 3D grids");
+    if (planes < 0) return fail(LSGB_ERR_INVALID, "planes < 0");
+    const int want = planes == 0 ? a->slab_auto : std::min(planes, s->g.nz);
+    const size_t slice = (size_t)s->g.nx * s->g.ny * s->esz;
+    if ((size_t)ADJ_PLANES * (want + 6) * slice > a->coef_bytes)
+        return fail(LSGB_ERR_INVALID, "a %d-plane slab does not fit the coefficient buffer", want);
+    a->slab = want;
     return LSGB_OK;
 }
 

@@ -162,7 +162,8 @@ cudaError_t noalloc_count_negative_f64(const Geo& g, const Lay& lay, const doubl
                                        cudaStream_t st);
 
 // Discrete adjoint (adjoint.cu).  Compact periodic fields of type T; the
-// coefficient buffer holds ADJ_PLANES planes of cells() elements.
+// stage transpose has ADJ_PLANES coefficient planes, computed in z slabs
+// (lsgb_adjoint_set_slab; one slab by default).
 constexpr int ADJ_PLANES = 19;
 
 // coefficient pass of the stage transpose: lam = adjoint of the stage
@@ -182,6 +183,11 @@ struct AdjStageArgs {
     double* gu;
     double* gv;
     double* gw;
+    // 3D z-slab: the pass covers the (unwrapped) planes z0-3 .. z0+zn+2 and
+    // stores plane k of the slab at slab-local index k - (z0 - 3); plane
+    // stride of the coefficient buffer = (zn + 6) nx ny.  Parameter
+    // gradients only for z0 <= k < z0 + zn.  2D: z0 = 0, zn = 1, no halo.
+    int z0, zn;
 };
 // gather pass: out = c_self lam + addend + transpose; acc (+)= c_n lam
 struct AdjGatherArgs {
@@ -193,6 +199,7 @@ struct AdjGatherArgs {
     void* acc;
     int acc_init;
     double c_self, c_n;
+    int z0, zn;  // planes gathered (3D): z0 .. z0+zn-1, coefficients as in AdjStageArgs
 };
 struct AdjReinitArgs {
     Geo g;

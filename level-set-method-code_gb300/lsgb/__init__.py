@@ -472,6 +472,10 @@ class Adjoint:
         """Which parameter gradients the backward accumulates (dL/dG0 always)."""
         _check(lib().lsgb_adjoint_set_grads(self._h, (1 if sl else 0) | (2 if velocity else 0)))
 
+    def set_slab(self, planes: int = 0):
+        """z planes per slab of the 3D stage transpose (0 = automatic)."""
+        _check(lib().lsgb_adjoint_set_slab(self._h, int(planes)))
+
     def forward(self, n_steps: int):
         _check(lib().lsgb_adjoint_forward(self._h, int(n_steps)))
 
