@@ -451,7 +451,7 @@ def run_ours(args, dist: Dist):
     traffic = load_traffic("f32", n)
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
-                "kernel": "stage3d_f32_pair (fused WENO5 RHS + RK3 stage combine, TMA-fed 2.5D tiles)",
+                "kernel": "stage3d_f32_col2 (fused WENO5 RHS + RK3 stage combine, TMA-fed 2.5D tiles, register-blocked in y and z)",
                 "algorithmic_bytes_per_launch": cells * s_bytes * 17 / 3,
                 "launches": st_n, "avg_launch_ms": st_ms / max(st_n, 1)}
     step_bytes = cells * s_bytes * (17 + (4 + 5 * REINIT_ITERS) / RK_PER_BENCH_STEP)

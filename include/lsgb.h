@@ -254,7 +254,8 @@ LSGB_API int lsgb_solver_kernel_times(lsgb_solver* s, double* stage_ms, int64_t*
                                       double* reinit_ms, int64_t* reinit_launches);
 
 /* Tile shape of the FP32 stage kernels: the z-chunk length (16, 32, 64) of
- * the 3D tiles or the block height (2, 4, 8) of the 2D blocks; 0 = default.
+ * the 3D tiles or the block height (2, 4, 8) of the 2D blocks; 0 = default
+ * (3D: the chunk length that fills the GPU's SMs best for the grid).
  * Every shape gives bit-identical results; only the speed differs. */
 LSGB_API int lsgb_solver_set_tile(lsgb_solver* s, int tile);
 LSGB_API int lsgb_solver_get_tile(const lsgb_solver* s, int* tile);

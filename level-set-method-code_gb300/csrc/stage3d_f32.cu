@@ -6,24 +6,33 @@
 // (rk3.h:87-121).  Compact arrays, periodic / zero-gradient neighbours by
 // index mapping (no ghost cells, no boundary pass).
 //
-// Shape (2.5D blocking, two planes per step):
-//   - a CTA owns a 32 x 8 column tile and marches a chunk of 64 z-planes two
-//     at a time; thread (x, y) owns the cells (x, y, k) and (x, y, k+1);
-//   - every per-cell quantity is held as a float2 over the plane pair, so the
-//     arithmetic runs as Blackwell's packed f32x2 FMA / MUL / ADD and every
-//     shared-memory read of a stencil point is one 8-byte load that serves
-//     both planes;
-//   - the plane pair plus a 3-cell x/y halo is staged in shared memory
-//     (double buffered, halo prefetched one pair ahead);
-//   - the squared regularised smoothness indicators q = (1e-6 + beta)^2 are
-//     computed once per cell and axis (shared memory for x and y, registers
-//     for z) and read by the faces;
-//   - WENO is evaluated per FACE: each face value is computed once and read by
-//     the two cells that share it, for both upwind directions -- the
-//     left-biased reconstruction of weno5_left (weno5.h:39-58) and the
-//     right-biased one of weno5_right (weno5.h:60-81), whose candidate
-//     polynomials share two of three terms -- so no cell branches on its
-//     upwind direction before the final selection.
+// Shape (2.5D blocking, register-blocked in y and z):
+//   - a CTA of 32 x 8 threads owns a 32 x 16 column tile and marches a chunk
+//     of up to 64 z-planes two at a time; thread (x, ty) owns the cells of
+//     rows 2 ty and 2 ty + 1 in planes k and k + 1 (four cells);
+//   - every per-cell quantity is a float2 over the plane pair, so the
+//     arithmetic runs as Blackwell's packed f32x2 FMA / MUL / ADD;
+//   - z: each thread keeps the G values of its two columns in register queues
+//     (G(k-3 .. k+4)), with the z indicators and the last z face carried;
+//   - y: each thread reads an 8-row window of the staged plane pair into
+//     registers and evaluates its rows' y faces there;
+//   - x: the only direction that goes through shared memory -- the plane
+//     pair plus a 3-cell halo is staged (double buffered, halo prefetched one
+//     pair ahead), every x face is computed once by one lane and stored, and
+//     its indicators are shared across the warp by shuffles;
+//   - u, v, w, G^n and S_L stream through a 3-deep pipeline of TMA bulk
+//     tensor copies (one thread issues, mbarriers with bounded waits signal
+//     arrival), or per-thread cp.async copies where a field's row pitch is
+//     not 16-byte aligned.
+// Two barriers per plane pair.  The kernel is bound by the FP32 pipe (packed
+// f32x2 instructions occupy it for two cycles), not by HBM or shared memory.
+//
+// WENO is evaluated per FACE: each face value is computed once and read by
+// the two cells that share it, for both upwind directions -- the
+// left-biased reconstruction of weno5_left (weno5.h:39-58) and the
+// right-biased one of weno5_right (weno5.h:60-81), whose candidate
+// polynomials share two of three terms -- so no cell branches on its upwind
+// direction before the final selection.
 //
 // Face between cells f-1 and f, samples g_m = G[f-3+m], m = 0..5:
 //   L(f-1) = (w0 Pa + w1 Pb + w2 Pc) / (w0 + w1 + w2),
@@ -48,26 +57,20 @@
 namespace lsgb {
 namespace {
 
-constexpr int TX = 32;
-constexpr int TY = 8;
+constexpr int TX = 32;                        // tile columns (one warp's lanes)
+constexpr int TY = 8;                         // thread rows of a CTA
 constexpr int NT = TX * TY;
-constexpr int MAXZC = 64;       // longest z chunk a CTA marches (planes, even)
-constexpr int PW = TX + 6;      // staged plane tile
-constexpr int PH = TY + 6;
-constexpr int QXW = TX + 4;     // x-indicators for tile x in [-2, TX+1]
-constexpr int QYH = TY + 4;     // y-indicators for tile y in [-2, TY+1]
-constexpr int NQX = QXW * TY;
-constexpr int NQY = TX * QYH;
-constexpr int NFX = (TX + 1) * TY;
-constexpr int NFY = TX * (TY + 1);
-constexpr int RING = PW * PH - TX * TY;
-constexpr int RPT = (RING + NT - 1) / NT;
-constexpr int NQ = NQX + NQY;
-constexpr int NF = NFX + NFY;
-constexpr int MINB = 3;         // resident CTAs per SM the register budget targets
-constexpr int NSTAGE = 3;                // TMA pipeline depth (plane pairs in flight)
-constexpr int NFIELD = 5;                // u, v, w, G^n, S_L
-constexpr int FTILE = 2 * TY * TX;       // floats of one field tile (2 planes)
+constexpr int RY = 2;                         // cell rows per thread
+constexpr int BY = TY * RY;                   // tile rows
+constexpr int MAXZC = 64;                     // longest z chunk a CTA marches (planes, even)
+constexpr int PW = TX + 6;                    // staged plane tile: columns
+constexpr int BPH = BY + 6;                   //                    rows
+constexpr int BRING = PW * BPH - TX * BY;     // halo ring of one staged plane
+constexpr int BRPT = (BRING + NT - 1) / NT;   // ring cells per thread
+constexpr int BNFX = (TX + 1) * BY;           // x faces of the tile
+constexpr int NSTAGE = 3;                     // TMA pipeline depth (plane pairs in flight)
+constexpr int NFIELD = 5;                     // u, v, w, G^n, S_L
+constexpr int BFTILE = 2 * BY * TX;           // floats of one staged field tile (2 planes)
 constexpr long long WAIT_CYCLES = 2000000000LL;  // bounded mbarrier wait (~1 s of SM clock)
 
 struct TmaMaps {
@@ -170,81 +173,171 @@ __device__ __forceinline__ void tma_load_3d(float* dst, const CUtensorMap* tm, i
         : "memory");
 }
 
-// IDX: element offsets (int when the field has < 2^31 cells).  TMA: stream
-// u, v, w, G^n and S_L through a NSTAGE-deep pipeline of bulk tensor copies
-// (one thread issues, mbarriers signal arrival); otherwise plain loads.
+// Ampere-style asynchronous 4-byte copies (the staging of fields whose row
+// pitch rules out bulk tensor copies); completion per thread by groups.
+__device__ __forceinline__ void cp_async4(float* dst, const float* src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(saddr(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+// Update of one plane pair from its centre values, the neighbour
+// differences G(+1) - G(-1) along x, y, z, the staged point-wise fields and
+// the face differences.
+template <int STAGE>
+__device__ __forceinline__ float2 cell_pair(const Coef& c, float2 gc, float2 gxd, float2 gyd, float2 gzd, float2 uu,
+                                            float2 vv, float2 ww, float2 gn, float2 s_l, float2 dxL, float2 dxR,
+                                            float2 dyL, float2 dyR, float2 dzL, float2 dzR) {
+    float2 ue = uu, ve = vv, we = ww;
+    const float2 gx = mul2(gxd, c2(c.inv_2dx));
+    const float2 gy = mul2(gyd, c2(c.inv_2dy));
+    const float2 gz = mul2(gzd, c2(c.inv_2dz));
+    const float2 sq = fma2(gx, gx, fma2(gy, gy, fma2(gz, gz, c2(c.eps))));
+    const float2 f = make_float2(s_l.x > c.eps ? -s_l.x * rsqrtf(sq.x) : 0.0f,
+                                 s_l.y > c.eps ? -s_l.y * rsqrtf(sq.y) : 0.0f);
+    ue = fma2(f, gx, ue);
+    ve = fma2(f, gy, ve);
+    we = fma2(f, gz, we);
+    const float2 dgx = mul2(make_float2(ue.x >= 0.0f ? dxL.x : dxR.x, ue.y >= 0.0f ? dxL.y : dxR.y), c2(c.inv_dx));
+    const float2 dgy = mul2(make_float2(ve.x >= 0.0f ? dyL.x : dyR.x, ve.y >= 0.0f ? dyL.y : dyR.y), c2(c.inv_dy));
+    const float2 dgz = mul2(make_float2(we.x >= 0.0f ? dzL.x : dzR.x, we.y >= 0.0f ? dzL.y : dzR.y), c2(c.inv_dz));
+    const float2 nrhs = fma2(ue, dgx, fma2(ve, dgy, mul2(we, dgz)));  // = -rhs
+    if (STAGE == 1) return fma2(c2(-c.dt), nrhs, gc);
+    if (STAGE == 2) return fma2(c2(-0.25f * c.dt), nrhs, fma2(c2(0.75f), gn, mul2(c2(0.25f), gc)));
+    return fma2(c2(-(2.0f / 3.0f) * c.dt), nrhs, fma2(c2(1.0f / 3.0f), gn, mul2(c2(2.0f / 3.0f), gc)));
+}
+
+// Both reconstructions at a face from its six samples s[0], s[st], .. s[5 st],
+// with the four indicators computed on the spot.
+__device__ __forceinline__ void face6(const float2* s, int st, float2& L, float2& R) {
+    const float2 g0 = s[0], g1 = s[st], g2 = s[2 * st], g3 = s[3 * st], g4 = s[4 * st], g5 = s[5 * st];
+    face(g0, g1, g2, g3, g4, g5, qbeta(g0, g1, g2), qbeta(g1, g2, g3), qbeta(g2, g3, g4), qbeta(g3, g4, g5), L, R);
+}
+
+// x face of column tx (lane tx) with the indicators shared across the warp:
+// each lane computes q at its own column and one edge indicator (q(-2),
+// q(-1) in lanes 0, 1; q(32) in lane 31), the rest come by shuffles.
+__device__ __forceinline__ float2 shfl_up2(float2 v, int d) {
+    return make_float2(__shfl_up_sync(0xffffffffu, v.x, d), __shfl_up_sync(0xffffffffu, v.y, d));
+}
+__device__ __forceinline__ float2 shfl_dn2(float2 v, int d) {
+    return make_float2(__shfl_down_sync(0xffffffffu, v.x, d), __shfl_down_sync(0xffffffffu, v.y, d));
+}
+__device__ __forceinline__ void xface_shfl(const float2* s, int lane, float2& L, float2& R) {
+    const float2 g0 = s[0], g1 = s[1], g2 = s[2], g3 = s[3], g4 = s[4], g5 = s[5];
+    const bool lo = lane < 2;
+    const float2 qc = qbeta(g2, g3, g4);
+    const float2 qe = qbeta(lo ? g0 : g3, lo ? g1 : g4, lo ? g2 : g5);
+    const float2 u2 = shfl_up2(qc, 2), u1 = shfl_up2(qc, 1), d1 = shfl_dn2(qc, 1), e1 = shfl_dn2(qe, 1);
+    const float2 qm2 = lane >= 2 ? u2 : qe;
+    const float2 qm1 = lane >= 1 ? u1 : e1;
+    const float2 qp1 = lane <= 30 ? d1 : qe;
+    face(g0, g1, g2, g3, g4, g5, qm2, qm1, qc, qp1, L, R);
+}
+
+// Per-column z state: G(k-3 .. k+4), q(k-1), q(k), q(k+1), face k-1/2.
+struct ZCol {
+    float zq[8];
+    float2 qa;
+    float qk1, pL, pR;
+};
+
+template <typename IDX>
+__device__ __forceinline__ void zcol_init(ZCol& z, const float* __restrict__ Gin, const IDX* zoff, IDX col) {
+#pragma unroll
+    for (int d = 0; d < 8; ++d) z.zq[d] = __ldg(Gin + zoff[d] + col);
+    z.qa = qbeta(make_float2(z.zq[1], z.zq[2]), make_float2(z.zq[2], z.zq[3]), make_float2(z.zq[3], z.zq[4]));
+    z.qk1 = qbeta(c2(z.zq[3]), c2(z.zq[4]), c2(z.zq[5])).x;
+    const float qm2 = qbeta(c2(z.zq[0]), c2(z.zq[1]), c2(z.zq[2])).x;
+    float2 L, R;
+    face(c2(z.zq[0]), c2(z.zq[1]), c2(z.zq[2]), c2(z.zq[3]), c2(z.zq[4]), c2(z.zq[5]), c2(qm2), c2(z.qa.x),
+         c2(z.qa.y), c2(z.qk1), L, R);
+    z.pL = L.x;
+    z.pR = R.x;
+}
+
+// z faces k+1/2, k+3/2 of a column -> face differences of planes k, k+1;
+// advances the queue by two planes (zn0, zn1 = G(k+5), G(k+6)).
+__device__ __forceinline__ void zcol_step(ZCol& z, float zn0, float zn1, float2& dzL, float2& dzR, float2& gzd) {
+    const float2 qb = qbeta(make_float2(z.zq[4], z.zq[5]), make_float2(z.zq[5], z.zq[6]),
+                            make_float2(z.zq[6], z.zq[7]));
+    float2 L, R;
+    face(make_float2(z.zq[1], z.zq[2]), make_float2(z.zq[2], z.zq[3]), make_float2(z.zq[3], z.zq[4]),
+         make_float2(z.zq[4], z.zq[5]), make_float2(z.zq[5], z.zq[6]), make_float2(z.zq[6], z.zq[7]),
+         make_float2(z.qa.x, z.qa.y), make_float2(z.qa.y, z.qk1), make_float2(z.qk1, qb.x), qb, L, R);
+    dzL = sub2(L, make_float2(z.pL, L.x));
+    dzR = sub2(R, make_float2(z.pR, R.x));
+    gzd = make_float2(z.zq[4] - z.zq[2], z.zq[5] - z.zq[3]);
+#pragma unroll
+    for (int d = 0; d < 6; ++d) z.zq[d] = z.zq[d + 2];
+    z.zq[6] = zn0;
+    z.zq[7] = zn1;
+    z.qa = make_float2(z.qk1, qb.x);
+    z.qk1 = qb.y;
+    z.pL = L.y;
+    z.pR = R.y;
+}
+
+// IDX: element offsets (int when the field has < 2^31 cells).  u, v, w, G^n
+// and S_L stream through an NSTAGE-deep pipeline of shared-memory stages:
+// TMA = bulk tensor copies of the CTA's tile (one thread issues, mbarriers
+// signal arrival); otherwise every thread copies its own four cells with
+// cp.async and waits for its own copies.
 template <int STAGE, bool TMA, typename IDX>
-__global__ void __launch_bounds__(NT, MINB)
-stage3d_f32_pair(Geo g, const float* __restrict__ Gin, const float* __restrict__ Gn,
-                 float* __restrict__ Gout, const float* __restrict__ u, const float* __restrict__ v,
-                 const float* __restrict__ w, const float* __restrict__ sl, Coef c,
-                 const __grid_constant__ TmaMaps tm, int* __restrict__ err) {
-    __shared__ float2 P2[2][PH][PW];
-    __shared__ float2 QA[NQ];          // x-indicators [TY][QXW], then y-indicators [QYH][TX]
-    __shared__ float2 FL[NF], FR[NF];  // x-faces [TY][TX+1], then y-faces [TY+1][TX]
+__global__ void __launch_bounds__(NT, 2)
+stage3d_f32_col2(Geo g, const float* __restrict__ Gin, const float* __restrict__ Gn, float* __restrict__ Gout,
+                 const float* __restrict__ u, const float* __restrict__ v, const float* __restrict__ w,
+                 const float* __restrict__ sl, Coef c, const __grid_constant__ TmaMaps tm, int* __restrict__ err) {
+    __shared__ float2 P2[2][BPH][PW];
+    __shared__ float2 FL[BNFX], FR[BNFX];  // x faces [BY][TX+1]
     __shared__ IDX zoff[MAXZC + 10];
     __shared__ __align__(8) uint64_t mbar[NSTAGE];
-    extern __shared__ __align__(128) float stg[];  // NSTAGE x NFIELD x FTILE (TMA only)
+    extern __shared__ __align__(128) float stg[];  // NSTAGE x NFIELD x BFTILE
 
     const int tx = threadIdx.x, ty = threadIdx.y;
     const int t = ty * TX + tx;
-    const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY;
+    const int i0 = blockIdx.x * TX, j0 = blockIdx.y * BY;
     const int z0 = blockIdx.z * c.zc;
     const int z1 = min(z0 + c.zc, g.nz);
     const int niter = (z1 - z0 + 1) / 2;
     const IDX sz = (IDX)g.nx * g.ny;
-    const bool valid = (i0 + tx) < g.nx && (j0 + ty) < g.ny;
-    const IDX col = (IDX)wrapg(j0 + ty, g.ny, g.bcy) * g.nx + wrapg(i0 + tx, g.nx, g.bcx);
     const bool has_sl = sl != nullptr;
+    const int ra = RY * ty;  // tile row of cell row A; row B = ra + 1
+    const bool xin = (i0 + tx) < g.nx;
+    const bool va = xin && (j0 + ra) < g.ny;
+    const bool vb = xin && (j0 + ra + 1) < g.ny;
+    const int gxc = wrapg(i0 + tx, g.nx, g.bcx);
+    const IDX colA = (IDX)wrapg(j0 + ra, g.ny, g.bcy) * g.nx + gxc;
+    const IDX colB = (IDX)wrapg(j0 + ra + 1, g.ny, g.bcy) * g.nx + gxc;
 
-    // ---- fixed per-thread task tables (offsets into one staged plane) ----
-    // halo ring of the staged plane pair: 3 full rows above and below, 3 cells
-    // left and right of each tile row
-    int ring_s[RPT];
-    IDX ring_g[RPT];
+    // halo ring of the staged plane pair: 3 full rows above and below, 3
+    // cells left and right of each tile row
+    int ring_s[BRPT];
+    IDX ring_g[BRPT];
 #pragma unroll
-    for (int r = 0; r < RPT; ++r) {
+    for (int r = 0; r < BRPT; ++r) {
         const int q = t + r * NT;
         int ly, lx;
         if (q < 3 * PW) {
             ly = q / PW; lx = q % PW;
         } else if (q < 6 * PW) {
-            ly = PH - 3 + (q - 3 * PW) / PW; lx = (q - 3 * PW) % PW;
+            ly = BPH - 3 + (q - 3 * PW) / PW; lx = (q - 3 * PW) % PW;
         } else {
             const int s = (q - 6 * PW) % 6;
             ly = 3 + (q - 6 * PW) / 6;
             lx = s < 3 ? s : TX + s;
         }
-        ring_s[r] = q < RING ? ly * PW + lx : -1;
-        ring_g[r] = q < RING ? (IDX)wrapg(j0 + ly - 3, g.ny, g.bcy) * g.nx + wrapg(i0 + lx - 3, g.nx, g.bcx) : 0;
+        ring_s[r] = q < BRING ? ly * PW + lx : -1;
+        ring_g[r] = q < BRING ? (IDX)wrapg(j0 + ly - 3, g.ny, g.bcy) * g.nx + wrapg(i0 + lx - 3, g.nx, g.bcx) : 0;
     }
-    // Indicator and face tasks, x and y in separate lists with compile-time
-    // strides.  Every thread has one task of each kind (slot A, index t);
-    // the remainder goes to whole warps (slot B): x-indicators 256..287 to
-    // threads 224..255, y-indicators 256..383 to threads 0..127, x-faces
-    // 256..263 to threads 248..255, y-faces 256..287 to threads 128..159, so
-    // no warp carries more than 3 + 3 tasks.  Offsets in float2 elements of
-    // one staged plane (P) and of the indicator array (QA).
-    //   x-indicator q: row q / QXW, column q % QXW -> P[row+3][cx..cx+2]
-    //   y-indicator q: cy = q / TX, cl = q % TX     -> P[cy..cy+2][cl+3]
-    //   x-face f: row f / (TX+1), fc = f % (TX+1)  -> P[row+3][fc..fc+5], QA[row][fc..fc+3]
-    //   y-face f: rr = f / TX, cl = f % TX          -> P[rr..rr+5][cl+3], QY[rr..rr+3][cl]
-    const int xi_a = (t / QXW + 3) * PW + t % QXW;
-    const bool has_xi_b = t >= NT - (NQX - NT);
-    const int xi_b = ((t + NQX - NT) / QXW + 3) * PW + (t + NQX - NT) % QXW;
-    const int yi_a = ty * PW + tx + 3;
-    const bool has_yi_b = t < NQY - NT;
-    const int yi_b = (ty + NT / TX) * PW + tx + 3;
-    const int fx_a_src = (t / (TX + 1) + 3) * PW + t % (TX + 1);
-    const int fx_a_q = (t / (TX + 1)) * QXW + t % (TX + 1);
-    const bool has_fx_b = t >= NT - (NFX - NT);
-    const int fxb = t + NFX - NT;  // face index of slot B
-    const int fx_b_src = (fxb / (TX + 1) + 3) * PW + fxb % (TX + 1);
-    const int fx_b_q = (fxb / (TX + 1)) * QXW + fxb % (TX + 1);
-    const bool has_fy_b = t >= NT / 2 && t < NT / 2 + (NFY - NT);
-    // y-face slot A = face (ty, tx): P[ty..ty+5][tx+3], QY[ty..ty+3][tx]
-    // y-face slot B = face (TY, tx)
-    // plane offsets of z-indices z0-3 .. z1+6 (periodic wrap or clamp), one
+    // x-face tasks: face column tx of rows ra and ra + 1 (samples
+    // P[row + 3][tx .. tx + 5]); the right-edge faces (column TX) of all BY
+    // rows go to the first BY lanes of the last warp
+    const bool has_fx_c = ty == TY - 1 && tx < BY;
+    // plane offsets of z-indices z0-3 .. z0+zc+6 (periodic wrap or clamp), one
     // table per CTA so the loop does no index arithmetic on z
     for (int d = t; d < c.zc + 10; d += NT) {
         int kk = z0 - 3 + d;
@@ -256,18 +349,33 @@ stage3d_f32_pair(Geo g, const float* __restrict__ Gin, const float* __restrict__
         }
         zoff[d] = (IDX)kk * sz;
     }
-
-    // ---- TMA pipeline prologue ----
     auto issue = [&](int it, int s) {
         const int kz = z0 + 2 * it;
-        float* base = stg + s * NFIELD * FTILE;
+        float* base = stg + s * NFIELD * BFTILE;
         const uint32_t nf = 3 + (STAGE > 1 ? 1 : 0) + (has_sl ? 1 : 0);
-        mbar_expect_tx(&mbar[s], nf * FTILE * 4);
-        tma_load_3d(base + 0 * FTILE, &tm.m[0], i0, j0, kz, &mbar[s]);
-        tma_load_3d(base + 1 * FTILE, &tm.m[1], i0, j0, kz, &mbar[s]);
-        tma_load_3d(base + 2 * FTILE, &tm.m[2], i0, j0, kz, &mbar[s]);
-        if (STAGE > 1) tma_load_3d(base + 3 * FTILE, &tm.m[3], i0, j0, kz, &mbar[s]);
-        if (has_sl) tma_load_3d(base + 4 * FTILE, &tm.m[4], i0, j0, kz, &mbar[s]);
+        mbar_expect_tx(&mbar[s], nf * BFTILE * 4);
+        tma_load_3d(base + 0 * BFTILE, &tm.m[0], i0, j0, kz, &mbar[s]);
+        tma_load_3d(base + 1 * BFTILE, &tm.m[1], i0, j0, kz, &mbar[s]);
+        tma_load_3d(base + 2 * BFTILE, &tm.m[2], i0, j0, kz, &mbar[s]);
+        if (STAGE > 1) tma_load_3d(base + 3 * BFTILE, &tm.m[3], i0, j0, kz, &mbar[s]);
+        if (has_sl) tma_load_3d(base + 4 * BFTILE, &tm.m[4], i0, j0, kz, &mbar[s]);
+    };
+    // plain form: this thread's cells of rows ra, ra + 1, planes k, k + 1
+    auto fetch = [&](int it, int s) {
+        const IDX* zf = zoff + 2 * it + 3;
+        float* base = stg + s * NFIELD * BFTILE + ra * TX + tx;
+#pragma unroll
+        for (int h = 0; h < 2; ++h)
+#pragma unroll
+            for (int p = 0; p < 2; ++p) {
+                const IDX o = zf[p] + (h ? colB : colA);
+                float* d = base + h * TX + p * BY * TX;
+                cp_async4(d, u + o);
+                cp_async4(d + BFTILE, v + o);
+                cp_async4(d + 2 * BFTILE, w + o);
+                if (STAGE > 1) cp_async4(d + 3 * BFTILE, Gn + o);
+                if (has_sl) cp_async4(d + 4 * BFTILE, sl + o);
+            }
     };
     if (TMA && t == 0) {
         for (int s = 0; s < NSTAGE; ++s) mbar_init(&mbar[s], 1);
@@ -276,75 +384,95 @@ stage3d_f32_pair(Geo g, const float* __restrict__ Gin, const float* __restrict__
     __syncthreads();  // zoff table and barriers ready
     if (TMA && t == 0)
         for (int it = 0; it < NSTAGE - 1 && it < niter; ++it) issue(it, it);
+    if (!TMA)
+        for (int it = 0; it < NSTAGE - 1; ++it) {
+            if (it < niter) fetch(it, it);
+            cp_async_commit();  // one group per iteration, empty ones included
+        }
 
-    // ---- z queues: G(k-3 .. k+4) and q_z(k-1 .. k+1) of the own column ----
-    float zq[8];
+    ZCol za, zb;
+    zcol_init(za, Gin, zoff, colA);
+    zcol_init(zb, Gin, zoff, colB);
+    float2 ring_v[BRPT];
 #pragma unroll
-    for (int d = 0; d < 8; ++d) zq[d] = __ldg(Gin + zoff[d] + col);
-    float2 qz_a = qbeta(make_float2(zq[1], zq[2]), make_float2(zq[2], zq[3]), make_float2(zq[3], zq[4]));  // (q(k-1), q(k))
-    float qz_k1 = qbeta(make_float2(zq[3], zq[3]), make_float2(zq[4], zq[4]), make_float2(zq[5], zq[5])).x;  // q(k+1)
-    const float qz_m2 = qbeta(make_float2(zq[0], zq[0]), make_float2(zq[1], zq[1]), make_float2(zq[2], zq[2])).x;  // q(k-2)
-    // face k-1/2 (between k-1 and k): samples G(k-3..k+2), q(k-2), q(k-1), q(k), q(k+1)
-    float zprevL, zprevR;
-    {
-        float2 L, R;
-        face(c2(zq[0]), c2(zq[1]), c2(zq[2]), c2(zq[3]), c2(zq[4]), c2(zq[5]), c2(qz_m2), c2(qz_a.x),
-             c2(qz_a.y), c2(qz_k1), L, R);
-        zprevL = L.x;
-        zprevR = R.x;
-    }
-    float2 ring_v[RPT];
-#pragma unroll
-    for (int r = 0; r < RPT; ++r)
+    for (int r = 0; r < BRPT; ++r)
         ring_v[r] = ring_s[r] >= 0 ? make_float2(__ldg(Gin + zoff[3] + ring_g[r]), __ldg(Gin + zoff[4] + ring_g[r]))
                                    : make_float2(0.0f, 0.0f);
 
     int buf = 0;
-    int cs = 0;         // TMA stage of this iteration (it % NSTAGE)
-    uint32_t cph = 0;   // its mbarrier phase parity ((it / NSTAGE) & 1)
+    int cs = 0;        // TMA stage of this iteration (it % NSTAGE)
+    uint32_t cph = 0;  // its mbarrier phase parity ((it / NSTAGE) & 1)
     for (int it = 0; it < niter; ++it) {
         const int k = z0 + 2 * it;
         const IDX* zo = zoff + 2 * it + 3;  // zo[d] = offset of plane k + d
         float2* P = &P2[buf][0][0];
-        P[(ty + 3) * PW + tx + 3] = make_float2(zq[3], zq[4]);
+        P[(ra + 3) * PW + tx + 3] = make_float2(za.zq[3], za.zq[4]);
+        P[(ra + 4) * PW + tx + 3] = make_float2(zb.zq[3], zb.zq[4]);
 #pragma unroll
-        for (int r = 0; r < RPT; ++r)
+        for (int r = 0; r < BRPT; ++r)
             if (ring_s[r] >= 0) P[ring_s[r]] = ring_v[r];
-
-        // loads for this pair's update (plain path) and the next pair's staging
-        const IDX oa = zo[0] + col;
-        const IDX ob = zo[1] + col;
-        float2 uu, vv, ww, gn = c2(0.0f), s_l = c2(c.s_l);
-        if (!TMA) {
-            uu = make_float2(__ldg(u + oa), __ldg(u + ob));
-            vv = make_float2(__ldg(v + oa), __ldg(v + ob));
-            ww = make_float2(__ldg(w + oa), __ldg(w + ob));
-            if (STAGE > 1) gn = make_float2(__ldg(Gn + oa), __ldg(Gn + ob));
-            if (has_sl) s_l = make_float2(__ldg(sl + oa), __ldg(sl + ob));
-        }
-        const float zn0 = __ldg(Gin + zo[5] + col);
-        const float zn1 = __ldg(Gin + zo[6] + col);
+        // next planes of the own columns and the next pair's halo
+        const float na0 = __ldg(Gin + zo[5] + colA), na1 = __ldg(Gin + zo[6] + colA);
+        const float nb0 = __ldg(Gin + zo[5] + colB), nb1 = __ldg(Gin + zo[6] + colB);
         if (it + 1 < niter) {
-            const IDX na = zo[2], nb = zo[3];
 #pragma unroll
-            for (int r = 0; r < RPT; ++r)
-                if (ring_s[r] >= 0) ring_v[r] = make_float2(__ldg(Gin + na + ring_g[r]), __ldg(Gin + nb + ring_g[r]));
+            for (int r = 0; r < BRPT; ++r)
+                if (ring_s[r] >= 0)
+                    ring_v[r] = make_float2(__ldg(Gin + zo[2] + ring_g[r]), __ldg(Gin + zo[3] + ring_g[r]));
         }
         __syncthreads();
+        // refill the stage last read in iteration it-1, which every thread
+        // finished before the barrier above
         if (TMA && t == 0 && it + NSTAGE - 1 < niter) {
-            // the stage being refilled was last read in iteration it-1, which
-            // every thread finished before the barrier above
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             issue(it + NSTAGE - 1, cs == 0 ? NSTAGE - 1 : cs - 1);
         }
-
-        // ---- per-cell indicators (x, y in shared memory; z in registers) ----
-        QA[t] = qbeta(P[xi_a], P[xi_a + 1], P[xi_a + 2]);
-        if (has_xi_b) QA[t + NQX - NT] = qbeta(P[xi_b], P[xi_b + 1], P[xi_b + 2]);
-        QA[NQX + t] = qbeta(P[yi_a], P[yi_a + PW], P[yi_a + 2 * PW]);
-        if (has_yi_b) QA[NQX + NT + t] = qbeta(P[yi_b], P[yi_b + PW], P[yi_b + 2 * PW]);
-        // q_z(k+2), q_z(k+3): triples centred at k+2 and k+3
-        const float2 qz_b = qbeta(make_float2(zq[4], zq[5]), make_float2(zq[5], zq[6]), make_float2(zq[6], zq[7]));
+        if (!TMA) {
+            if (it + NSTAGE - 1 < niter) fetch(it + NSTAGE - 1, cs == 0 ? NSTAGE - 1 : cs - 1);
+            cp_async_commit();
+        }
+        // ---- x faces ----
+        {
+            float2 L, R;
+            xface_shfl(P + (ra + 3) * PW + tx, tx, L, R);
+            FL[ra * (TX + 1) + tx] = L;
+            FR[ra * (TX + 1) + tx] = R;
+            xface_shfl(P + (ra + 4) * PW + tx, tx, L, R);
+            FL[(ra + 1) * (TX + 1) + tx] = L;
+            FR[(ra + 1) * (TX + 1) + tx] = R;
+            if (has_fx_c) {
+                face6(P + (tx + 3) * PW + TX, 1, L, R);
+                FL[tx * (TX + 1) + TX] = L;
+                FR[tx * (TX + 1) + TX] = R;
+            }
+        }
+        // ---- y: window of tile rows ra - 3 .. ra + 4, faces ra, ra + 1, ra + 2 ----
+        float2 dyLA, dyRA, dyLB, dyRB, gyA, gyB, gxA, gxB;
+        {
+            const float2* col = P + ra * PW + tx + 3;
+            float2 y[8];
+#pragma unroll
+            for (int m = 0; m < 8; ++m) y[m] = col[m * PW];
+            float2 q[7];
+#pragma unroll
+            for (int m = 1; m < 7; ++m) q[m] = qbeta(y[m - 1], y[m], y[m + 1]);
+            float2 L0, R0, L1, R1, L2, R2;
+            face(y[0], y[1], y[2], y[3], y[4], y[5], q[1], q[2], q[3], q[4], L0, R0);
+            face(y[1], y[2], y[3], y[4], y[5], y[6], q[2], q[3], q[4], q[5], L1, R1);
+            face(y[2], y[3], y[4], y[5], y[6], y[7], q[3], q[4], q[5], q[6], L2, R2);
+            dyLA = sub2(L1, L0);
+            dyRA = sub2(R1, R0);
+            dyLB = sub2(L2, L1);
+            dyRB = sub2(R2, R1);
+            gyA = sub2(y[4], y[2]);
+            gyB = sub2(y[5], y[3]);
+            gxA = sub2(col[3 * PW + 1], col[3 * PW - 1]);
+            gxB = sub2(col[4 * PW + 1], col[4 * PW - 1]);
+        }
+        // ---- z faces of both columns ----
+        float2 dzLA, dzRA, dzLB, dzRB, gzA, gzB;
+        zcol_step(za, na0, na1, dzLA, dzRA, gzA);
+        zcol_step(zb, nb0, nb1, dzLB, dzRB, gzB);
         if (TMA) {
             const bool ok = mbar_wait(&mbar[cs], cph);
             if (__syncthreads_or(!ok)) {
@@ -358,101 +486,33 @@ stage3d_f32_pair(Geo g, const float* __restrict__ Gin, const float* __restrict__
                 return;
             }
         } else {
-            __syncthreads();
+            cp_async_wait<NSTAGE - 1>();  // this iteration's group (own cells only)
+            __syncthreads();              // x faces complete
         }
 
-        // ---- faces ----
-        {
-            float2 L, R;
-            const float2* sx = P + fx_a_src;
-            const float2* qx = QA + fx_a_q;
-            face(sx[0], sx[1], sx[2], sx[3], sx[4], sx[5], qx[0], qx[1], qx[2], qx[3], L, R);
-            FL[t] = L;
-            FR[t] = R;
-            if (has_fx_b) {
-                sx = P + fx_b_src;
-                qx = QA + fx_b_q;
-                face(sx[0], sx[1], sx[2], sx[3], sx[4], sx[5], qx[0], qx[1], qx[2], qx[3], L, R);
-                FL[fxb] = L;
-                FR[fxb] = R;
-            }
-            const float2* sy = P + yi_a;  // P[ty][tx+3]
-            const float2* qy = QA + NQX + t;
-            face(sy[0], sy[PW], sy[2 * PW], sy[3 * PW], sy[4 * PW], sy[5 * PW], qy[0], qy[TX], qy[2 * TX],
-                 qy[3 * TX], L, R);
-            FL[NFX + t] = L;
-            FR[NFX + t] = R;
-            if (has_fy_b) {
-                // face row TY: P[TY..TY+5][tx+3], QY[TY..TY+3][tx]
-                sy = P + TY * PW + tx + 3;
-                qy = QA + NQX + TY * TX + tx;
-                face(sy[0], sy[PW], sy[2 * PW], sy[3 * PW], sy[4 * PW], sy[5 * PW], qy[0], qy[TX], qy[2 * TX],
-                     qy[3 * TX], L, R);
-                FL[NFX + TY * TX + tx] = L;
-                FR[NFX + TY * TX + tx] = R;
-            }
-        }
-        // z faces k+1/2 and k+3/2 as one pair: samples G(k-2+m), G(k-1+m)
-        float2 zL, zR;
-        face(make_float2(zq[1], zq[2]), make_float2(zq[2], zq[3]), make_float2(zq[3], zq[4]),
-             make_float2(zq[4], zq[5]), make_float2(zq[5], zq[6]), make_float2(zq[6], zq[7]),
-             make_float2(qz_a.x, qz_a.y), make_float2(qz_a.y, qz_k1), make_float2(qz_k1, qz_b.x),
-             qz_b, zL, zR);
-        __syncthreads();
-
-        // ---- cell update for planes k, k+1 ----
-        if (TMA) {
-            const float* sb = stg + cs * NFIELD * FTILE + ty * TX + tx;
-            uu = make_float2(sb[0 * FTILE], sb[0 * FTILE + TX * TY]);
-            vv = make_float2(sb[1 * FTILE], sb[1 * FTILE + TX * TY]);
-            ww = make_float2(sb[2 * FTILE], sb[2 * FTILE + TX * TY]);
-            if (STAGE > 1) gn = make_float2(sb[3 * FTILE], sb[3 * FTILE + TX * TY]);
-            if (has_sl) s_l = make_float2(sb[4 * FTILE], sb[4 * FTILE + TX * TY]);
-        }
-        const float2* ctr = P + (ty + 3) * PW + tx + 3;
-        const float2 gc = ctr[0];
-        float2 ue = uu, ve = vv, we = ww;
-        {
-            const float2 gx = mul2(sub2(ctr[1], ctr[-1]), c2(c.inv_2dx));
-            const float2 gy = mul2(sub2(ctr[PW], ctr[-PW]), c2(c.inv_2dy));
-            const float2 gz = mul2(make_float2(zq[4] - zq[2], zq[5] - zq[3]), c2(c.inv_2dz));
-            const float2 sq = fma2(gx, gx, fma2(gy, gy, fma2(gz, gz, c2(c.eps))));
-            const float2 f = make_float2(s_l.x > c.eps ? -s_l.x * rsqrtf(sq.x) : 0.0f,
-                                         s_l.y > c.eps ? -s_l.y * rsqrtf(sq.y) : 0.0f);
-            ue = fma2(f, gx, ue);
-            ve = fma2(f, gy, ve);
-            we = fma2(f, gz, we);
-        }
-        const int xf = ty * (TX + 1) + tx, yfc = NFX + ty * TX + tx;
-        const float2 dxL = sub2(FL[xf + 1], FL[xf]);
-        const float2 dxR = sub2(FR[xf + 1], FR[xf]);
-        const float2 dyL = sub2(FL[yfc + TX], FL[yfc]);
-        const float2 dyR = sub2(FR[yfc + TX], FR[yfc]);
-        // z: plane k uses faces (k-1/2, k+1/2) = (prev, zL.x); plane k+1 (zL.x, zL.y)
-        const float2 dzL = sub2(zL, make_float2(zprevL, zL.x));
-        const float2 dzR = sub2(zR, make_float2(zprevR, zR.x));
-        const float2 dgx = mul2(make_float2(ue.x >= 0.0f ? dxL.x : dxR.x, ue.y >= 0.0f ? dxL.y : dxR.y), c2(c.inv_dx));
-        const float2 dgy = mul2(make_float2(ve.x >= 0.0f ? dyL.x : dyR.x, ve.y >= 0.0f ? dyL.y : dyR.y), c2(c.inv_dy));
-        const float2 dgz = mul2(make_float2(we.x >= 0.0f ? dzL.x : dzR.x, we.y >= 0.0f ? dzL.y : dzR.y), c2(c.inv_dz));
-        const float2 nrhs = fma2(ue, dgx, fma2(ve, dgy, mul2(we, dgz)));  // = -rhs
-        float2 out;
-        if (STAGE == 1) out = fma2(c2(-c.dt), nrhs, gc);
-        else if (STAGE == 2) out = fma2(c2(-0.25f * c.dt), nrhs, fma2(c2(0.75f), gn, mul2(c2(0.25f), gc)));
-        else out = fma2(c2(-(2.0f / 3.0f) * c.dt), nrhs, fma2(c2(1.0f / 3.0f), gn, mul2(c2(2.0f / 3.0f), gc)));
-        if (valid) {
-            Gout[oa] = out.x;
-            if (k + 1 < z1) Gout[oa + sz] = out.y;
-        }
-
-        // ---- advance the z queues by two planes ----
+        // ---- cell update, rows A and B ----
 #pragma unroll
-        for (int d = 0; d < 6; ++d) zq[d] = zq[d + 2];
-        zq[6] = zn0;
-        zq[7] = zn1;
-        qz_a = make_float2(qz_k1, qz_b.x);   // (q(k+1), q(k+2)) -> new (q(k'-1), q(k'))
-        qz_k1 = qz_b.y;                      // q(k+3) -> new q(k'+1)
-        zprevL = zL.y;
-        zprevR = zR.y;
+        for (int h = 0; h < 2; ++h) {
+            const IDX o = zo[0] + (h ? colB : colA);
+            const float* f = stg + cs * NFIELD * BFTILE + (ra + h) * TX + tx;
+            constexpr int pl = BY * TX;
+            const float2 uu = make_float2(f[0], f[pl]);
+            const float2 vv = make_float2(f[BFTILE], f[BFTILE + pl]);
+            const float2 ww = make_float2(f[2 * BFTILE], f[2 * BFTILE + pl]);
+            const float2 gn = STAGE > 1 ? make_float2(f[3 * BFTILE], f[3 * BFTILE + pl]) : c2(0.0f);
+            const float2 s_l = has_sl ? make_float2(f[4 * BFTILE], f[4 * BFTILE + pl]) : c2(c.s_l);
+            const int xf = (ra + h) * (TX + 1) + tx;
+            // centre values G(k), G(k+1): the queues already advanced by two planes
+            const float2 gc = h ? make_float2(zb.zq[1], zb.zq[2]) : make_float2(za.zq[1], za.zq[2]);
+            const float2 out = cell_pair<STAGE>(
+                c, gc, h ? gxB : gxA, h ? gyB : gyA, h ? gzB : gzA, uu, vv, ww, gn, s_l,
+                sub2(FL[xf + 1], FL[xf]), sub2(FR[xf + 1], FR[xf]), h ? dyLB : dyLA, h ? dyRB : dyRA,
+                h ? dzLB : dzLA, h ? dzRB : dzRA);
+            if (h ? vb : va) {
+                Gout[o] = out.x;
+                if (k + 1 < z1) Gout[o + sz] = out.y;
+            }
+        }
         buf ^= 1;
         if (++cs == NSTAGE) {
             cs = 0;
@@ -475,13 +535,13 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
     return fn;
 }
 
-// 3D map over a compact FP32 field with a (32, 8, 2) box; zero fill outside.
-bool encode_field(CUtensorMap* m, const float* ptr, const Geo& g) {
+// 3D map over a compact FP32 field with a (32, rows, depth) box; zero fill outside.
+bool encode_field(CUtensorMap* m, const float* ptr, const Geo& g, int rows, int depth) {
     PFN_cuTensorMapEncodeTiled_v12000 fn = encode_fn();
     if (!fn || !ptr) return false;
     cuuint64_t dims[3] = {(cuuint64_t)g.nx, (cuuint64_t)g.ny, (cuuint64_t)g.nz};
     cuuint64_t strides[2] = {(cuuint64_t)g.nx * 4, (cuuint64_t)g.nx * g.ny * 4};
-    cuuint32_t box[3] = {TX, TY, 2};
+    cuuint32_t box[3] = {TX, (cuuint32_t)rows, (cuuint32_t)depth};
     cuuint32_t estr[3] = {1, 1, 1};
     return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, (void*)ptr, dims, strides, box, estr,
               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
@@ -491,16 +551,14 @@ bool encode_field(CUtensorMap* m, const float* ptr, const Geo& g) {
 template <int STAGE, bool TMA, typename IDX>
 cudaError_t launch_one(const StageArgs& a, const Coef& c, const TmaMaps& tm, int* err, cudaStream_t st) {
     const dim3 block(TX, TY, 1);
-    const dim3 grid((a.g.nx + TX - 1) / TX, (a.g.ny + TY - 1) / TY, (a.g.nz + c.zc - 1) / c.zc);
-    const size_t dyn = TMA ? (size_t)NSTAGE * NFIELD * FTILE * sizeof(float) : 0;
-    auto kern = stage3d_f32_pair<STAGE, TMA, IDX>;
-    if (TMA) {
-        static bool attr_set = false;  // per instantiation
-        if (!attr_set) {
-            cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
-            if (e != cudaSuccess) return e;
-            attr_set = true;
-        }
+    const dim3 grid((a.g.nx + TX - 1) / TX, (a.g.ny + BY - 1) / BY, (a.g.nz + c.zc - 1) / c.zc);
+    const size_t dyn = (size_t)NSTAGE * NFIELD * BFTILE * sizeof(float);
+    auto kern = stage3d_f32_col2<STAGE, TMA, IDX>;
+    static bool attr_set = false;  // per instantiation
+    if (!attr_set) {
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+        if (e != cudaSuccess) return e;
+        attr_set = true;
     }
     kern<<<grid, block, dyn, st>>>(a.g, (const float*)a.Gin, (const float*)a.Gn, (float*)a.Gout,
                                     (const float*)a.u, (const float*)a.v, (const float*)a.w,
@@ -513,6 +571,30 @@ cudaError_t launch_stage(const StageArgs& a, const Coef& c, const TmaMaps& tm, i
     if (a.stage == 1) return launch_one<1, TMA, IDX>(a, c, tm, err, st);
     if (a.stage == 2) return launch_one<2, TMA, IDX>(a, c, tm, err, st);
     return launch_one<3, TMA, IDX>(a, c, tm, err, st);
+}
+
+// z-chunk of the default tile shape: the fewest waves of chunk work over the
+// resident CTA slots (2 per SM), counting a chunk's queue prologue as three
+// plane-pair iterations; small grids take short chunks so every SM has work.
+int default_zc(const Geo& g) {
+    static const int slots = [] {
+        int dev = 0, n = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        return 2 * (n > 0 ? n : 1);
+    }();
+    const long long cols = (long long)((g.nx + TX - 1) / TX) * ((g.ny + BY - 1) / BY);
+    int best = MAXZC;
+    long long best_cost = -1;
+    for (int zc : {MAXZC, 32, 16}) {
+        const long long ctas = cols * ((g.nz + zc - 1) / zc);
+        const long long cost = (ctas + slots - 1) / slots * (zc / 2 + 3);
+        if (best_cost < 0 || cost < best_cost) {
+            best_cost = cost;
+            best = zc;
+        }
+    }
+    return best;
 }
 
 }  // namespace
@@ -529,14 +611,14 @@ cudaError_t launch_stage3d_f32_tiled(const StageArgs& a, int* err, cudaStream_t 
     c.s_l = (float)a.s_l;
     c.eps = (float)a.eps;
     c.dt = (float)a.dt;
-    c.zc = (a.tile == 16 || a.tile == 32) ? a.tile : MAXZC;
+    c.zc = (a.tile == 16 || a.tile == 32 || a.tile == MAXZC) ? a.tile : default_zc(a.g);
     TmaMaps tm;
     std::memset(&tm, 0, sizeof(tm));
     // bulk tensor copies need 16-byte row pitch and an error flag to report into
     bool tma = err != nullptr && (a.g.nx % 4) == 0;
     const void* fields[NFIELD] = {a.u, a.v, a.w, a.stage > 1 ? a.Gn : nullptr, a.sl};
     for (int f = 0; f < NFIELD && tma; ++f)
-        if (fields[f] && !encode_field(&tm.m[f], (const float*)fields[f], a.g)) tma = false;
+        if (fields[f] && !encode_field(&tm.m[f], (const float*)fields[f], a.g, BY, 2)) tma = false;
     const bool small = a.g.cells() < (1LL << 31) - 1;
     cudaError_t e;
     if (tma) e = small ? launch_stage<true, int>(a, c, tm, err, st) : launch_stage<true, long long>(a, c, tm, err, st);
