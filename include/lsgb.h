@@ -281,7 +281,9 @@ LSGB_API int lsgb_batch_destroy(lsgb_batch* b);
 LSGB_API int lsgb_batch_add(lsgb_batch* b, const lsgb_params* p, lsgb_solver** solver, int* index);
 LSGB_API int lsgb_batch_size(const lsgb_batch* b, int* n);
 LSGB_API int lsgb_batch_solver(lsgb_batch* b, int index, lsgb_solver** out);
-/* lsgb_solver_autotune on every instance. */
+/* lsgb_solver_autotune on every instance, then (FP32) each uniform z-chunk
+ * (16, 32, 64) for the 3D instances against that, timed as one stage of the
+ * whole batch over its lanes; the fastest assignment of tiles stays. */
 LSGB_API int lsgb_batch_autotune(lsgb_batch* b, int reps);
 /* Advance every instance n_steps steps (asynchronous on the batch stream;
  * later calls on an instance's own handle are ordered after it). */

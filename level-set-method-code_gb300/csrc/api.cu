@@ -1103,10 +1103,84 @@ extern "C" int lsgb_batch_solver(lsgb_batch* b, int index, lsgb_solver** out) {
     return LSGB_OK;
 }
 
+namespace {
+
+// One RK3 stage-1 launch (G -> A, the state is not touched) of every
+// instance, spread over the lanes as a step spreads them, `reps` times;
+// CUDA-event time per repetition on the batch stream.
+int batch_time_stage1(lsgb_batch* b, int reps, float* ms) {
+    cudaEvent_t e0, e1;
+    LSGB_CUDA(cudaEventCreate(&e0));
+    LSGB_CUDA(cudaEventCreate(&e1));
+    int rc = LSGB_OK;
+    cudaEventRecord(e0, b->main);
+    cudaEventRecord(b->fork, b->main);
+    for (cudaStream_t l : b->lanes) cudaStreamWaitEvent(l, b->fork, 0);
+    for (int r = 0; r < reps && rc == LSGB_OK; ++r)
+        for (size_t i = 0; i < b->inst.size() && rc == LSGB_OK; ++i) {
+            lsgb_solver* s = b->inst[i];
+            cudaStream_t own = s->st;
+            s->st = b->lanes[i % b->lanes.size()];
+            StageArgs a = stage_args(s->p, s->g, s->lay);
+            a.u = s->u; a.v = s->v; a.w = s->w; a.sl = s->sl;
+            a.err = err_flag(s);
+            a.tile = s->tile;
+            a.Gn = s->G; a.Gin = s->G; a.Gout = s->A; a.stage = 1;
+            rc = launch_stage(s, a);
+            s->st = own;
+        }
+    for (size_t l = 0; l < b->lanes.size(); ++l) {
+        cudaEventRecord(b->lane_done[l], b->lanes[l]);
+        cudaStreamWaitEvent(b->main, b->lane_done[l], 0);
+    }
+    cudaEventRecord(e1, b->main);
+    if (cudaEventSynchronize(e1) != cudaSuccess && rc == LSGB_OK) rc = fail(LSGB_ERR_CUDA, "batch timing failed");
+    float t = 0.0f;
+    cudaEventElapsedTime(&t, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    *ms = t / (reps > 0 ? reps : 1);
+    return rc;
+}
+
+}  // namespace
+
+// Tiles for throughput of the whole batch: every instance's fastest shape
+// alone (lsgb_solver_autotune), then each uniform z-chunk for the 3D
+// instances, timed together over the lanes; the fastest assignment stays.
+// (Alone, short chunks win by filling the SMs; run together, the lanes fill
+// them and long chunks win by their smaller halo overhead.)
 extern "C" int lsgb_batch_autotune(lsgb_batch* b, int reps) {
     LSGB_TRY(batch_ok(b));
     for (lsgb_solver* s : b->inst) LSGB_TRY(lsgb_solver_autotune(s, reps, nullptr, nullptr));
     batch_drop_graph(b);
+    if (b->prec != LSGB_PREC_F32 || b->inst.empty()) return LSGB_OK;
+    for (lsgb_solver* s : b->inst)
+        if (!s->have_G || !s->have_vel) return LSGB_OK;
+    if (reps < 1) reps = 3;
+    std::vector<int> best(b->inst.size());
+    for (size_t i = 0; i < b->inst.size(); ++i) best[i] = b->inst[i]->tile;
+    float t_best = 0.0f;
+    LSGB_TRY(batch_time_stage1(b, 1, &t_best));  // warm-up
+    LSGB_TRY(batch_time_stage1(b, reps, &t_best));
+    const std::vector<int> tuned = best;
+    for (int zc : {16, 32, 64}) {
+        bool any = false;
+        for (size_t i = 0; i < b->inst.size(); ++i) {
+            lsgb_solver* s = b->inst[i];
+            s->tile = s->p.dim == 3 ? zc : tuned[i];
+            any = any || s->p.dim == 3;
+        }
+        if (!any) break;
+        float t = 0.0f;
+        LSGB_TRY(batch_time_stage1(b, reps, &t));
+        if (t < t_best) {
+            t_best = t;
+            for (size_t i = 0; i < b->inst.size(); ++i) best[i] = b->inst[i]->tile;
+        }
+    }
+    for (size_t i = 0; i < b->inst.size(); ++i) b->inst[i]->tile = best[i];
+    for (lsgb_solver* s : b->inst) LSGB_TRY(check_flag(s));
     return LSGB_OK;
 }
 

@@ -290,7 +290,8 @@ template <int STAGE, bool TMA, typename IDX>
 __global__ void __launch_bounds__(NT, 2)
 stage3d_f32_col2(Geo g, const float* __restrict__ Gin, const float* __restrict__ Gn, float* __restrict__ Gout,
                  const float* __restrict__ u, const float* __restrict__ v, const float* __restrict__ w,
-                 const float* __restrict__ sl, Coef c, const __grid_constant__ TmaMaps tm, int* __restrict__ err) {
+                 const float* __restrict__ sl, Coef c, const __grid_constant__ TmaMaps tm, int* __restrict__ err,
+                 int hsl /* sl != nullptr */) {
     __shared__ float2 P2[2][BPH][PW];
     __shared__ float2 FL[BNFX], FR[BNFX];  // x faces [BY][TX+1]
     __shared__ IDX zoff[MAXZC + 10];
@@ -304,7 +305,7 @@ stage3d_f32_col2(Geo g, const float* __restrict__ Gin, const float* __restrict__
     const int z1 = min(z0 + c.zc, g.nz);
     const int niter = (z1 - z0 + 1) / 2;
     const IDX sz = (IDX)g.nx * g.ny;
-    const bool has_sl = sl != nullptr;
+    const bool has_sl = hsl != 0;
     const int ra = RY * ty;  // tile row of cell row A; row B = ra + 1
     const bool xin = (i0 + tx) < g.nx;
     const bool va = xin && (j0 + ra) < g.ny;
@@ -562,7 +563,7 @@ cudaError_t launch_one(const StageArgs& a, const Coef& c, const TmaMaps& tm, int
     }
     kern<<<grid, block, dyn, st>>>(a.g, (const float*)a.Gin, (const float*)a.Gn, (float*)a.Gout,
                                     (const float*)a.u, (const float*)a.v, (const float*)a.w,
-                                    (const float*)a.sl, c, tm, err);
+                                    (const float*)a.sl, c, tm, err, a.sl != nullptr);
     return cudaGetLastError();
 }
 
