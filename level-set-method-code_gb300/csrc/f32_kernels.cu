@@ -136,11 +136,14 @@ __global__ void __launch_bounds__(256) stage_f32_kernel(Geo g, const float* __re
 // :46-89) are recomputed from phi0 in FP64, and on flagged cells the forcing
 // and the update are formed in FP64 before the final rounding.
 // The pseudo-step at one cell from its value phi, phi0 and the neighbour
-// values pn / p0 in the order -x, +x, -y, +y (, -z, +z).
+// values pn / p0 in the order -x, +x, -y, +y (, -z, +z), in two parts: the
+// FP32 Godunov term and the constraint's crossing flags / stability test
+// (reinit_cell_f32), and the FP64 constrained update of a forced cell
+// (reinit_forced_f64).
 template <int DIM>
-__device__ __forceinline__ float reinit_cell(float phi, float ph0, const float* pn, const float* p0, float inv_dx,
-                                             float inv_dy, float inv_dz, float dx2, float dtau_f, double dx,
-                                             double dtau, double beta) {
+__device__ __forceinline__ float reinit_cell_f32(float phi, float ph0, const float* pn, const float* p0,
+                                                 float inv_dx, float inv_dy, float inv_dz, float dx2,
+                                                 int& flag, bool& forced) {
     const float S = ph0 * rsqrtf(fmaf(ph0, ph0, dx2));
     const bool pos = S > 0.0f;
     float gsq = 0.0f;
@@ -159,34 +162,36 @@ __device__ __forceinline__ float reinit_cell(float phi, float ph0, const float* 
     // computeInterfaceCrossings3D is a sign test: the exact product of two
     // floats is never rounded to zero in FP64, so comparing signs in FP32
     // decides it identically; only flagged cells go on to FP64 arithmetic.
-    int flag = 0;
+    flag = 0;
 #pragma unroll
     for (int q = 0; q < 2 * DIM; ++q)
         if ((ph0 < 0.0f && p0[q] > 0.0f) || (ph0 > 0.0f && p0[q] < 0.0f)) flag |= 1 << q;
-    bool forced = false;
-    double outd = 0.0;
-    if (flag != 0) {
-        double sum0 = 0.0;
-        int cnt = 0;
+    bool stable = flag != 0 && (phi > 0.0f) == (ph0 > 0.0f);
 #pragma unroll
-        for (int q = 0; q < 2 * DIM; ++q)
-            if ((flag >> q) & 1) { sum0 += (double)p0[q]; cnt++; }
-        bool stable = (phi > 0.0f) == (ph0 > 0.0f);
+    for (int q = 0; q < 2 * DIM; ++q)
+        if ((flag >> q) & 1) stable = stable && ((pn[q] > 0.0f) == (p0[q] > 0.0f));
+    forced = stable;
+    return term;
+}
+
+// FP64 update of a forced cell: r~ from the crossing neighbours' phi0, the
+// forcing beta (r~ sum(phi of crossing neighbours) - phi) / dx, and
+// phi + dtau (term + forcing), rounded once to FP32.
+template <int DIM>
+__device__ __forceinline__ float reinit_forced_f64(float phi, float ph0, float term, int flag, const float* pn,
+                                                   const float* p0, double dx, double dtau, double beta) {
+    double sum0 = 0.0;
+    int cnt = 0;
 #pragma unroll
-        for (int q = 0; q < 2 * DIM; ++q)
-            if ((flag >> q) & 1) stable = stable && ((pn[q] > 0.0f) == (p0[q] > 0.0f));
-        if (stable) {
-            const double rt = (cnt > 0 && fabs(sum0) > 1e-15) ? (double)ph0 / sum0 : 0.0;
-            double sum = 0.0;
+    for (int q = 0; q < 2 * DIM; ++q)
+        if ((flag >> q) & 1) { sum0 += (double)p0[q]; cnt++; }
+    const double rt = (cnt > 0 && fabs(sum0) > 1e-15) ? (double)ph0 / sum0 : 0.0;
+    double sum = 0.0;
 #pragma unroll
-            for (int q = 0; q < 2 * DIM; ++q)
-                if ((flag >> q) & 1) sum += (double)pn[q];
-            const double forcing = beta * (rt * sum - (double)phi) / dx;
-            outd = (double)phi + dtau * ((double)term + forcing);
-            forced = true;
-        }
-    }
-    return forced ? (float)outd : fmaf(dtau_f, term, phi);
+    for (int q = 0; q < 2 * DIM; ++q)
+        if ((flag >> q) & 1) sum += (double)pn[q];
+    const double forcing = beta * (rt * sum - (double)phi) / dx;
+    return (float)((double)phi + dtau * ((double)term + forcing));
 }
 
 // Neighbour offset along one axis: +-stride inside, the periodic image or
@@ -197,38 +202,80 @@ __device__ __forceinline__ IDX nb_off(int c, int n, int bc, IDX stride, bool up)
     return c > 0 ? -stride : (bc == LSGB_BC_PERIODIC ? (IDX)(n - 1) * stride : (IDX)0);
 }
 
+constexpr int RT = 256;  // threads of a pseudo-step block
+
+// One pseudo-step, one thread per cell.  Forced cells (the interface band)
+// are rare and their FP64 update is long, so a block queues them in shared
+// memory and finishes them with dense lanes after the FP32 pass: a warp that
+// holds one forced cell no longer runs the FP64 sequence for all 32 lanes.
 template <int DIM, typename IDX>
-__global__ void __launch_bounds__(256) reinit_f32_kernel(Geo g, const float* __restrict__ phin,
-                                                         const float* __restrict__ phi0,
-                                                         float* __restrict__ phinew, float inv_dx,
-                                                         float inv_dy, float inv_dz, float dx2,
-                                                         float dtau_f, double dx, double dtau,
-                                                         double beta) {
+__global__ void __launch_bounds__(RT) reinit_f32_kernel(Geo g, const float* __restrict__ phin,
+                                                        const float* __restrict__ phi0,
+                                                        float* __restrict__ phinew, float inv_dx,
+                                                        float inv_dy, float inv_dz, float dx2,
+                                                        float dtau_f, double dx, double dtau,
+                                                        double beta) {
+    __shared__ int nq;
+    __shared__ IDX q_id[RT];
+    __shared__ int q_flag[RT];
+    __shared__ float q_phi[RT], q_ph0[RT], q_term[RT];
+    __shared__ float q_pn[2 * DIM][RT], q_p0[2 * DIM][RT];
+    const int t = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+    if (t == 0) nq = 0;
+    __syncthreads();
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     int j = blockIdx.y * blockDim.y + threadIdx.y;
     int k = DIM == 3 ? blockIdx.z * blockDim.z + threadIdx.z : 0;
-    if (i >= g.nx || j >= g.ny || k >= g.nz) return;
-    const IDX sy = g.nx;
-    const IDX sz = (IDX)g.nx * g.ny;
-    const IDX id = (IDX)j * sy + (IDX)k * sz + i;
-    IDX nb[6];
-    nb[0] = id + nb_off<IDX>(i, g.nx, g.bcx, (IDX)1, false);
-    nb[1] = id + nb_off<IDX>(i, g.nx, g.bcx, (IDX)1, true);
-    nb[2] = id + nb_off<IDX>(j, g.ny, g.bcy, sy, false);
-    nb[3] = id + nb_off<IDX>(j, g.ny, g.bcy, sy, true);
-    if (DIM == 3) {
-        nb[4] = id + nb_off<IDX>(k, g.nz, g.bcz, sz, false);
-        nb[5] = id + nb_off<IDX>(k, g.nz, g.bcz, sz, true);
-    }
-    const float phi = __ldg(phin + id);
-    const float ph0 = __ldg(phi0 + id);
-    float pn[6], p0[6];
+    if (i < g.nx && j < g.ny && k < g.nz) {
+        const IDX sy = g.nx;
+        const IDX sz = (IDX)g.nx * g.ny;
+        const IDX id = (IDX)j * sy + (IDX)k * sz + i;
+        IDX nb[6];
+        nb[0] = id + nb_off<IDX>(i, g.nx, g.bcx, (IDX)1, false);
+        nb[1] = id + nb_off<IDX>(i, g.nx, g.bcx, (IDX)1, true);
+        nb[2] = id + nb_off<IDX>(j, g.ny, g.bcy, sy, false);
+        nb[3] = id + nb_off<IDX>(j, g.ny, g.bcy, sy, true);
+        if (DIM == 3) {
+            nb[4] = id + nb_off<IDX>(k, g.nz, g.bcz, sz, false);
+            nb[5] = id + nb_off<IDX>(k, g.nz, g.bcz, sz, true);
+        }
+        const float phi = __ldg(phin + id);
+        const float ph0 = __ldg(phi0 + id);
+        float pn[6], p0[6];
 #pragma unroll
-    for (int q = 0; q < 2 * DIM; ++q) {
-        pn[q] = __ldg(phin + nb[q]);
-        p0[q] = __ldg(phi0 + nb[q]);
+        for (int q = 0; q < 2 * DIM; ++q) {
+            pn[q] = __ldg(phin + nb[q]);
+            p0[q] = __ldg(phi0 + nb[q]);
+        }
+        int flag;
+        bool forced;
+        const float term = reinit_cell_f32<DIM>(phi, ph0, pn, p0, inv_dx, inv_dy, inv_dz, dx2, flag, forced);
+        if (forced) {
+            const int e = atomicAdd(&nq, 1);
+            q_id[e] = id;
+            q_flag[e] = flag;
+            q_phi[e] = phi;
+            q_ph0[e] = ph0;
+            q_term[e] = term;
+#pragma unroll
+            for (int q = 0; q < 2 * DIM; ++q) {
+                q_pn[q][e] = pn[q];
+                q_p0[q][e] = p0[q];
+            }
+        } else {
+            phinew[id] = fmaf(dtau_f, term, phi);
+        }
     }
-    phinew[id] = reinit_cell<DIM>(phi, ph0, pn, p0, inv_dx, inv_dy, inv_dz, dx2, dtau_f, dx, dtau, beta);
+    __syncthreads();
+    for (int e = t; e < nq; e += RT) {
+        float pn[6], p0[6];
+#pragma unroll
+        for (int q = 0; q < 2 * DIM; ++q) {
+            pn[q] = q_pn[q][e];
+            p0[q] = q_p0[q][e];
+        }
+        phinew[q_id[e]] = reinit_forced_f64<DIM>(q_phi[e], q_ph0[e], q_term[e], q_flag[e], pn, p0, dx, dtau, beta);
+    }
 }
 
 inline dim3 cell_block(const Geo& g) { return g.dim == 3 ? dim3(32, 4, 2) : dim3(32, 8, 1); }
