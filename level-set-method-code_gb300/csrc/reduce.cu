@@ -1,10 +1,12 @@
 // reduce.cu -- deterministic on-device reductions over the interior cells.
 //
-// Two passes with a fixed grid: pass 1 reduces a grid-stride share per block
-// (warp shuffles, then one shared-memory step across the block's warps) into
-// `partials`; pass 2 reduces the partials in a single block in a fixed order.
-// The result is therefore the same bits on every run for a given grid size.
-// Sums accumulate in FP64 whatever the field precision.
+// Two passes with a fixed grid: pass 1 reduces a fixed share of rows per
+// block (warp shuffles, then one shared-memory step across the block's warps)
+// into `partials`; pass 2 reduces the partials in a single block in a fixed
+// order.  The result is therefore the same bits on every run for a given grid
+// size.  Sums accumulate in FP64 whatever the field precision; counts in
+// 64-bit integers (exact; FP64 adds run at a small fraction of the FP32 rate
+// on this GPU).
 //
 // Reference counterparts: computeInterfaceVolume (Local_code/level-set_MPI_3D/
 // include/io.h:263-288), computeL2Error3D (io.h:229-258), and the velocity
@@ -52,30 +54,35 @@ __device__ __forceinline__ void block_reduce2(double& a, double& b) {
     }
 }
 
-template <int OP, typename F>
+// Pass 1: one warp per row of the interior (rows (j, k) dealt round-robin
+// to the grid's warps, lanes along x), so the loads are coalesced and no
+// per-cell index arithmetic is needed.  The functor F keeps a per-thread
+// state (F::State), adds cells to it (F::add) and hands two doubles to the
+// block reduction (F::finish); F::OP is the combining operation.
+template <typename F>
 __global__ void __launch_bounds__(RED_THREADS) red_pass1(Geo g, F f, double* partials) {
-    double a = identity<OP>(), b = identity<OP>();
-    const long long n = g.cells();
-    const long long nxy = (long long)g.nx * g.ny;
-    for (long long e = blockIdx.x * (long long)RED_THREADS + threadIdx.x; e < n;
-         e += (long long)gridDim.x * RED_THREADS) {
-        const int k = (int)(e / nxy);
-        const long long r = e - (long long)k * nxy;
-        const int j = (int)(r / g.nx);
-        const int i = (int)(r - (long long)j * g.nx);
-        double x, y;
-        f(i, j, k, x, y);
-        a = combine<OP>(a, x);
-        b = combine<OP>(b, y);
+    typename F::State st = F::init();
+    constexpr int WPB = RED_THREADS / 32;
+    const int lane = threadIdx.x & 31;
+    const int nrows = g.ny * g.nz;
+    for (int row = blockIdx.x * WPB + (threadIdx.x >> 5); row < nrows; row += gridDim.x * WPB) {
+        const int k = row / g.ny;
+        const int j = row - k * g.ny;
+        for (int i = lane; i < g.nx; i += 32) f.add(st, i, j, k);
     }
-    block_reduce2<OP>(a, b);
+    double a, b;
+    F::finish(st, a, b);
+    block_reduce2<F::OP>(a, b);
     if (threadIdx.x == 0) {
         partials[2 * blockIdx.x] = a;
         partials[2 * blockIdx.x + 1] = b;
     }
 }
 
-template <int OP>
+// Pass 2 over the block partials; SQRT_B takes the square root of the second
+// result (a maximum of squares: sqrt is monotone, so this is the maximum of
+// the roots bit for bit).
+template <int OP, bool SQRT_B>
 __global__ void __launch_bounds__(RED_THREADS) red_pass2(int nblocks, const double* partials, double* out) {
     double a = identity<OP>(), b = identity<OP>();
     for (int q = threadIdx.x; q < nblocks; q += RED_THREADS) {
@@ -83,15 +90,19 @@ __global__ void __launch_bounds__(RED_THREADS) red_pass2(int nblocks, const doub
         b = combine<OP>(b, partials[2 * q + 1]);
     }
     block_reduce2<OP>(a, b);
-    if (threadIdx.x == 0) { out[0] = a; out[1] = b; }
+    if (threadIdx.x == 0) {
+        out[0] = a;
+        out[1] = SQRT_B ? sqrt(b) : b;
+    }
 }
 
-template <int OP, typename F>
+template <typename F, bool SQRT_B = false>
 cudaError_t run_reduce(const Geo& g, F f, double* partials, double* out, cudaStream_t st) {
-    long long want = (g.cells() + RED_THREADS - 1) / RED_THREADS;
-    int nb = (int)(want < RED_BLOCKS ? (want < 1 ? 1 : want) : RED_BLOCKS);
-    red_pass1<OP><<<nb, RED_THREADS, 0, st>>>(g, f, partials);
-    red_pass2<OP><<<1, RED_THREADS, 0, st>>>(nb, partials, out);
+    const long long rows = (long long)g.ny * g.nz;
+    const long long want = (rows + RED_THREADS / 32 - 1) / (RED_THREADS / 32);
+    const int nb = (int)(want < RED_BLOCKS ? (want < 1 ? 1 : want) : RED_BLOCKS);
+    red_pass1<F><<<nb, RED_THREADS, 0, st>>>(g, f, partials);
+    red_pass2<F::OP, SQRT_B><<<1, RED_THREADS, 0, st>>>(nb, partials, out);
     count_launches(2);
     return cudaGetLastError();
 }
@@ -100,48 +111,64 @@ __host__ __device__ __forceinline__ long long addr(const Lay& l, int i, int j, i
     return l.off + i + (long long)j * l.sy + (long long)k * l.sz;
 }
 
+// Cells with G < 0, counted exactly in a 64-bit integer per thread.
 template <typename T>
 struct CountNeg {
+    static constexpr int OP = OP_SUM;
+    using State = long long;
     Lay l;
     const T* G;
-    __device__ void operator()(int i, int j, int k, double& x, double& y) const {
-        x = G[addr(l, i, j, k)] < (T)0 ? 1.0 : 0.0;
-        y = 0.0;
-    }
+    __device__ static State init() { return 0; }
+    __device__ void add(State& s, int i, int j, int k) const { s += G[addr(l, i, j, k)] < (T)0 ? 1 : 0; }
+    __device__ static void finish(State s, double& a, double& b) { a = (double)s; b = 0.0; }
 };
 
+// sum of (G - R)^2 in FP64.
 template <typename T>
 struct SqDiff {
+    static constexpr int OP = OP_SUM;
+    using State = double;
     Lay l, rl;
     const T* G;
     const double* R;
-    __device__ void operator()(int i, int j, int k, double& x, double& y) const {
+    __device__ static State init() { return 0.0; }
+    __device__ void add(State& s, int i, int j, int k) const {
         const double d = (double)G[addr(l, i, j, k)] - R[addr(rl, i, j, k)];
-        x = d * d;
-        y = 0.0;
+        s += d * d;
     }
+    __device__ static void finish(State s, double& a, double& b) { a = s; b = 0.0; }
 };
 
+// max(|u| + |v| + |w|) and max(u^2 + v^2 + w^2) in FP64 (the root is taken
+// once, in pass 2).
 template <typename T>
 struct Speed {
+    static constexpr int OP = OP_MAX;
+    struct State {
+        double l1, sq;
+    };
     Lay l;
     const T *u, *v, *w;
-    __device__ void operator()(int i, int j, int k, double& x, double& y) const {
+    __device__ static State init() { return State{-DBL_MAX, -DBL_MAX}; }
+    __device__ void add(State& s, int i, int j, int k) const {
         const long long a = addr(l, i, j, k);
         const double uu = (double)u[a], vv = (double)v[a], ww = w ? (double)w[a] : 0.0;
-        x = fabs(uu) + fabs(vv) + fabs(ww);
-        y = sqrt(uu * uu + vv * vv + ww * ww);
+        s.l1 = fmax(s.l1, fabs(uu) + fabs(vv) + fabs(ww));
+        s.sq = fmax(s.sq, uu * uu + vv * vv + ww * ww);
     }
+    __device__ static void finish(State s, double& a, double& b) { a = s.l1; b = s.sq; }
 };
 
+// Cells whose value is not finite, counted exactly.
 template <typename T>
 struct NonFinite {
+    static constexpr int OP = OP_SUM;
+    using State = long long;
     Lay l;
     const T* G;
-    __device__ void operator()(int i, int j, int k, double& x, double& y) const {
-        x = isfinite((double)G[addr(l, i, j, k)]) ? 0.0 : 1.0;
-        y = 0.0;
-    }
+    __device__ static State init() { return 0; }
+    __device__ void add(State& s, int i, int j, int k) const { s += isfinite((double)G[addr(l, i, j, k)]) ? 0 : 1; }
+    __device__ static void finish(State s, double& a, double& b) { a = (double)s; b = 0.0; }
 };
 
 }  // namespace
@@ -149,25 +176,25 @@ struct NonFinite {
 template <typename T>
 cudaError_t launch_count_negative(const Geo& g, const Lay& lay, const T* G, double* partials,
                                   double* out, cudaStream_t st) {
-    return run_reduce<OP_SUM>(g, CountNeg<T>{lay, G}, partials, out, st);
+    return run_reduce(g, CountNeg<T>{lay, G}, partials, out, st);
 }
 
 template <typename T>
 cudaError_t launch_sq_diff(const Geo& g, const Lay& lay, const T* G, const double* Gref,
                            const Lay& ref_lay, double* partials, double* out, cudaStream_t st) {
-    return run_reduce<OP_SUM>(g, SqDiff<T>{lay, ref_lay, G, Gref}, partials, out, st);
+    return run_reduce(g, SqDiff<T>{lay, ref_lay, G, Gref}, partials, out, st);
 }
 
 template <typename T>
 cudaError_t launch_max_speed(const Geo& g, const Lay& lay, const T* u, const T* v, const T* w,
                              double* partials, double* out, cudaStream_t st) {
-    return run_reduce<OP_MAX>(g, Speed<T>{lay, u, v, g.dim == 3 ? w : nullptr}, partials, out, st);
+    return run_reduce<Speed<T>, true>(g, Speed<T>{lay, u, v, g.dim == 3 ? w : nullptr}, partials, out, st);
 }
 
 template <typename T>
 cudaError_t launch_nonfinite(const Geo& g, const Lay& lay, const T* G, double* partials,
                              double* out, cudaStream_t st) {
-    return run_reduce<OP_SUM>(g, NonFinite<T>{lay, G}, partials, out, st);
+    return run_reduce(g, NonFinite<T>{lay, G}, partials, out, st);
 }
 
 template cudaError_t launch_count_negative<float>(const Geo&, const Lay&, const float*, double*, double*, cudaStream_t);

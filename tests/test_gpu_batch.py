@@ -60,12 +60,14 @@ def test_batch_matches_single_runs(cuda, lsgb_mod, precision):
 
 
 def test_tile_shapes_are_bit_identical(cuda, lsgb_mod):
+    """Explicit shapes and the default (0) agree bit for bit; the 3D cases
+    cover the bulk-tensor staging (nx % 4 == 0) and the cp.async staging."""
     from lsgb import synthetic as syn
-    for dim, n in [(3, (36, 20, 70)), (2, (70, 45, 1))]:
+    for dim, n in [(3, (36, 20, 70)), (3, (37, 21, 30)), (2, (70, 45, 1))]:
         p, f = instance(lsgb_mod, syn, dim, n, 7, "f32")
         outs = []
         tiles = [16, 32, 64] if dim == 3 else [2, 4, 8]
-        for tile in tiles:
+        for tile in [0] + tiles:
             with lsgb_mod.Solver(p, "f32") as s:
                 s.set_fields(*f)
                 s.set_tile(tile)
