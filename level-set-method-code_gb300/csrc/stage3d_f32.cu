@@ -574,28 +574,22 @@ cudaError_t launch_stage(const StageArgs& a, const Coef& c, const TmaMaps& tm, i
     return launch_one<3, TMA, IDX>(a, c, tm, err, st);
 }
 
-// z-chunk of the default tile shape: the fewest waves of chunk work over the
-// resident CTA slots (2 per SM), counting a chunk's queue prologue as three
-// plane-pair iterations; small grids take short chunks so every SM has work.
+// z-chunk of the default tile shape: the longest chunk that still gives every
+// SM at least six CTAs (two resident at a time, so the last wave's tail and a
+// chunk's queue prologue stay small), else the shortest.  Calibrated on
+// 160^3 .. 512^3 against the timed alternatives (lsgb_solver_autotune picks
+// per grid by measurement).
 int default_zc(const Geo& g) {
-    static const int slots = [] {
+    static const int sms = [] {
         int dev = 0, n = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-        return 2 * (n > 0 ? n : 1);
+        return n > 0 ? n : 1;
     }();
     const long long cols = (long long)((g.nx + TX - 1) / TX) * ((g.ny + BY - 1) / BY);
-    int best = MAXZC;
-    long long best_cost = -1;
-    for (int zc : {MAXZC, 32, 16}) {
-        const long long ctas = cols * ((g.nz + zc - 1) / zc);
-        const long long cost = (ctas + slots - 1) / slots * (zc / 2 + 3);
-        if (best_cost < 0 || cost < best_cost) {
-            best_cost = cost;
-            best = zc;
-        }
-    }
-    return best;
+    for (int zc : {MAXZC, 32})
+        if (cols * ((g.nz + zc - 1) / zc) >= 6LL * sms) return zc;
+    return 16;
 }
 
 }  // namespace
