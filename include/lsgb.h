@@ -260,6 +260,13 @@ LSGB_API int lsgb_solver_kernel_times(lsgb_solver* s, double* stage_ms, int64_t*
 LSGB_API int lsgb_solver_set_tile(lsgb_solver* s, int tile);
 LSGB_API int lsgb_solver_get_tile(const lsgb_solver* s, int* tile);
 
+/* Test hook for the time-out path: while on, the TMA-fed FP32 3D stage kernel
+ * issues no bulk copies, so each of its CTAs gives up its bounded wait after
+ * about a second, sets the handle's device error flag and returns; the next
+ * synchronising call (lsgb_solver_get_G, ...) reports LSGB_ERR_CUDA and clears
+ * the flag.  The context stays usable.  Off by default; no other effect. */
+LSGB_API int lsgb_solver_debug_drop_copies(lsgb_solver* s, int on);
+
 /* Autotuner: times one stage launch per candidate tile shape (reps launches
  * each, CUDA events on the handle's stream; the state G is not modified) and
  * keeps the fastest.  Needs G and the velocity.  FP64 handles have one shape. */

@@ -344,6 +344,7 @@ struct lsgb_solver {
     double* h_res = nullptr;     // pinned result slots
     int step = 0;
     int tile = 0;  // tile-shape choice handed to the stage kernels (0 = default)
+    int drop_copies = 0;  // test hook (lsgb_solver_debug_drop_copies)
     bool have_G = false, have_vel = false;
     // kernel timing (lsgb_solver_enable_timing)
     bool timing = false;
@@ -467,6 +468,7 @@ int rk3_step(lsgb_solver* s) {
     a.u = s->u; a.v = s->v; a.w = s->w; a.sl = s->sl;
     a.err = err_flag(s);
     a.tile = s->tile;
+    a.drop_copies = s->drop_copies;
     a.Gn = s->G;
     a.Gin = s->G; a.Gout = s->A; a.stage = 1;
     LSGB_TRY(launch_stage(s, a));
@@ -920,6 +922,12 @@ extern "C" int lsgb_solver_get_tile(const lsgb_solver* s, int* tile) {
     LSGB_TRY(solver_ok(s));
     if (!tile) return fail(LSGB_ERR_INVALID, "tile is NULL");
     *tile = s->tile;
+    return LSGB_OK;
+}
+
+extern "C" int lsgb_solver_debug_drop_copies(lsgb_solver* s, int on) {
+    LSGB_TRY(solver_ok(s));
+    s->drop_copies = on ? 1 : 0;
     return LSGB_OK;
 }
 

@@ -84,6 +84,7 @@ struct StageArgs {
     int stage;               // 1, 2, 3
     int* err;                // nullable device error flag (bounded waits)
     int tile;                // tile-shape choice (0 = default; see lsgb_solver_set_tile)
+    int drop_copies;         // test hook: the TMA-fed kernel issues no bulk copies (its waits time out)
 };
 
 // HCR-2 pseudo-step arguments (handle path: r~ and flags recomputed from phi0).

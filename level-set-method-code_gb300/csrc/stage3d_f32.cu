@@ -80,6 +80,7 @@ struct TmaMaps {
 struct Coef {
     float inv_dx, inv_dy, inv_dz, inv_2dx, inv_2dy, inv_2dz, s_l, eps, dt;
     int zc;  // z-chunk length (even, <= MAXZC): tile shape chosen per grid by the autotuner
+    int drop;  // test hook: issue no bulk copies, so every wait runs into its limit
 };
 
 __device__ __forceinline__ float2 c2(float a) { return make_float2(a, a); }
@@ -383,8 +384,9 @@ stage3d_f32_col2(Geo g, const float* __restrict__ Gin, const float* __restrict__
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();  // zoff table and barriers ready
-    if (TMA && t == 0)
-        for (int it = 0; it < NSTAGE - 1 && it < niter; ++it) issue(it, it);
+    int issued = 0;  // iterations whose copies thread 0 has issued
+    if (TMA && t == 0 && !c.drop)
+        for (; issued < NSTAGE - 1 && issued < niter; ++issued) issue(issued, issued);
     if (!TMA)
         for (int it = 0; it < NSTAGE - 1; ++it) {
             if (it < niter) fetch(it, it);
@@ -424,9 +426,10 @@ stage3d_f32_col2(Geo g, const float* __restrict__ Gin, const float* __restrict__
         __syncthreads();
         // refill the stage last read in iteration it-1, which every thread
         // finished before the barrier above
-        if (TMA && t == 0 && it + NSTAGE - 1 < niter) {
+        if (TMA && t == 0 && !c.drop && it + NSTAGE - 1 < niter) {
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             issue(it + NSTAGE - 1, cs == 0 ? NSTAGE - 1 : cs - 1);
+            issued = it + NSTAGE;
         }
         if (!TMA) {
             if (it + NSTAGE - 1 < niter) fetch(it + NSTAGE - 1, cs == 0 ? NSTAGE - 1 : cs - 1);
@@ -478,11 +481,11 @@ stage3d_f32_col2(Geo g, const float* __restrict__ Gin, const float* __restrict__
             const bool ok = mbar_wait(&mbar[cs], cph);
             if (__syncthreads_or(!ok)) {
                 // a bulk copy did not arrive in time: flag it, give the copies
-                // still in flight a bounded chance to land, and leave
+                // still in flight (issued by thread 0) a bounded chance to
+                // land, and leave
                 if (t == 0) {
                     atomicExch(err, 1);
-                    for (int j = it; j < niter && j < it + NSTAGE; ++j)
-                        mbar_wait(&mbar[j % NSTAGE], (uint32_t)((j / NSTAGE) & 1));
+                    for (int j = it; j < issued; ++j) mbar_wait(&mbar[j % NSTAGE], (uint32_t)((j / NSTAGE) & 1));
                 }
                 return;
             }
@@ -607,6 +610,7 @@ cudaError_t launch_stage3d_f32_tiled(const StageArgs& a, int* err, cudaStream_t 
     c.eps = (float)a.eps;
     c.dt = (float)a.dt;
     c.zc = (a.tile == 16 || a.tile == 32 || a.tile == MAXZC) ? a.tile : default_zc(a.g);
+    c.drop = a.drop_copies;
     TmaMaps tm;
     std::memset(&tm, 0, sizeof(tm));
     // bulk tensor copies need 16-byte row pitch and an error flag to report into

@@ -23,6 +23,7 @@ _PKG = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 LIB_PATH = os.path.join(_PKG, "_build", "liblsgb.so")
 
 OK = 0
+ERR_INVALID, ERR_CUDA, ERR_ALLOC, ERR_NUMERIC, ERR_STATE, ERR_UNSUPPORTED = 1, 2, 3, 4, 5, 6
 BC_PERIODIC, BC_ZERO_GRADIENT = 0, 1
 PREC_F64, PREC_F32 = 0, 1
 LAYOUT_GHOSTED, LAYOUT_COMPACT = 0, 1
@@ -362,6 +363,13 @@ def _autotune(self, reps: int = 3):
     return t.value, ms.value
 
 
+def _debug_drop_copies(self, on: bool):
+    """Test hook: the TMA-fed FP32 3D stage kernel issues no bulk copies, so
+    its bounded waits time out and the next synchronising call raises."""
+    _check(lib().lsgb_solver_debug_drop_copies(self._h, int(bool(on))))
+
+
+Solver.debug_drop_copies = _debug_drop_copies
 Solver.set_tile = _set_tile
 Solver.get_tile = _get_tile
 Solver.autotune = _autotune
