@@ -1291,7 +1291,10 @@ struct lsgb_adjoint {
     int grads = LSGB_GRAD_SL | LSGB_GRAD_VELOCITY;  // parameter gradients accumulated
     size_t slot = 0;           // bytes per field slot (multiple of 256)
     int tape_slots = 0, ckpt_slots = 0;
-    char* tape = nullptr;      // recompute tape of one segment
+    char* tape = nullptr;      // the recompute tape the next launches use (one of tape_buf)
+    char* tape_buf[2] = {nullptr, nullptr};  // two tapes: segment n-1 is recorded while n is reversed
+    cudaStream_t rs = nullptr;               // recording stream (second tape only)
+    cudaEvent_t ev_rec[2] = {nullptr, nullptr}, ev_rev[2] = {nullptr, nullptr};
     char* ckpts = nullptr;     // G at every segment start
     void* coef = nullptr;      // coefficient planes (stage slab or HCR-2 full domain)
     int slab = 1;              // z planes per coefficient slab of the stage transpose (3D)
@@ -1557,10 +1560,16 @@ extern "C" int lsgb_adjoint_create(lsgb_solver* s, int checkpoint_interval, lsgb
 extern "C" int lsgb_adjoint_destroy(lsgb_adjoint* a) {
     if (!a) return LSGB_OK;
     if (a->s && a->s->st) cudaStreamSynchronize(a->s->st);
-    void* ptrs[] = {a->tape, a->ckpts, a->coef, a->lam[0], a->lam[1], a->lam[2], a->lam[3],
-                    a->grad[0], a->grad[1], a->grad[2], a->grad[3], a->target};
+    if (a->rs) cudaStreamSynchronize(a->rs);
+    void* ptrs[] = {a->tape_buf[0], a->tape_buf[1], a->ckpts, a->coef, a->lam[0], a->lam[1], a->lam[2],
+                    a->lam[3], a->grad[0], a->grad[1], a->grad[2], a->grad[3], a->target};
     for (void* q : ptrs)
         if (q) cudaFree(q);
+    for (int b = 0; b < 2; ++b) {
+        if (a->ev_rec[b]) cudaEventDestroy(a->ev_rec[b]);
+        if (a->ev_rev[b]) cudaEventDestroy(a->ev_rev[b]);
+    }
+    if (a->rs) cudaStreamDestroy(a->rs);
     delete a;
     return LSGB_OK;
 }
@@ -1673,27 +1682,83 @@ extern "C" int lsgb_adjoint_backward(lsgb_adjoint* a, const double* dL_dGT, int 
     }
     if (need > a->tape_slots) {
         LSGB_CUDA(cudaStreamSynchronize(s->st));
-        if (a->tape) cudaFree(a->tape);
-        a->tape = nullptr;
+        if (a->rs) LSGB_CUDA(cudaStreamSynchronize(a->rs));
+        for (int b = 0; b < 2; ++b) {
+            if (a->tape_buf[b]) cudaFree(a->tape_buf[b]);
+            a->tape_buf[b] = nullptr;
+        }
         a->tape_slots = 0;
-        LSGB_TRY(adj_alloc((void**)&a->tape, (size_t)need * a->slot, "adjoint tape"));
+        LSGB_TRY(adj_alloc((void**)&a->tape_buf[0], (size_t)need * a->slot, "adjoint tape"));
+        // the second tape is optional: without it the segments are recorded in turn
+        if (nseg > 1 && cudaMalloc((void**)&a->tape_buf[1], (size_t)need * a->slot) != cudaSuccess) {
+            cudaGetLastError();
+            a->tape_buf[1] = nullptr;
+        }
         a->tape_slots = need;
+    }
+    const bool two = a->tape_buf[1] != nullptr;
+    if (two && !a->rs) {
+        LSGB_CUDA(cudaStreamCreateWithFlags(&a->rs, cudaStreamNonBlocking));
+        for (int b = 0; b < 2; ++b) {
+            LSGB_CUDA(cudaEventCreateWithFlags(&a->ev_rec[b], cudaEventDisableTiming));
+            LSGB_CUDA(cudaEventCreateWithFlags(&a->ev_rev[b], cudaEventDisableTiming));
+        }
     }
     for (int b = 0; b < 4; ++b)
         if ((b == 0 && (a->grads & LSGB_GRAD_SL)) || (b > 0 && (a->grads & LSGB_GRAD_VELOCITY)))
             LSGB_CUDA(cudaMemsetAsync(a->grad[b], 0, sizeof(double) * (size_t)s->g.cells(), s->st));
-    // the current adjoint field lives in one of the four buffers
-    void* L = a->lam[0];
-    for (int seg = nseg - 1; seg >= 0; --seg) {
+    // Segment seg's tape: its checkpoint re-advanced with the forward kernels
+    // on stream st into tape buffer b.
+    auto record = [&](int seg, int b, cudaStream_t st) -> int {
         const int t0 = a->step0 + seg * a->ckpt, t1 = std::min(t0 + a->ckpt, a->step0 + a->n_steps);
         int slots = 0;
-        std::vector<TapeStep> plan = tape_plan(s->p, t0, t1, &slots);
-        LSGB_CUDA(cudaMemcpyAsync(tslot(a, 0), a->ckpts + (size_t)seg * a->slot, nbytes(s),
-                                  cudaMemcpyDeviceToDevice, s->st));
-        LSGB_TRY(adj_record(a, plan));
+        const std::vector<TapeStep> plan = tape_plan(s->p, t0, t1, &slots);
+        a->tape = a->tape_buf[b];
+        cudaStream_t own = s->st;
+        s->st = st;
+        int rc = LSGB_OK;
+        if (cudaMemcpyAsync(tslot(a, 0), a->ckpts + (size_t)seg * a->slot, nbytes(s), cudaMemcpyDeviceToDevice,
+                            st) != cudaSuccess)
+            rc = fail(LSGB_ERR_CUDA, "checkpoint restore: %s", cudaGetErrorString(cudaGetLastError()));
+        if (rc == LSGB_OK) rc = adj_record(a, plan);
+        s->st = own;
+        return rc;
+    };
+    // With two tapes, segment seg-1 is recorded on the recording stream while
+    // segment seg is reversed on the solver's stream (the recording of a
+    // buffer waits for the reversal that last read it).  Same kernels and
+    // inputs either way, so the gradients are the same bits.
+    if (two) {
+        LSGB_CUDA(cudaEventRecord(a->ev_rec[0], s->st));
+        LSGB_CUDA(cudaStreamWaitEvent(a->rs, a->ev_rec[0], 0));
+        LSGB_TRY(record(nseg - 1, 0, a->rs));
+        LSGB_CUDA(cudaEventRecord(a->ev_rec[0], a->rs));
+    }
+    // the current adjoint field lives in one of the four buffers
+    void* L = a->lam[0];
+    int cur = 0;
+    for (int seg = nseg - 1; seg >= 0; --seg) {
+        if (two) {
+            LSGB_CUDA(cudaStreamWaitEvent(s->st, a->ev_rec[cur], 0));
+            if (seg > 0) {
+                if (seg + 1 < nseg) LSGB_CUDA(cudaStreamWaitEvent(a->rs, a->ev_rev[cur ^ 1], 0));
+                LSGB_TRY(record(seg - 1, cur ^ 1, a->rs));
+                LSGB_CUDA(cudaEventRecord(a->ev_rec[cur ^ 1], a->rs));
+            }
+        } else {
+            LSGB_TRY(record(seg, 0, s->st));
+        }
+        const int t0 = a->step0 + seg * a->ckpt, t1 = std::min(t0 + a->ckpt, a->step0 + a->n_steps);
+        int slots = 0;
+        const std::vector<TapeStep> plan = tape_plan(s->p, t0, t1, &slots);
+        a->tape = a->tape_buf[cur];
         for (int q = (int)plan.size() - 1; q >= 0; --q) {
             if (s->prec == LSGB_PREC_F64) LSGB_TRY(adj_reverse_step<double>(a, plan[q], &L));
             else LSGB_TRY(adj_reverse_step<float>(a, plan[q], &L));
+        }
+        if (two) {
+            LSGB_CUDA(cudaEventRecord(a->ev_rev[cur], s->st));
+            cur ^= 1;
         }
     }
     // keep dL/dG_0 in lam[0]
