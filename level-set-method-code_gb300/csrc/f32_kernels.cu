@@ -163,9 +163,19 @@ __device__ __forceinline__ float reinit_cell_f32(float phi, float ph0, const flo
     // floats is never rounded to zero in FP64, so comparing signs in FP32
     // decides it identically; only flagged cells go on to FP64 arithmetic.
     flag = 0;
+    // no crossing where phi0 and all its neighbours lie strictly on one side
+    // (most cells): the per-neighbour tests below would all fail there
+    float lo = p0[0], hi = p0[0];
 #pragma unroll
-    for (int q = 0; q < 2 * DIM; ++q)
-        if ((ph0 < 0.0f && p0[q] > 0.0f) || (ph0 > 0.0f && p0[q] < 0.0f)) flag |= 1 << q;
+    for (int q = 1; q < 2 * DIM; ++q) {
+        lo = fminf(lo, p0[q]);
+        hi = fmaxf(hi, p0[q]);
+    }
+    if (!((ph0 > 0.0f && lo > 0.0f) || (ph0 < 0.0f && hi < 0.0f))) {
+#pragma unroll
+        for (int q = 0; q < 2 * DIM; ++q)
+            if ((ph0 < 0.0f && p0[q] > 0.0f) || (ph0 > 0.0f && p0[q] < 0.0f)) flag |= 1 << q;
+    }
     bool stable = flag != 0 && (phi > 0.0f) == (ph0 > 0.0f);
 #pragma unroll
     for (int q = 0; q < 2 * DIM; ++q)

@@ -558,12 +558,9 @@ cudaError_t launch_one(const StageArgs& a, const Coef& c, const TmaMaps& tm, int
     const dim3 grid((a.g.nx + TX - 1) / TX, (a.g.ny + BY - 1) / BY, (a.g.nz + c.zc - 1) / c.zc);
     const size_t dyn = (size_t)NSTAGE * NFIELD * BFTILE * sizeof(float);
     auto kern = stage3d_f32_col2<STAGE, TMA, IDX>;
-    static bool attr_set = false;  // per instantiation
-    if (!attr_set) {
-        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
-        if (e != cudaSuccess) return e;
-        attr_set = true;
-    }
+    // once per instantiation (thread-safe initialisation of a local static)
+    static const cudaError_t attr = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+    if (attr != cudaSuccess) return attr;
     kern<<<grid, block, dyn, st>>>(a.g, (const float*)a.Gin, (const float*)a.Gn, (float*)a.Gout,
                                     (const float*)a.u, (const float*)a.v, (const float*)a.w,
                                     (const float*)a.sl, c, tm, err, a.sl != nullptr);
