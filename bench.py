@@ -298,7 +298,7 @@ def measure_batched(torch, lsgb, syn, steps: int, dist: Dist):
     with CUDA events on the batch stream."""
     wls = syn.config4()
     cells = 0
-    with lsgb.Batch("f32", lanes=8) as b:
+    with lsgb.Batch("f32", lanes=16) as b:
         for wl in wls:
             n = wl.n[0]
             p = lsgb.params(wl.dim, n, n, n, s_l=wl.s_l, enable_reinit=True, reinit_interval=RK_PER_BENCH_STEP,

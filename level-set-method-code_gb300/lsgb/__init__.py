@@ -390,7 +390,7 @@ class _Borrowed(Solver):
 class Batch:
     """Many independent instances advanced together (lsgb_batch_*)."""
 
-    def __init__(self, precision: str = "f32", lanes: int = 8):
+    def __init__(self, precision: str = "f32", lanes: int = 16):
         self._h = C.c_void_p()
         prec = {"f64": PREC_F64, "f32": PREC_F32}[precision]
         _check(lib().lsgb_batch_create(prec, int(lanes), C.byref(self._h)))
