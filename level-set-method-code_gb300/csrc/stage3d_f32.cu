@@ -384,9 +384,8 @@ stage3d_f32_col2(Geo g, const float* __restrict__ Gin, const float* __restrict__
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();  // zoff table and barriers ready
-    int issued = 0;  // iterations whose copies thread 0 has issued
     if (TMA && t == 0 && !c.drop)
-        for (; issued < NSTAGE - 1 && issued < niter; ++issued) issue(issued, issued);
+        for (int it = 0; it < NSTAGE - 1 && it < niter; ++it) issue(it, it);
     if (!TMA)
         for (int it = 0; it < NSTAGE - 1; ++it) {
             if (it < niter) fetch(it, it);
@@ -429,7 +428,6 @@ stage3d_f32_col2(Geo g, const float* __restrict__ Gin, const float* __restrict__
         if (TMA && t == 0 && !c.drop && it + NSTAGE - 1 < niter) {
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             issue(it + NSTAGE - 1, cs == 0 ? NSTAGE - 1 : cs - 1);
-            issued = it + NSTAGE;
         }
         if (!TMA) {
             if (it + NSTAGE - 1 < niter) fetch(it + NSTAGE - 1, cs == 0 ? NSTAGE - 1 : cs - 1);
@@ -485,6 +483,7 @@ stage3d_f32_col2(Geo g, const float* __restrict__ Gin, const float* __restrict__
                 // land, and leave
                 if (t == 0) {
                     atomicExch(err, 1);
+                    const int issued = c.drop ? 0 : min(niter, it + NSTAGE);  // iterations whose copies went out
                     for (int j = it; j < issued; ++j) mbar_wait(&mbar[j % NSTAGE], (uint32_t)((j / NSTAGE) & 1));
                 }
                 return;
