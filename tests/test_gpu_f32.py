@@ -7,7 +7,8 @@ on every run):
     front, <= 1e-3 * dx (the north-star bound on the zero-level-set error);
   * rough random fields (every upwind branch, non-smooth WENO weights):
     L_inf <= 5e-5 after 4 steps -- a kernel-logic check on ragged tiles,
-    z-chunk seams, the 3-cell minimum and zero-gradient axes.
+    z-chunk seams, the 3-cell minimum and zero-gradient axes (y and z, or all
+    three, with the bulk-tensor staging at nx = 36).
 """
 import numpy as np
 import pytest
@@ -44,7 +45,7 @@ def test_f32_smooth_fields_vs_f64(cuda, lsgb_mod, n):
 
 
 @pytest.mark.parametrize("n,bc", [((37, 19, 70), 0), ((33, 9, 5), 0), ((3, 3, 3), 0),
-                                  ((35, 11, 66), 1), ((64, 16, 128), 0)])
+                                  ((35, 11, 66), 1), ((64, 16, 128), 0), ((36, 21, 33), 2)])
 def test_f32_rough_fields_vs_f64(cuda, lsgb_mod, n, bc):
     rng = np.random.default_rng(sum(n) + bc)
     shape = tuple(q + 6 for q in reversed(n))
@@ -52,8 +53,9 @@ def test_f32_rough_fields_vs_f64(cuda, lsgb_mod, n, bc):
     G = np.sqrt((xx - .5) ** 2 + (yy - .45) ** 2 + (zz - .55) ** 2) - 0.3 + 0.02 * rng.standard_normal(shape)
     u, v, w = (rng.standard_normal(shape) for _ in range(3))
     sl = np.abs(rng.standard_normal(shape)) * 0.2
+    # bc: 0 periodic, 1 zero-gradient in y and z, 2 zero-gradient on every axis
     p = lsgb_mod.params(3, *n, s_l=0.15, dt=2e-4, enable_reinit=True, reinit_interval=2,
-                        reinit_iterations=2, bc_y=bc, bc_z=bc)
+                        reinit_iterations=2, bc_x=int(bc == 2), bc_y=int(bc > 0), bc_z=int(bc > 0))
     for field in (None, sl):
         g64 = run(lsgb_mod, p, "f64", 4, G, u, v, w, field)
         g32 = run(lsgb_mod, p, "f32", 4, G, u, v, w, field)
