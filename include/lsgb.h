@@ -411,6 +411,12 @@ LSGB_API int lsgb_sample_rhs(int nx, int ny, const double* G, const double* u, c
 LSGB_API int lsgb_sample_rk3_step(int nx, int ny, double* G, const double* u, const double* v, double dx,
                                   double dy, double dt, double S_L, const double* G_initial, double* work,
                                   void* stream);
+/* compute_first_order_upwind (sample/first_order_upwind.hpp:4-12,
+ * first_order_upwind.cpp:6-69): the first-order upwind step, in place on G,
+ * over the reference's range j = 3 .. ny+3, i = 3 .. nx+3 (one ghost row and
+ * column past the interior on the high side); work = 1 array. */
+LSGB_API int lsgb_sample_first_order_upwind(int nx, int ny, double* G, const double* u, const double* v, double dx,
+                                            double dy, double dt, double S_L, double* work, void* stream);
 /* Field2D::apply_periodic / apply_anchored_bc (sample/field.hpp:15-18,
  * field.cpp:16-63). */
 LSGB_API int lsgb_sample_apply_periodic(int nx, int ny, double* G, void* stream);

@@ -10,6 +10,8 @@
 //   Field2D::reinitialize     field.hpp:21      Field2D::reinitialize
 //   compute_geqn_rhs          weno5_rk3.hpp:10  lsgb::sample::compute_geqn_rhs (Field2D arguments)
 //   RK3_step                  weno5_rk3.hpp:20  lsgb::sample::RK3_step (same signature)
+//   compute_first_order_upwind first_order_upwind.hpp:4
+//                                               lsgb::sample::compute_first_order_upwind (Field2D arguments)
 //   save_G_to_bin             main.cpp:34       lsgb::sample::save_G_to_bin
 //   load_field_from_bin       main.cpp:16       lsgb::sample::load_field_from_bin
 //
@@ -97,6 +99,11 @@ inline void RK3_step(Field2D& G_field, const Field2D& u_field, const Field2D& v_
                      double dt, double S_L, const Field2D& G_initial) {
     check(lsgb_sample_rk3_step(G_field.nx, G_field.ny, G_field.dev, u_field.dev, v_field.dev, dx, dy, dt, S_L,
                                G_initial.dev, nullptr, nullptr));
+}
+
+inline void compute_first_order_upwind(Field2D& G, const Field2D& u, const Field2D& v, double dx, double dy,
+                                       double dt, double S_L) {
+    check(lsgb_sample_first_order_upwind(G.nx, G.ny, G.dev, u.dev, v.dev, dx, dy, dt, S_L, nullptr, nullptr));
 }
 
 // Interior rows only, each nx doubles, no header (main.cpp:34-51): the

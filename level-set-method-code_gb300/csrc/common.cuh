@@ -250,6 +250,8 @@ cudaError_t sample_launch_periodic(const SampleArgs& a, double* G, cudaStream_t 
 cudaError_t sample_launch_reinit_step(const SampleArgs& a, const double* phi, double* out, double dtau,
                                       cudaStream_t st);
 cudaError_t sample_launch_zero_ghosts(const SampleArgs& a, double* G, cudaStream_t st);
+// compute_first_order_upwind, in place on G through tmp (one array)
+cudaError_t sample_launch_first_order_upwind(const SampleArgs& a, double* G, double* tmp, cudaStream_t st);
 
 // The FP64 array part of the reference's binary dump (dump.cu): from a
 // compact state (x/z ghosts as the boundary fill leaves them, y ghosts =

@@ -110,6 +110,25 @@ extern "C" int lsgb_sample_rk3_step(int nx, int ny, double* G, const double* u, 
     return rk3_sequence(a, G, w.p, w.p + n, false, st);
 }
 
+extern "C" int lsgb_sample_first_order_upwind(int nx, int ny, double* G, const double* u, const double* v,
+                                              double dx, double dy, double dt, double S_L, double* work,
+                                              void* stream) {
+    LSGB_TRY(check_grid(nx, ny));
+    LSGB_TRY(check_spacing(dx, dy));
+    if (!std::isfinite(dt) || !std::isfinite(S_L)) return fail(LSGB_ERR_INVALID, "dt and S_L must be finite");
+    LSGB_TRY(check_dev(G, "G"));
+    LSGB_TRY(check_dev(u, "u"));
+    LSGB_TRY(check_dev(v, "v"));
+    cudaStream_t st = (cudaStream_t)stream;
+    Work w(st);
+    LSGB_TRY(w.get(work, field_bytes(nx, ny)));
+    SampleArgs a = sample_args(nx, ny, 1, dx, dy, dt, S_L);
+    a.u = u;
+    a.v = v;
+    LSGB_CUDA(sample_launch_first_order_upwind(a, G, w.p, st));
+    return LSGB_OK;
+}
+
 extern "C" int lsgb_sample_apply_periodic(int nx, int ny, double* G, void* stream) {
     LSGB_TRY(check_grid(nx, ny));
     LSGB_TRY(check_dev(G, "G"));

@@ -282,6 +282,46 @@ __global__ void __launch_bounds__(256) sample_reinit_kernel(S2 s, const double* 
     out_[q * s.stride + s.at(j, i)] = c + dtau * rhs;
 }
 
+// compute_first_order_upwind (sample/first_order_upwind.cpp:6-69): the
+// first-order upwind step from G into out over j = 3 .. ny+3, i = 3 .. nx+3
+// (the reference's inclusive bounds on the ghosted sizes, one ghost row and
+// column past the interior on the high side); the copy kernel below writes
+// the same range back into G (the reference's G_new -> G loop).
+__global__ void __launch_bounds__(256) sample_fou_kernel(S2 s, const double* __restrict__ G,
+                                                         const double* __restrict__ u,
+                                                         const double* __restrict__ v, double* __restrict__ out,
+                                                         double dx, double dy, double dt, double S_L) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 3;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y + 3;
+    if (i > s.nx + 3 || j > s.ny + 3) return;
+    const double EPS = 1e-10;
+    const double c = G[s.at(j, i)];
+    const double Gx_mns = (c - G[s.at(j, i - 1)]) / dx;
+    const double Gx_pls = (G[s.at(j, i + 1)] - c) / dx;
+    const double Gy_mns = (c - G[s.at(j - 1, i)]) / dy;
+    const double Gy_pls = (G[s.at(j + 1, i)] - c) / dy;
+    const double dG_dx = 0.5 * (Gx_mns + Gx_pls);
+    const double dG_dy = 0.5 * (Gy_mns + Gy_pls);
+    const double mag_sq = dG_dx * dG_dx + dG_dy * dG_dy;
+    double u_first = u[s.at(j, i)], v_first = v[s.at(j, i)];
+    if (mag_sq > EPS * EPS) {
+        const double mag = sqrt(mag_sq);
+        u_first = u_first - S_L * dG_dx / mag;
+        v_first = v_first - S_L * dG_dy / mag;
+    }
+    const double a_pls = smax(u_first, 0.0), a_mns = smin(u_first, 0.0);
+    const double b_pls = smax(v_first, 0.0), b_mns = smin(v_first, 0.0);
+    out[s.at(j, i)] = c - dt * (a_pls * Gx_mns + a_mns * Gx_pls + b_pls * Gy_mns + b_mns * Gy_pls);
+}
+
+__global__ void __launch_bounds__(256) sample_fou_copy_kernel(S2 s, const double* __restrict__ src,
+                                                              double* __restrict__ dst) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 3;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y + 3;
+    if (i > s.nx + 3 || j > s.ny + 3) return;
+    dst[s.at(j, i)] = src[s.at(j, i)];
+}
+
 __global__ void zero_ghosts_kernel(S2 s, double* G_) {
     const long long total = s.nxT * (s.ny + 6);
     double* G = G_ + blockIdx.y * s.stride;
@@ -359,6 +399,15 @@ cudaError_t sample_launch_reinit_step(const SampleArgs& a, const double* phi, do
     const dim3 b(32, 8, 1), gr = interior_grid(s, a.n_inst, b);
     sample_reinit_kernel<<<gr, b, 0, st>>>(s, phi, out, a.init, a.init_stride, a.dx, a.dy, dtau);
     count_launches(1);
+    return cudaGetLastError();
+}
+
+cudaError_t sample_launch_first_order_upwind(const SampleArgs& a, double* G, double* tmp, cudaStream_t st) {
+    const S2 s = make_s2(a.nx, a.ny);
+    const dim3 b(32, 8, 1), gr((s.nx + 1 + b.x - 1) / b.x, (s.ny + 1 + b.y - 1) / b.y, 1);
+    sample_fou_kernel<<<gr, b, 0, st>>>(s, G, a.u, a.v, tmp, a.dx, a.dy, a.dt, a.S_L);
+    sample_fou_copy_kernel<<<gr, b, 0, st>>>(s, tmp, G);
+    count_launches(2);
     return cudaGetLastError();
 }
 

@@ -83,6 +83,14 @@ def rk3_step(G, u, v, dx: float, dy: float, dt: float, S_L: float, G_initial, st
     return G
 
 
+def first_order_upwind(G, u, v, dx: float, dy: float, dt: float, S_L: float, stream=None):
+    """compute_first_order_upwind, in place on G."""
+    nx, ny = _dims(G)
+    _check(lib().lsgb_sample_first_order_upwind(nx, ny, _p(G), _p(u), _p(v), C.c_double(dx), C.c_double(dy),
+                                                C.c_double(dt), C.c_double(S_L), None, _stream(stream)))
+    return G
+
+
 def apply_periodic(G, stream=None):
     nx, ny = _dims(G)
     _check(lib().lsgb_sample_apply_periodic(nx, ny, _p(G), _stream(stream)))

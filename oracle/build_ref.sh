@@ -3,8 +3,8 @@
 # (Local_code/level-set_MPI_{2D,3D}/include), unmodified, behind the
 # extern "C" drivers in this folder and the single-rank MPI stub; and
 # oracle/_ref/libref_sample.so: the sample surface's sources
-# (sample/field.cpp, sample/weno5_rk3.cpp) compiled in place behind
-# ref_sample_driver.cpp.
+# (sample/field.cpp, sample/weno5_rk3.cpp, sample/first_order_upwind.cpp)
+# compiled in place behind ref_sample_driver.cpp.
 # Test infrastructure only.  Nothing is copied out of the reference tree: the
 # headers and sources are read in place, and only the shared libraries are
 # written (into oracle/_ref/, which git ignores).
@@ -28,6 +28,7 @@ FLAGS="-O2 -std=c++14 -fPIC -shared -ffp-contract=off -fno-fast-math -w"
 "$CXX" $FLAGS -I"$here/mpi_stub" -I"$ref_root/Local_code/level-set_MPI_2D/include" \
     "$here/ref_driver2d.cpp" -o "$out/libref2d.so" &
 "$CXX" $FLAGS -fopenmp -std=c++17 -I"$ref_root/sample" "$here/ref_sample_driver.cpp" \
-    "$ref_root/sample/field.cpp" "$ref_root/sample/weno5_rk3.cpp" -o "$out/libref_sample.so" &
+    "$ref_root/sample/field.cpp" "$ref_root/sample/weno5_rk3.cpp" "$ref_root/sample/first_order_upwind.cpp" \
+    -o "$out/libref_sample.so" &
 wait %1 && wait %2 && wait %3
 echo "built $out/libref3d.so $out/libref2d.so $out/libref_sample.so"

@@ -188,6 +188,45 @@ void orcs_rk3_step(int nx, int ny, double* G, const double* u, const double* v, 
     rk3_any(nx, ny, G, u, v, 0.0, 0.0, dx, dy, dt, S_L, init);
 }
 
+/* compute_first_order_upwind, sample/first_order_upwind.cpp:6-69: the
+ * first-order upwind G-equation step (Jacobi, in place on G).  The loops run
+ * over j = 3 .. ny+3 and i = 3 .. nx+3 inclusive (the reference's bounds
+ * `<= ny-3` / `<= nx-3` on the ghosted sizes), which includes the first
+ * ghost row and column on the high side. */
+void orcs_first_order_upwind(int nx, int ny, double* G, const double* u, const double* v, double dx, double dy,
+                             double dt, double S_L) {
+    const int nxT = nx + 6, nyT = ny + 6;
+    const size_t n = (size_t)nxT * nyT;
+    const double EPS = 1e-10;
+    double* Gn = malloc(n * sizeof(double));
+    memcpy(Gn, G, n * sizeof(double));
+    for (int j = 3; j <= nyT - 3; ++j)
+        for (int i = 3; i <= nxT - 3; ++i) {
+            const double Gx_mns = (AT(G, j, i) - AT(G, j, i - 1)) / dx;
+            const double Gx_pls = (AT(G, j, i + 1) - AT(G, j, i)) / dx;
+            const double Gy_mns = (AT(G, j, i) - AT(G, j - 1, i)) / dy;
+            const double Gy_pls = (AT(G, j + 1, i) - AT(G, j, i)) / dy;
+            const double dG_dx = 0.5 * (Gx_mns + Gx_pls);
+            const double dG_dy = 0.5 * (Gy_mns + Gy_pls);
+            const double mag_sq = dG_dx * dG_dx + dG_dy * dG_dy;
+            double u_first, v_first;
+            if (mag_sq > EPS * EPS) {
+                const double mag = sqrt(mag_sq);
+                u_first = AT(u, j, i) - S_L * dG_dx / mag;
+                v_first = AT(v, j, i) - S_L * dG_dy / mag;
+            } else {
+                u_first = AT(u, j, i);
+                v_first = AT(v, j, i);
+            }
+            const double a_pls = smax(u_first, 0.0), a_mns = smin(u_first, 0.0);
+            const double b_pls = smax(v_first, 0.0), b_mns = smin(v_first, 0.0);
+            AT(Gn, j, i) = AT(G, j, i) - dt * (a_pls * Gx_mns + a_mns * Gx_pls + b_pls * Gy_mns + b_mns * Gy_pls);
+        }
+    for (int j = 3; j <= nyT - 3; ++j)
+        for (int i = 3; i <= nxT - 3; ++i) AT(G, j, i) = AT(Gn, j, i);
+    free(Gn);
+}
+
 /* Field2D::reinitialize, sample/field.cpp:66-129 */
 void orcs_reinitialize(int nx, int ny, double* G, const double* init, double dx, double dy, int iters) {
     const int nxT = nx + 6, nyT = ny + 6;

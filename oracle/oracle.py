@@ -338,6 +338,13 @@ class SampleOracle:
                         C.c_double(S_L))
         return out
 
+    def first_order_upwind(self, G, u, v, dx, dy, dt, S_L):
+        nx, ny = self._dims(G)
+        out = G.copy()
+        self._fn("first_order_upwind")(nx, ny, _ptr(out), _ptr(u), _ptr(v), C.c_double(dx), C.c_double(dy),
+                                       C.c_double(dt), C.c_double(S_L))
+        return out
+
     def rk3_step(self, G, u, v, dx, dy, dt, S_L, G_initial):
         nx, ny = self._dims(G)
         out = G.copy()

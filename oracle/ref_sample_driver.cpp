@@ -1,5 +1,5 @@
 // extern "C" driver around the reference's sample surface (sample/field.cpp,
-// sample/weno5_rk3.cpp), compiled from those files in place by build_ref.sh
+// sample/weno5_rk3.cpp, sample/first_order_upwind.cpp), compiled from those files in place by build_ref.sh
 // into oracle/_ref/libref_sample.so.  Test infrastructure only.
 //
 // Arrays cross the boundary as flat row-major [ny+6][nx+6] doubles, the
@@ -10,6 +10,7 @@
 #include <vector>
 
 #include "field.hpp"
+#include "first_order_upwind.hpp"
 #include "weno5_rk3.hpp"
 
 namespace {
@@ -48,6 +49,17 @@ void refs_rk3_step(int nx, int ny, double* G, const double* u, const double* v, 
     to_field(vf, v);
     to_field(g0, G_initial);
     RK3_step(g, uf, vf, dx, dy, dt, S_L, g0);
+    from_field(g, G);
+}
+
+// compute_first_order_upwind (sample/first_order_upwind.cpp:6-69), in place on G
+void refs_first_order_upwind(int nx, int ny, double* G, const double* u, const double* v, double dx, double dy,
+                             double dt, double S_L) {
+    Field2D g(nx, ny), uf(nx, ny), vf(nx, ny);
+    to_field(g, G);
+    to_field(uf, u);
+    to_field(vf, v);
+    compute_first_order_upwind(g.data, uf.data, vf.data, dx, dy, dt, S_L);
     from_field(g, G);
 }
 

@@ -38,6 +38,32 @@ def small_inputs(pb: Problem, seed: int):
     return [np.ascontiguousarray(a) for a in (G, *vel)]
 
 
+def sample_fixtures():
+    """Sample surface (sample/field.cpp, sample/weno5_rk3.cpp,
+    sample/first_order_upwind.cpp): a Bunsen cone with noise, random velocity
+    fields, the config.hpp physics."""
+    sref = SampleOracle("ref")
+    for tag, (nx, ny) in (("24x20", (24, 20)), ("3x3", (3, 3))):
+        rng = np.random.default_rng(syn.seed_for(92, nx))
+        G0 = smp.bunsen(nx, ny)
+        dx, dy = smp.spacing(nx, ny)
+        G = np.ascontiguousarray(G0 + 2e-4 * rng.standard_normal(G0.shape))
+        u = np.ascontiguousarray(0.3 * rng.standard_normal(G0.shape))
+        v = np.ascontiguousarray(0.8 + 0.3 * rng.standard_normal(G0.shape))
+        dt = 1e-4
+        run_f0, t_f0 = sref.run(G, G0, 25, dx, dy, dt, smp.SL, smp.U0, smp.V0, smp.EPS_U, smp.EPS_V, 0)
+        run_f50, t_f50 = sref.run(G, G0, 25, dx, dy, dt, smp.SL, smp.U0, smp.V0, smp.EPS_U, smp.EPS_V, 50)
+        np.savez_compressed(os.path.join(HERE, f"golden_sample_{tag}.npz"),
+                            G=G, G0=G0, u=u, v=v, dx=dx, dy=dy, dt=dt, S_L=smp.SL,
+                            rhs=sref.rhs(G, u, v, dx, dy, smp.SL),
+                            rk3=sref.rk3_step(G, u, v, dx, dy, dt, smp.SL, G0),
+                            periodic=sref.apply_periodic(G), anchored=sref.apply_anchored_bc(G, G0),
+                            reinit10=sref.reinitialize(G, G0, dx, dy, 10),
+                            fou=sref.first_order_upwind(G, u, v, dx, dy, dt, smp.SL),
+                            run25_f0=run_f0, t25_f0=t_f0, run25_f50=run_f50, t25_f50=t_f50)
+
+
+
 def main():
     if not build_ref():
         sys.exit("reference tree not found")
@@ -85,26 +111,7 @@ def main():
                         area0=ref.volume(pb, G), area_final=ref.volume(pb, fin),
                         l2_final=ref.l2(pb, fin, G))
 
-    # sample surface (sample/field.cpp, sample/weno5_rk3.cpp): a Bunsen cone
-    # with noise, random velocity fields, the config.hpp physics
-    sref = SampleOracle("ref")
-    for tag, (nx, ny) in (("24x20", (24, 20)), ("3x3", (3, 3))):
-        rng = np.random.default_rng(syn.seed_for(92, nx))
-        G0 = smp.bunsen(nx, ny)
-        dx, dy = smp.spacing(nx, ny)
-        G = np.ascontiguousarray(G0 + 2e-4 * rng.standard_normal(G0.shape))
-        u = np.ascontiguousarray(0.3 * rng.standard_normal(G0.shape))
-        v = np.ascontiguousarray(0.8 + 0.3 * rng.standard_normal(G0.shape))
-        dt = 1e-4
-        run_f0, t_f0 = sref.run(G, G0, 25, dx, dy, dt, smp.SL, smp.U0, smp.V0, smp.EPS_U, smp.EPS_V, 0)
-        run_f50, t_f50 = sref.run(G, G0, 25, dx, dy, dt, smp.SL, smp.U0, smp.V0, smp.EPS_U, smp.EPS_V, 50)
-        np.savez_compressed(os.path.join(HERE, f"golden_sample_{tag}.npz"),
-                            G=G, G0=G0, u=u, v=v, dx=dx, dy=dy, dt=dt, S_L=smp.SL,
-                            rhs=sref.rhs(G, u, v, dx, dy, smp.SL),
-                            rk3=sref.rk3_step(G, u, v, dx, dy, dt, smp.SL, G0),
-                            periodic=sref.apply_periodic(G), anchored=sref.apply_anchored_bc(G, G0),
-                            reinit10=sref.reinitialize(G, G0, dx, dy, 10),
-                            run25_f0=run_f0, t25_f0=t_f0, run25_f50=run_f50, t25_f50=t_f50)
+    sample_fixtures()
 
     # the reference's default 3D case end to end (its committed log pins it)
     l2, v0, v1, steps = ref.deformation_test()
@@ -118,4 +125,7 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    if sys.argv[1:] == ["sample"]:
+        sample_fixtures()  # only the sample-surface fixtures
+    else:
+        main()

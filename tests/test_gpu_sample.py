@@ -31,6 +31,7 @@ def test_sample_matches_golden(cuda, lsgb_mod, tag):
     assert np.array_equal(H(smp.apply_periodic(T(G))), g["periodic"])
     assert np.array_equal(H(smp.apply_anchored_bc(T(G), T(G0))), g["anchored"])
     assert np.array_equal(H(smp.reinitialize(T(G), T(G0), dx, dy, 10)), g["reinit10"])
+    assert np.array_equal(H(smp.first_order_upwind(T(G), T(u), T(v), dx, dy, dt, sl)), g["fou"])
     Gd = T(G)
     t = smp.run(Gd, T(G0), 25, dx, dy, [0], dt=dt, S_L=sl)
     assert np.array_equal(H(Gd), g["run25_f0"]) and t[0] == float(g["t25_f0"])
@@ -58,6 +59,15 @@ def test_sample_matches_port(cuda, lsgb_mod, port, nx, ny):
     for iters in (1, 4):
         assert np.array_equal(H(smp.reinitialize(T(G), T(G0), dx, dy, iters)),
                               so.reinitialize(G, G0, dx, dy, iters))
+    # first-order upwind scheme: three steps in place, and a flat field (the |grad G| = 0 gate)
+    Gd, ref = T(G), G.copy()
+    for _ in range(3):
+        smp.first_order_upwind(Gd, T(u), T(v), dx, dy, dt, 0.4)
+        ref = so.first_order_upwind(ref, u, v, dx, dy, dt, 0.4)
+    assert np.array_equal(H(Gd), ref)
+    flat = np.ascontiguousarray(np.full_like(G, 0.25))
+    assert np.array_equal(H(smp.first_order_upwind(T(flat), T(u), T(v), dx, dy, dt, 0.4)),
+                          so.first_order_upwind(flat, u, v, dx, dy, dt, 0.4))
 
 
 def test_frequency_sweep_matches_port_per_instance(cuda, lsgb_mod):

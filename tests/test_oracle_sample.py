@@ -32,6 +32,7 @@ def test_port_matches_golden(sport, tag):
     assert np.array_equal(sport.apply_periodic(G), g["periodic"])
     assert np.array_equal(sport.apply_anchored_bc(G, G0), g["anchored"])
     assert np.array_equal(sport.reinitialize(G, G0, dx, dy, 10), g["reinit10"])
+    assert np.array_equal(sport.first_order_upwind(G, u, v, dx, dy, dt, sl), g["fou"])
     out, t = sport.run(G, G0, 25, dx, dy, dt, sl, 0.0, 0.8, 0.05, 0.05, 0)
     assert np.array_equal(out, g["run25_f0"]) and t == float(g["t25_f0"])
     out, t = sport.run(G, G0, 25, dx, dy, dt, sl, 0.0, 0.8, 0.05, 0.05, 50)
@@ -52,7 +53,8 @@ def test_port_matches_reference(sport, nx, ny):
     v = np.ascontiguousarray(0.8 + 0.2 * rng.standard_normal(G0.shape))
     for name, args in [("rhs", (G, u, v, dx, dy, 0.4)), ("rk3_step", (G, u, v, dx, dy, 2e-4, 0.4, G0)),
                        ("apply_periodic", (G,)), ("apply_anchored_bc", (G, G0)),
-                       ("reinitialize", (G, G0, dx, dy, 7))]:
+                       ("reinitialize", (G, G0, dx, dy, 7)),
+                       ("first_order_upwind", (G, u, v, dx, dy, 2e-4, 0.4))]:
         assert np.array_equal(getattr(sport, name)(*args), getattr(ref, name)(*args)), name
     a, ta = sport.run(G, G0, 12, dx, dy, 2e-4, 0.4, 0.0, 0.8, 0.05, 0.05, 120)
     b, tb = ref.run(G, G0, 12, dx, dy, 2e-4, 0.4, 0.0, 0.8, 0.05, 0.05, 120)
