@@ -248,3 +248,40 @@ def config4(n2d: int = 48, n3d: int = 48, n_vel: int = 8):
         out.append(Workload(dim=dim, n=(n,) * dim, s_l=s_l, center=(float(c[0]), float(c[1]), float(c[2]) if dim == 3 else 0.0),
                             r0=r0, vel_k=ks, vel_c=cs, vel_phase=ph))
     return out
+
+
+# ---- the reference's 2D known-answer case -----------------------------------
+ZALESAK_T_FINAL = 6.283185  # T_FINAL, Local_code/level-set_MPI_2D/include/config.h:65
+
+
+def zalesak_fields(n: int):
+    """(G0, u, v) of the reference's Zalesak case on an n x n grid of [0,1]^2
+    (dx = 1/(n-1)), ghosted (n+6, n+6) float64 arrays with the same rounded
+    operations as initZalesakTestCase (Local_code/level-set_MPI_2D/include/
+    initial_conditions.h:91-125, 209-227, 260-272; coordinates config.h:281-294):
+    slotted disk (0.5, 0.75), r = 0.15, slot 0.05 x 0.25, rotated about
+    (0.5, 0.5) at omega = 2 pi / T_FINAL.  Ghost values follow the same
+    formula (the solvers read only interior cells of the inputs).  Returns
+    also dx and the CFL time step (0.2 dx / |u_const|, u_const = 1)."""
+    dx = (1.0 - 0.0) / (n - 1)
+    idx = (np.arange(n + 6) - 3).astype(np.float64)
+    x1 = 0.0 + idx * dx
+    y1 = 0.0 + idx * dx
+    y, x = np.meshgrid(y1, x1, indexing="ij")
+    cx, cy, r, sw, sln = 0.5, 0.75, 0.15, 0.05, 0.25
+    ddx = x - cx
+    ddy = y - cy
+    dist_disk = np.sqrt(ddx * ddx + ddy * ddy) - r
+    half = sw / 2.0
+    bottom = cy - r
+    top = bottom + sln
+    sdx = np.abs(x - cx) - half
+    sdy = np.fmax(bottom - y, y - top)
+    dist_slot = np.where((sdx < 0.0) & (sdy < 0.0), np.fmax(sdx, sdy),
+                         np.where(sdx < 0.0, sdy, np.where(sdy < 0.0, sdx, np.sqrt(sdx * sdx + sdy * sdy))))
+    G = np.fmax(dist_disk, -dist_slot)
+    omega = 2.0 * math.pi / ZALESAK_T_FINAL
+    u = -omega * (y - 0.5)
+    v = omega * (x - 0.5)
+    dt = 0.2 * min(dx, dx) / max(abs(1.0) + abs(0.0) + 0.0, 1e-10)
+    return np.ascontiguousarray(G), np.ascontiguousarray(u), np.ascontiguousarray(v), dx, dt

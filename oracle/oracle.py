@@ -301,6 +301,18 @@ class Oracle:
         return l2.value, v0.value, v1.value, st.value
 
 
+    def zalesak_test(self, n: int):
+        """The reference's 2D Zalesak known-answer run on n x n (ref only).
+        Returns (G0, u, v, G_final) as ghosted (n+6, n+6) arrays and
+        (l2, area0, area1, steps)."""
+        assert self.kind == "ref"
+        shape = (n + 6, n + 6)
+        G0, u, v, Gf = (np.zeros(shape) for _ in range(4))
+        out = np.zeros(4)
+        self._l2.ref2d_zalesak(n, _ptr(G0), _ptr(u), _ptr(v), _ptr(Gf), _ptr(out))
+        return G0, u, v, Gf, (float(out[0]), float(out[1]), float(out[2]), int(out[3]))
+
+
 class SampleOracle:
     """The sample surface (sample/field.cpp, sample/weno5_rk3.cpp): 2D
     Field2D arrays as float64 numpy arrays of shape (ny+6, nx+6).

@@ -122,6 +122,58 @@ void ref2d_run(const orc_params* p, int n_steps, double* G, const double* u_in,
 }
 
 
+/* The reference's 2D known-answer case (src/main.cpp:198-371 run with
+ * -t zalesak; logs in Local_code/level-set_MPI_2D/log/<n>x<n>.log): Zalesak's
+ * slotted disk rotated once about (0.5, 0.5) on an n x n grid of [0,1]^2
+ * (dx = 1/(n-1)), periodic X, zero-gradient Y, S_L = 0, no reinit, dt from
+ * calculateTimeStep with u_const = 1 and the final-step clip.  Outputs: the
+ * ghosted initial G (after the boundary fill), u, v, the final G, and
+ * out = {L2 error, initial area, final area, steps}. */
+void ref2d_zalesak(int n, double* G0_out, double* u_out, double* v_out, double* G_final, double* out) {
+    SimParams s = initDefaultParams();
+    s.nx = n; s.ny = n;
+    s.nghost = 3;
+    s.nx_total = n + 6; s.ny_total = n + 6;
+    s.dx = (DOMAIN_X_MAX - DOMAIN_X_MIN) / (n - 1);
+    s.dy = (DOMAIN_Y_MAX - DOMAIN_Y_MIN) / (n - 1);
+    setupMPIDomainDecomposition(s, 0, 1);
+    s.s_l = S_L;
+    s.u_const = U_CONST;
+    s.v_const = V_CONST;
+    s.t_final = T_FINAL;
+    s.cfl = CFL;
+    s.enable_reinit = false;
+    s.dt = calculateTimeStep(s);
+    const size_t tot = (size_t)s.nx_total * s.local_ny_total;
+    std::vector<double> G(tot, 0.0), Gnew(tot, 0.0), G1(tot, 0.0), G2(tot, 0.0), Grhs(tot, 0.0), Gi(tot, 0.0),
+        u(tot, 0.0), v(tot, 0.0);
+    initZalesakTestCase(G.data(), u.data(), v.data(), s);
+    applyBoundaryConditions(G.data(), s);
+    applyVelocityBoundaryConditions(u.data(), v.data(), s);
+    copyInitialField(G.data(), Gi.data(), (int)tot);
+    const double area0 = computeInterfaceArea(G.data(), s);
+    if (G0_out) std::memcpy(G0_out, G.data(), sizeof(double) * tot);
+    if (u_out) std::memcpy(u_out, u.data(), sizeof(double) * tot);
+    if (v_out) std::memcpy(v_out, v.data(), sizeof(double) * tot);
+    double* pG = G.data();
+    double* pGn = Gnew.data();
+    double current_time = 0.0;
+    int step = 0;
+    const int max_steps = (int)(s.t_final / s.dt) + 100;
+    while (current_time < s.t_final && step < max_steps) {
+        if (current_time + s.dt > s.t_final) s.dt = s.t_final - current_time;
+        rk3TimeStep(pG, pGn, G1.data(), G2.data(), Grhs.data(), u.data(), v.data(), s);
+        double* t = pG; pG = pGn; pGn = t;
+        current_time += s.dt;
+        step++;
+    }
+    out[0] = computeL2Error(pG, Gi.data(), s);
+    out[1] = area0;
+    out[2] = computeInterfaceArea(pG, s);
+    out[3] = (double)step;
+    if (G_final) std::memcpy(G_final, pG, sizeof(double) * tot);
+}
+
 /* the reference's binary dump writer on a ghosted array (io.h) */
 int ref2d_save_binary(const orc_params* p, const double* G, const char* path) {
     SimParams s = to_sim(p);

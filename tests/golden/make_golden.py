@@ -64,6 +64,32 @@ def sample_fixtures():
 
 
 
+def zalesak_fixture(n: int = 201):
+    """The reference's 2D Zalesak known-answer run (src/main.cpp with -t zalesak,
+    log Local_code/level-set_MPI_2D/log/201x201.log), compiled without
+    contraction: SHA-256 of the interior of its initial and final G, and its
+    scalars at full precision, beside the logged ones."""
+    import hashlib
+    ref = Oracle("ref")
+    G0, u, v, Gf, (l2, a0, a1, steps) = ref.zalesak_test(n)
+    g0, un, vn, dx, dt = syn.zalesak_fields(n)
+    inner = (slice(3, -3), slice(3, -3))
+    for a, b, name in ((G0, g0, "G0"), (u, un, "u"), (v, vn, "v")):
+        assert np.array_equal(a[inner], b[inner]), f"numpy restatement of the Zalesak {name} differs"
+    sha = lambda a: hashlib.sha256(np.ascontiguousarray(a[inner]).tobytes()).hexdigest()
+    out = {"n": n, "dx": dx, "dt": dt, "t_final": syn.ZALESAK_T_FINAL, "steps": steps,
+           "G0_sha256": sha(G0), "G_final_sha256": sha(Gf), "l2": l2, "area_initial": a0, "area_final": a1,
+           "negative_cells_initial": int((G0[inner] < 0).sum()), "negative_cells_final": int((Gf[inner] < 0).sum()),
+           "log": {"source": "Local_code/level-set_MPI_2D/log/201x201.log", "l2": "8.576633e-02",
+                   "area_initial": "0.057850", "area_final": "0.058800", "steps": 6284},
+           "note": "the logged initial area is 4 cells smaller than this build's: the same sources built with "
+                   "fused multiply-add contraction (-mfma -ffp-contract=fast) print 0.057850 and the same final "
+                   "values, so the logged binary most likely contracted the coordinate or distance arithmetic; "
+                   "this fixture is the uncontracted build the FP64 path reproduces"}
+    with open(os.path.join(HERE, f"golden_zalesak_{n}.json"), "w") as f:
+        json.dump(out, f, indent=2)
+
+
 def main():
     if not build_ref():
         sys.exit("reference tree not found")
@@ -112,6 +138,7 @@ def main():
                         l2_final=ref.l2(pb, fin, G))
 
     sample_fixtures()
+    zalesak_fixture()
 
     # the reference's default 3D case end to end (its committed log pins it)
     l2, v0, v1, steps = ref.deformation_test()
@@ -127,5 +154,7 @@ def main():
 if __name__ == "__main__":
     if sys.argv[1:] == ["sample"]:
         sample_fixtures()  # only the sample-surface fixtures
+    elif sys.argv[1:] == ["zalesak"]:
+        zalesak_fixture()  # only the 2D known-answer run (about a minute of CPU)
     else:
         main()

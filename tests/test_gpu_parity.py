@@ -156,6 +156,39 @@ def test_deformation_64_matches_reference_log(cuda, lsgb_mod, port):
     assert l2 == pytest.approx(gold["l2"], rel=1e-9)
 
 
+def test_zalesak_201_matches_reference(cuda, lsgb_mod):
+    """The reference's 2D known answer (Zalesak's disk rotated once on 201^2,
+    periodic X, zero-gradient Y, 6284 steps with the final-step clip;
+    Local_code/level-set_MPI_2D/log/201x201.log) through the FP64 handle: the
+    final field equals the compiled reference's bit for bit (SHA-256 of the
+    interior) and the printed L2 and final area match the log."""
+    import hashlib
+    from lsgb import synthetic as syn
+    gold = json.load(open(os.path.join(GOLD, "golden_zalesak_201.json")))
+    n = gold["n"]
+    G0, u, v, dx, dt = syn.zalesak_fields(n)
+    p = lsgb_mod.params(2, n, n, 1, dx=dx, dy=dx, dt=dt, s_l=0.0, enable_reinit=False, bc_y=1)
+    with lsgb_mod.Solver(p, "f64") as s:
+        s.set_fields(G0, u, v)
+        t, steps = 0.0, 0
+        while t < syn.ZALESAK_T_FINAL:
+            if t + dt > syn.ZALESAK_T_FINAL:
+                dt = syn.ZALESAK_T_FINAL - t
+                s.set_dt(dt)
+            s.advance(1)
+            t += dt
+            steps += 1
+        G = s.get_G()
+        l2 = s.l2_error(G0)
+        area, count = s.volume()
+    sha = hashlib.sha256(np.ascontiguousarray(G[3:-3, 3:-3]).tobytes()).hexdigest()
+    assert steps == gold["steps"]
+    assert sha == gold["G_final_sha256"]
+    assert count == gold["negative_cells_final"]
+    assert f"{l2:.6e}" == gold["log"]["l2"] and f"{area:.6f}" == gold["log"]["area_final"]
+    assert l2 == pytest.approx(gold["l2"], rel=1e-12)
+
+
 # -- fresh seeded cases against the C restatement -----------------------------
 CASES = [
     (3, True, 0.2, 13, 11, 9), (3, True, 0.0, 3, 3, 3), (3, True, 0.25, 33, 5, 17),

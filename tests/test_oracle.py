@@ -86,6 +86,42 @@ def test_port_deformation_matches_reference_log():
     assert (l2.value, v0.value, v1.value) == (gold["l2"], gold["volume_initial"], gold["volume_final"])
 
 
+def zalesak_run(port, n=201):
+    """The reference's 2D Zalesak loop (Local_code/level-set_MPI_2D/src/main.cpp:314-335):
+    fixed dt, then the final step clipped to t_final."""
+    from lsgb import synthetic as syn
+    G0, u, v, dx, dt = syn.zalesak_fields(n)
+    t, full = 0.0, 0
+    while t < syn.ZALESAK_T_FINAL and t + dt <= syn.ZALESAK_T_FINAL:
+        t += dt
+        full += 1
+    pb = Problem(nx=n, ny=n, dim=2, dx=dx, dy=dx, dt=dt, periodic_y=False)
+    G = port.run(pb, full, G0, u, v)
+    if t < syn.ZALESAK_T_FINAL:
+        last = Problem(nx=n, ny=n, dim=2, dx=dx, dy=dx, dt=syn.ZALESAK_T_FINAL - t, periodic_y=False)
+        G = port.run(last, 1, G, u, v)
+        full += 1
+    return pb, G0, G, full
+
+
+def test_port_zalesak_matches_reference_log(port):
+    """The reference's 2D known answer: Zalesak's disk rotated once on 201^2
+    (log Local_code/level-set_MPI_2D/log/201x201.log).  The restated initial
+    field and the port's final field equal the compiled reference's (SHA-256
+    of the interiors); the scalars equal its values and the log's printed
+    L2, final area and step count."""
+    import hashlib
+    gold = json.load(open(os.path.join(GOLD, "golden_zalesak_201.json")))
+    sha = lambda a: hashlib.sha256(np.ascontiguousarray(a[3:-3, 3:-3]).tobytes()).hexdigest()
+    pb, G0, G, steps = zalesak_run(port)
+    assert sha(G0) == gold["G0_sha256"]
+    assert sha(G) == gold["G_final_sha256"]
+    assert steps == gold["steps"] == gold["log"]["steps"]
+    l2, a0, a1 = port.l2(pb, G, G0), port.volume(pb, G0), port.volume(pb, G)
+    assert (l2, a0, a1) == (gold["l2"], gold["area_initial"], gold["area_final"])
+    assert f"{l2:.6e}" == gold["log"]["l2"] and f"{a1:.6f}" == gold["log"]["area_final"]
+
+
 needs_ref = pytest.mark.skipif(not ref_available(), reason="oracle/_ref not built (no reference tree)")
 
 
