@@ -156,20 +156,16 @@ def test_deformation_64_matches_reference_log(cuda, lsgb_mod, port):
     assert l2 == pytest.approx(gold["l2"], rel=1e-9)
 
 
-def test_zalesak_201_matches_reference(cuda, lsgb_mod):
-    """The reference's 2D known answer (Zalesak's disk rotated once on 201^2,
-    periodic X, zero-gradient Y, 6284 steps with the final-step clip;
-    Local_code/level-set_MPI_2D/log/201x201.log) through the FP64 handle: the
-    final field equals the compiled reference's bit for bit (SHA-256 of the
-    interior) and the printed L2 and final area match the log."""
-    import hashlib
+def zalesak_gpu(lsgb, n):
+    """The reference's Zalesak loop on the FP64 handle: returns the final
+    ghosted G, its L2 error against G0, the final area and cell count, the
+    initial area and the step count."""
     from lsgb import synthetic as syn
-    gold = json.load(open(os.path.join(GOLD, "golden_zalesak_201.json")))
-    n = gold["n"]
     G0, u, v, dx, dt = syn.zalesak_fields(n)
-    p = lsgb_mod.params(2, n, n, 1, dx=dx, dy=dx, dt=dt, s_l=0.0, enable_reinit=False, bc_y=1)
-    with lsgb_mod.Solver(p, "f64") as s:
+    p = lsgb.params(2, n, n, 1, dx=dx, dy=dx, dt=dt, s_l=0.0, enable_reinit=False, bc_y=1)
+    with lsgb.Solver(p, "f64") as s:
         s.set_fields(G0, u, v)
+        a0, _ = s.volume()
         t, steps = 0.0, 0
         while t < syn.ZALESAK_T_FINAL:
             if t + dt > syn.ZALESAK_T_FINAL:
@@ -181,6 +177,33 @@ def test_zalesak_201_matches_reference(cuda, lsgb_mod):
         G = s.get_G()
         l2 = s.l2_error(G0)
         area, count = s.volume()
+    return G, l2, area, count, a0, steps
+
+
+# printed values of the reference's logs (Local_code/level-set_MPI_2D/log/<n>x<n>.log)
+ZALESAK_LOGS = {401: ("8.373019e-02", "0.058081", 12567), 801: ("8.250949e-02", "0.058311", 25133)}
+
+
+@pytest.mark.parametrize("n", [401, 801])
+def test_zalesak_larger_grids_match_reference_logs(cuda, lsgb_mod, n):
+    """The same known answer on the 401^2 and 801^2 logs: the printed L2,
+    final area and step count."""
+    _, l2, area, _, a0, steps = zalesak_gpu(lsgb_mod, n)
+    print(f"n={n}: l2={l2:.6e} area0={a0:.6f} area={area:.6f} steps={steps}")
+    log_l2, log_area, log_steps = ZALESAK_LOGS[n]
+    assert steps == log_steps
+    assert f"{l2:.6e}" == log_l2 and f"{area:.6f}" == log_area
+
+
+def test_zalesak_201_matches_reference(cuda, lsgb_mod):
+    """The reference's 2D known answer (Zalesak's disk rotated once on 201^2,
+    periodic X, zero-gradient Y, 6284 steps with the final-step clip;
+    Local_code/level-set_MPI_2D/log/201x201.log) through the FP64 handle: the
+    final field equals the compiled reference's bit for bit (SHA-256 of the
+    interior) and the printed L2 and final area match the log."""
+    import hashlib
+    gold = json.load(open(os.path.join(GOLD, "golden_zalesak_201.json")))
+    G, l2, area, count, _, steps = zalesak_gpu(lsgb_mod, gold["n"])
     sha = hashlib.sha256(np.ascontiguousarray(G[3:-3, 3:-3]).tobytes()).hexdigest()
     assert steps == gold["steps"]
     assert sha == gold["G_final_sha256"]
