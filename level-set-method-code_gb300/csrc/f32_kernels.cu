@@ -6,8 +6,8 @@
 // approximate reciprocal per reconstruction; the HCR-2 interface constraint
 // (r~ = phi0 / sum phi0_nb and the forcing beta (r~ sum phi - phi) / dx, the
 // sub-cell position of G = 0) is evaluated in FP64 on the flagged cells.
-// Accuracy against the FP64 path is measured, not assumed (bench.py
-// --precision-report and tests/test_gpu_precision.py).
+// Accuracy against the FP64 path is measured, not assumed (tests/test_gpu_f32.py,
+// lsgb/precision.py, and the precision_vs_fp64 entry of bench.py's line).
 //
 // WENO-5 in mirrored form: with sgn = (u_eff >= 0), the 7 samples G[i-3..i+3]
 // are read as w[m] = G[i-3+m] (sgn) or G[i+3-m] (!sgn).  Both the left-biased

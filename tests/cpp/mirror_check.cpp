@@ -3,7 +3,7 @@
 // rk3TimeStep3D, swap, reinitializeWithSwap3D, computeInterfaceVolume), on
 // device arrays.  Reads G,u,v,w (ghosted FP64, raw) from argv[1]..argv[4],
 // runs n steps with reinit every `interval`, writes G to argv[5] and prints
-// the volume.  Built and run by tests/test_gpu_cpp.py.
+// the volume.  Built and run by tests/test_cpp_mirror.py.
 #include <cuda_runtime.h>
 
 #include <cstdio>
