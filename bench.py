@@ -57,6 +57,7 @@ def parse():
     ap.add_argument("--adjoint-steps", type=int, default=300, help="RK3 steps of the adjoint form (0 = skip)")
     ap.add_argument("--adjoint-n", type=int, default=192)
     ap.add_argument("--sample-steps", type=int, default=10, help="steps of the sample-surface frequency sweep (0 = skip)")
+    ap.add_argument("--plane-n", type=int, default=4096, help="grid of the 2D stage-kernel leg (0 = skip)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--json-out", default=None)
     return ap.parse_args()
@@ -332,6 +333,35 @@ def measure_batched(torch, lsgb, syn, steps: int, dist: Dist):
             "workload": "config4: 48 2D (64^2..1024^2) + 48 3D (32^3..192^3), FP32-bulk, reinit every 5"}
 
 
+def measure_plane(torch, lsgb, syn, n: int, steps: int, peak_gbs: float, dist: Dist):
+    """The 2D FP32 stage kernel on one n x n plane (periodic): the first 2D
+    instance of configuration 4 (circle, 8-mode divergence-free velocity,
+    its S_L) at n^2, HCR-2 every 5 steps.  Stage launches of `steps` RK3
+    steps timed with the handle's CUDA events; algorithmic bytes per launch:
+    G, u, v in and G' out (16 B per cell), plus G^n in stages 2 and 3."""
+    wl = syn.config4(1, 0)[0]
+    wl.n = (n, n)
+    p = lsgb.params(2, n, n, 1, s_l=wl.s_l, enable_reinit=True, reinit_interval=RK_PER_BENCH_STEP,
+                    reinit_iterations=REINIT_ITERS)
+    with lsgb.Solver(p, "f32") as s:
+        s.synth(syn.to_device_desc(wl))
+        s.compute_dt(CFL)
+        s.advance(RK_PER_BENCH_STEP)  # warm-up, one reinit period
+        s.enable_timing(True)
+        s.advance(steps)
+        st, sn, rt, rn = s.kernel_times()
+        s.enable_timing(False)
+    st, rt = dist.max(st), dist.max(rt)
+    ms = st / max(sn, 1)
+    alg = n * n * 4 * (4 + 5 + 5) / 3  # average over the three stages
+    return {"stage_avg_launch_ms": ms, "stage_launches": sn, "reinit_avg_launch_ms": rt / max(rn, 1),
+            "gcell_stage_per_s": n * n / (ms * 1e-3) / 1e9,
+            "roofline": {"bound": "hbm", "achieved": alg / (ms * 1e-3) / 1e9, "peak": peak_gbs, "unit": "GB/s",
+                         "frac": alg / (ms * 1e-3) / 1e9 / peak_gbs, "algorithmic_bytes_per_launch": alg},
+            "kernel": "stage2d_f32_rows (fused WENO5 RHS + RK3 stage combine, 32 x 32 row-pair tiles)",
+            "workload": f"{n}^2 periodic plane, config-4 2D instance 0 construction, FP32-bulk, reinit every 5"}
+
+
 def measure_adjoint(torch, lsgb, n: int, steps: int, dist: Dist):
     """Configuration 5: gradient of the smoothed-Heaviside front mismatch with
     respect to the per-cell flame speed S_L(x) at n^3 (FP32-bulk), through
@@ -520,6 +550,10 @@ def run_ours(args, dist: Dist):
     if args.batch_steps > 0:
         batched = measure_batched(torch, lsgb, syn, args.batch_steps, dist)
 
+    plane = None
+    if args.plane_n > 0:
+        plane = measure_plane(torch, lsgb, syn, args.plane_n, 20, roofline["peak"], dist)
+
     sample = None
     if args.sample_steps > 0:
         sample = measure_sample(torch, lsgb, args.sample_steps, dist,
@@ -545,7 +579,7 @@ def run_ours(args, dist: Dist):
             "config": {"workload": f"config3 {n}^3 periodic, FP32-bulk WENO5-RK3 + HCR-2 (every 5 steps, "
                                    "2 pseudo-steps, FP64 interface constraint), S_L=0.2, CFL 0.5",
                        "grid": n, "bench_step": "5 RK3 steps + 1 HCR-2 reinit", "dt": dt,
-                       "l2": "inputs larger than L2 (each FP32 field 512 MiB)",
+                       "l2": f"inputs larger than L2 (each FP32 field {n ** 3 * 4 / 2 ** 20:.0f} MiB)",
                        "parallelism": f"replicas x{dist.world}"},
             "roofline": roofline,
             "whole_step_algorithmic_GBps": whole_step_gbs,
@@ -556,6 +590,7 @@ def run_ours(args, dist: Dist):
             "fp64": fp64,
             "precision_vs_fp64": prec,
             "reinit_avg_launch_ms": re_ms / max(re_n, 1),
+            "plane2d": plane,
             "batched": batched,
             "adjoint": adjoint,
             "sample_sweep": sample,

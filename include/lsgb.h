@@ -253,10 +253,10 @@ LSGB_API int lsgb_solver_enable_timing(lsgb_solver* s, int enable);
 LSGB_API int lsgb_solver_kernel_times(lsgb_solver* s, double* stage_ms, int64_t* stage_launches,
                                       double* reinit_ms, int64_t* reinit_launches);
 
-/* Tile shape of the FP32 stage kernels: the z-chunk length (16, 32, 64) of
- * the 3D tiles or the block height (2, 4, 8) of the 2D blocks; 0 = default
- * (3D: the chunk length that fills the GPU's SMs best for the grid).
- * Every shape gives bit-identical results; only the speed differs. */
+/* Tile shape of the FP32 3D stage kernel: the z-chunk length (16, 32, 64);
+ * 0 = default (the chunk length that fills the GPU's SMs best for the grid).
+ * Every shape gives bit-identical results; only the speed differs.  The 2D
+ * FP32 kernel and the FP64 kernels have one shape: 0 only. */
 LSGB_API int lsgb_solver_set_tile(lsgb_solver* s, int tile);
 LSGB_API int lsgb_solver_get_tile(const lsgb_solver* s, int* tile);
 
@@ -269,7 +269,8 @@ LSGB_API int lsgb_solver_debug_drop_copies(lsgb_solver* s, int on);
 
 /* Autotuner: times one stage launch per candidate tile shape (reps launches
  * each, CUDA events on the handle's stream; the state G is not modified) and
- * keeps the fastest.  Needs G and the velocity.  FP64 handles have one shape. */
+ * keeps the fastest.  Needs G and the velocity.  Handles with one shape
+ * report tile 0 and time 0. */
 LSGB_API int lsgb_solver_autotune(lsgb_solver* s, int reps, int* best_tile, float* best_ms);
 
 /* ------------------------------------------------------------------------

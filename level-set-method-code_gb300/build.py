@@ -31,7 +31,7 @@ EXTRA = {
     "sample_api.cu": ["-Xcompiler", "-ffp-contract=off"],
 }
 SOURCES = ["api.cu", "f64_kernels.cu", "f32_kernels.cu", "reduce.cu", "synth.cu", "noalloc.cu", "stage3d_f32.cu",
-           "adjoint.cu", "sample_kernels.cu", "sample_api.cu", "dump.cu", "diag.cu"]
+           "stage2d_f32.cu", "adjoint.cu", "sample_kernels.cu", "sample_api.cu", "dump.cu", "diag.cu"]
 
 
 def _nvcc() -> str:

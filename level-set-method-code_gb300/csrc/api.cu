@@ -898,12 +898,11 @@ extern "C" int lsgb_solver_kernel_times(lsgb_solver* s, double* stage_ms, int64_
 // ---------------------------------------------------------------------------
 namespace {
 
-// Tile shapes the FP32 kernels accept: z-chunk length of the 3D tiles,
-// block height of the 2D blocks.  FP64 kernels have one shape.
+// Tile shapes the FP32 kernels accept: the z-chunk length of the 3D tiles.
+// The 2D FP32 kernel (32 x 32 tiles) and the FP64 kernels have one shape.
 int tile_candidates(const lsgb_solver* s, int* c) {
-    if (s->prec != LSGB_PREC_F32) return 0;
-    if (s->p.dim == 3) { c[0] = 16; c[1] = 32; c[2] = 64; return 3; }
-    c[0] = 2; c[1] = 4; c[2] = 8; return 3;
+    if (s->prec != LSGB_PREC_F32 || s->p.dim != 3) return 0;
+    c[0] = 16; c[1] = 32; c[2] = 64; return 3;
 }
 
 }  // namespace

@@ -109,6 +109,8 @@ cudaError_t launch_stage_f64(const StageArgs& a, cudaStream_t st);
 cudaError_t launch_stage_f32(const StageArgs& a, cudaStream_t st);
 // err: device flag set when a bounded in-kernel wait gives up (nullable: no TMA path)
 cudaError_t launch_stage3d_f32_tiled(const StageArgs& a, int* err, cudaStream_t st);
+// The 2D FP32 stage (stage2d_f32.cu): row-pair tiles of 32 x 32 cells.
+cudaError_t launch_stage2d_f32_tiled(const StageArgs& a, cudaStream_t st);
 cudaError_t launch_reinit_f64(const ReinitArgs& a, cudaStream_t st);
 cudaError_t launch_reinit_f32(const ReinitArgs& a, cudaStream_t st);
 

@@ -1,0 +1,210 @@
+// stage2d_f32.cu -- the FP32-bulk 2D RK3 stage kernel.
+//
+// One launch = one TVD-RK3 stage over the whole 2D grid, fused: the u_eff
+// WENO-5 right-hand side of computeRHS (Local_code/level-set_MPI_2D/include/
+// rk3.h:54-98, weno5.h:135-230) and the stage combination of rk3Stage1..3
+// (rk3.h:104-150).  Compact arrays, periodic / zero-gradient neighbours by
+// index mapping.
+//
+// Shape: a CTA of 32 x 8 threads owns a 32 x 32 tile; thread (x, ty) owns
+// rows 4 ty .. 4 ty + 3 of column x as two row pairs, and every per-cell
+// quantity is a float2 over a row pair (packed f32x2 arithmetic).
+//   - The tile plus a halo (3 columns left and right, 4 rows above and below)
+//     is staged once in shared memory as row pairs.
+//   - x: every x face of the tile is computed once, by the lane of its
+//     column, with its indicators shared across the warp by shuffles, and
+//     stored; the two cells that share it read it after the barrier.
+//   - y: each thread reads its column's 12-row window and evaluates the
+//     faces of its rows (as face pairs) in registers.
+// The face values are the per-face WENO reconstructions of weno_f32x2.cuh
+// (both upwind biases per face, indicators times 144, weights times 10,
+// values times 6), the same arithmetic as the 3D kernel.
+#include "common.cuh"
+#include "weno_f32x2.cuh"
+
+namespace lsgb {
+namespace {
+
+using namespace wf;
+
+constexpr int TX = 32;                 // tile columns (one warp's lanes)
+constexpr int TY = 8;                  // thread rows of a CTA
+constexpr int NT = TX * TY;
+constexpr int RPT = 4;                 // cell rows per thread (two row pairs)
+constexpr int BY = TY * RPT;           // tile rows
+constexpr int PW = TX + 6;             // staged columns: tile x -3 .. TX+2
+constexpr int PP = (BY + 8) / 2;       // staged row pairs: tile rows -4 .. BY+3
+constexpr int NST = PP * PW;           // staged float2 entries
+constexpr int NFX = (TX + 1) * (BY / 2);  // x faces of the tile, per row pair
+
+struct Coef2 {
+    float inv_dx, inv_dy, inv_2dx, inv_2dy, s_l, eps, dt;
+};
+
+// Stage update of one row pair from its centre values, the neighbour
+// differences G(+1) - G(-1) along x and y, the point-wise fields and the
+// face differences; the 2D form of the 3D kernel's cell update.
+template <int STAGE>
+__device__ __forceinline__ float2 cell2(const Coef2& c, float2 gc, float2 gxd, float2 gyd, float2 uu, float2 vv,
+                                        float2 gn, float2 s_l, float2 dxL, float2 dxR, float2 dyL, float2 dyR) {
+    const float2 gx = mul2(gxd, c2(c.inv_2dx));
+    const float2 gy = mul2(gyd, c2(c.inv_2dy));
+    const float2 sq = fma2(gx, gx, fma2(gy, gy, c2(c.eps)));
+    const float2 f = make_float2(s_l.x > c.eps ? -s_l.x * rsqrtf(sq.x) : 0.0f,
+                                 s_l.y > c.eps ? -s_l.y * rsqrtf(sq.y) : 0.0f);
+    const float2 ue = fma2(f, gx, uu);
+    const float2 ve = fma2(f, gy, vv);
+    const float2 dgx = mul2(make_float2(ue.x >= 0.0f ? dxL.x : dxR.x, ue.y >= 0.0f ? dxL.y : dxR.y), c2(c.inv_dx));
+    const float2 dgy = mul2(make_float2(ve.x >= 0.0f ? dyL.x : dyR.x, ve.y >= 0.0f ? dyL.y : dyR.y), c2(c.inv_dy));
+    const float2 nrhs = fma2(ue, dgx, mul2(ve, dgy));  // = -rhs
+    if (STAGE == 1) return fma2(c2(-c.dt), nrhs, gc);
+    if (STAGE == 2) return fma2(c2(-0.25f * c.dt), nrhs, fma2(c2(0.75f), gn, mul2(c2(0.25f), gc)));
+    return fma2(c2(-(2.0f / 3.0f) * c.dt), nrhs, fma2(c2(1.0f / 3.0f), gn, mul2(c2(2.0f / 3.0f), gc)));
+}
+
+template <int STAGE, typename IDX>
+__global__ void __launch_bounds__(NT) stage2d_f32_rows(Geo g, const float* __restrict__ Gin,
+                                                       const float* __restrict__ Gn, float* __restrict__ Gout,
+                                                       const float* __restrict__ u, const float* __restrict__ v,
+                                                       const float* __restrict__ sl, Coef2 c) {
+    __shared__ float2 P[NST];              // [PP][PW]: (row 2p-4, row 2p-3) of tile column x-3
+    __shared__ float2 FL[NFX], FR[NFX];    // x faces [BY/2][TX+1]
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int t = ty * TX + tx;
+    const int i0 = blockIdx.x * TX, j0 = blockIdx.y * BY;
+    const IDX nx = g.nx;
+
+    // ---- stage the tile and its halo (every entry: two rows of one column);
+    // tiles whose halo lies inside the grid skip the wrap / clamp arithmetic ----
+    const bool inner = i0 >= 3 && i0 + PW - 3 <= g.nx && j0 >= 4 && j0 + 2 * PP - 4 <= g.ny;
+    if (inner) {
+        const float* base = Gin + (IDX)(j0 - 4) * nx + (i0 - 3);
+        for (int e = t; e < NST; e += NT) {
+            const int pp = e / PW, lx = e - pp * PW;
+            const float* q = base + (IDX)(2 * pp) * nx + lx;
+            P[e] = make_float2(__ldg(q), __ldg(q + nx));
+        }
+    } else {
+        for (int e = t; e < NST; e += NT) {
+            const int pp = e / PW, lx = e - pp * PW;
+            const IDX x = wrapg(i0 + lx - 3, g.nx, g.bcx);
+            const int r0 = j0 + 2 * pp - 4;
+            P[e] = make_float2(__ldg(Gin + (IDX)wrapg(r0, g.ny, g.bcy) * nx + x),
+                               __ldg(Gin + (IDX)wrapg(r0 + 1, g.ny, g.bcy) * nx + x));
+        }
+    }
+    // point-wise fields of the own cells (rows clamped into range; rows past
+    // the grid are computed but not stored)
+    const int gxc = wrapg(i0 + tx, g.nx, g.bcx);
+    float2 uu[2], vv[2], gn[2], s_l[2];
+    IDX orow[4];
+#pragma unroll
+    for (int r = 0; r < RPT; ++r) orow[r] = (IDX)min(j0 + RPT * ty + r, g.ny - 1) * nx + gxc;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const IDX a = orow[2 * h], b = orow[2 * h + 1];
+        uu[h] = make_float2(__ldg(u + a), __ldg(u + b));
+        vv[h] = make_float2(__ldg(v + a), __ldg(v + b));
+        gn[h] = STAGE > 1 ? make_float2(__ldg(Gn + a), __ldg(Gn + b)) : c2(0.0f);
+        s_l[h] = sl ? make_float2(__ldg(sl + a), __ldg(sl + b)) : c2(c.s_l);
+    }
+    __syncthreads();
+
+    // ---- x faces of the own row pairs; the tile's right-edge faces (column
+    // TX) of all BY/2 row pairs go to the first lanes of the last warp ----
+    const int pa = 2 * ty + 2;  // staged pair of rows 4ty, 4ty+1 (pair pa+1: rows 4ty+2, 4ty+3)
+    {
+        float2 L, R;
+        xface_shfl(P + pa * PW + tx, tx, L, R);
+        FL[(pa - 2) * (TX + 1) + tx] = L;
+        FR[(pa - 2) * (TX + 1) + tx] = R;
+        xface_shfl(P + (pa + 1) * PW + tx, tx, L, R);
+        FL[(pa - 1) * (TX + 1) + tx] = L;
+        FR[(pa - 1) * (TX + 1) + tx] = R;
+        if (ty == TY - 1 && tx < BY / 2) {
+            face6(P + (tx + 2) * PW + TX, 1, L, R);
+            FL[tx * (TX + 1) + TX] = L;
+            FR[tx * (TX + 1) + TX] = R;
+        }
+    }
+    // ---- y: window of tile rows 4ty-4 .. 4ty+7 of column tx; y[m] = row 4ty-4+m ----
+    float y[12];
+#pragma unroll
+    for (int m = 0; m < 6; ++m) {
+        const float2 w = P[(2 * ty + m) * PW + tx + 3];
+        y[2 * m] = w.x;
+        y[2 * m + 1] = w.y;
+    }
+    // indicators q(r) of rows 4ty-2 .. 4ty+6, qy[m] = q(row 4ty-4+m), m = 2 .. 10
+    float qy[11];
+#pragma unroll
+    for (int m = 2; m < 10; m += 2) {
+        const float2 q = qbeta(make_float2(y[m - 1], y[m]), make_float2(y[m], y[m + 1]),
+                               make_float2(y[m + 1], y[m + 2]));
+        qy[m] = q.x;
+        qy[m + 1] = q.y;
+    }
+    qy[10] = qbeta(c2(y[9]), c2(y[10]), c2(y[11])).x;
+    // face pairs (f, f+1), f = 4ty + 2h: samples rows f-3 .. f+3, indicators q(f-2) .. q(f+2)
+    float2 FyL[3], FyR[3];
+#pragma unroll
+    for (int h = 0; h < 3; ++h) {
+        const int m = 2 * h + 1;  // window index of row f-3
+        face(make_float2(y[m], y[m + 1]), make_float2(y[m + 1], y[m + 2]), make_float2(y[m + 2], y[m + 3]),
+             make_float2(y[m + 3], y[m + 4]), make_float2(y[m + 4], y[m + 5]), make_float2(y[m + 5], y[m + 6]),
+             make_float2(qy[m + 1], qy[m + 2]), make_float2(qy[m + 2], qy[m + 3]),
+             make_float2(qy[m + 3], qy[m + 4]), make_float2(qy[m + 4], qy[m + 5]), FyL[h], FyR[h]);
+    }
+    __syncthreads();  // x faces complete
+
+    // ---- cell update, row pairs A (4ty, 4ty+1) and B (4ty+2, 4ty+3) ----
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const float2* ctr = P + (pa + h) * PW + tx + 3;
+        const int xf = (pa - 2 + h) * (TX + 1) + tx;
+        const int m = 4 + 2 * h;  // window index of the pair's first row
+        const float2 nextL = make_float2(FyL[h].y, FyL[h + 1].x), nextR = make_float2(FyR[h].y, FyR[h + 1].x);
+        const float2 out = cell2<STAGE>(
+            c, ctr[0], sub2(ctr[1], ctr[-1]), sub2(make_float2(y[m + 1], y[m + 2]), make_float2(y[m - 1], y[m])),
+            uu[h], vv[h], gn[h], s_l[h], sub2(FL[xf + 1], FL[xf]), sub2(FR[xf + 1], FR[xf]), sub2(nextL, FyL[h]),
+            sub2(nextR, FyR[h]));
+        const int r = j0 + RPT * ty + 2 * h;
+        if (i0 + tx < g.nx) {
+            if (r < g.ny) Gout[orow[2 * h]] = out.x;
+            if (r + 1 < g.ny) Gout[orow[2 * h + 1]] = out.y;
+        }
+    }
+}
+
+template <int STAGE, typename IDX>
+cudaError_t launch2(const StageArgs& a, const Coef2& c, cudaStream_t st) {
+    const dim3 block(TX, TY, 1);
+    const dim3 grid((a.g.nx + TX - 1) / TX, (a.g.ny + BY - 1) / BY, 1);
+    stage2d_f32_rows<STAGE, IDX><<<grid, block, 0, st>>>(a.g, (const float*)a.Gin, (const float*)a.Gn,
+                                                          (float*)a.Gout, (const float*)a.u, (const float*)a.v,
+                                                          (const float*)a.sl, c);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t launch_stage2d_f32_tiled(const StageArgs& a, cudaStream_t st) {
+    Coef2 c;
+    // face values carry a factor 6 (see face())
+    c.inv_dx = (float)(1.0 / (6.0 * a.dx));
+    c.inv_dy = (float)(1.0 / (6.0 * a.dy));
+    c.inv_2dx = (float)(1.0 / (2.0 * a.dx));
+    c.inv_2dy = (float)(1.0 / (2.0 * a.dy));
+    c.s_l = (float)a.s_l;
+    c.eps = (float)a.eps;
+    c.dt = (float)a.dt;
+    const bool small = a.g.cells() < (1LL << 31) - 1;
+    cudaError_t e;
+    if (a.stage == 1) e = small ? launch2<1, int>(a, c, st) : launch2<1, long long>(a, c, st);
+    else if (a.stage == 2) e = small ? launch2<2, int>(a, c, st) : launch2<2, long long>(a, c, st);
+    else e = small ? launch2<3, int>(a, c, st) : launch2<3, long long>(a, c, st);
+    count_launches(1);
+    return e;
+}
+
+}  // namespace lsgb

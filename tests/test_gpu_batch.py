@@ -66,7 +66,7 @@ def test_tile_shapes_are_bit_identical(cuda, lsgb_mod):
     for dim, n in [(3, (36, 20, 70)), (3, (37, 21, 30)), (2, (70, 45, 1))]:
         p, f = instance(lsgb_mod, syn, dim, n, 7, "f32")
         outs = []
-        tiles = [16, 32, 64] if dim == 3 else [2, 4, 8]
+        tiles = [16, 32, 64] if dim == 3 else []  # the 2D kernel has one shape
         for tile in [0] + tiles:
             with lsgb_mod.Solver(p, "f32") as s:
                 s.set_fields(*f)
@@ -78,6 +78,6 @@ def test_tile_shapes_are_bit_identical(cuda, lsgb_mod):
         with lsgb_mod.Solver(p, "f32") as s:
             s.set_fields(*f)
             best, ms = s.autotune()
-            assert best in tiles and ms > 0
+            assert (best in tiles and ms > 0) if tiles else (best, ms) == (0, 0.0)
             with pytest.raises(lsgb_mod.LsgbError):
                 s.set_tile(5)
