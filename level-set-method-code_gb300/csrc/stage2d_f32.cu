@@ -6,11 +6,14 @@
 // (rk3.h:104-150).  Compact arrays, periodic / zero-gradient neighbours by
 // index mapping.
 //
-// Shape: a CTA of 32 x 8 threads owns a 32 x 32 tile; thread (x, ty) owns
+// Shape: a CTA of 32 x 8 threads works on 32 x 32 tiles; thread (x, ty) owns
 // rows 4 ty .. 4 ty + 3 of column x as two row pairs, and every per-cell
-// quantity is a float2 over a row pair (packed f32x2 arithmetic).
+// quantity is a float2 over a row pair (packed f32x2 arithmetic).  The grid
+// is persistent (as many CTAs as fit on the GPU, at most one per tile); a CTA
+// takes tiles blockIdx.x, blockIdx.x + gridDim.x, ...
 //   - The tile plus a halo (3 columns left and right, 4 rows above and below)
-//     is staged once in shared memory as row pairs.
+//     is staged in shared memory as row pairs by asynchronous copies, double
+//     buffered: the next tile's copies are in flight while this one computes.
 //   - x: every x face of the tile is computed once, by the lane of its
 //     column, with its indicators shared across the warp by shuffles, and
 //     stored; the two cells that share it read it after the barrier.
@@ -62,127 +65,159 @@ __device__ __forceinline__ float2 cell2(const Coef2& c, float2 gc, float2 gxd, f
     return fma2(c2(-(2.0f / 3.0f) * c.dt), nrhs, fma2(c2(1.0f / 3.0f), gn, mul2(c2(2.0f / 3.0f), gc)));
 }
 
-template <int STAGE, typename IDX>
-__global__ void __launch_bounds__(NT) stage2d_f32_rows(Geo g, const float* __restrict__ Gin,
-                                                       const float* __restrict__ Gn, float* __restrict__ Gout,
-                                                       const float* __restrict__ u, const float* __restrict__ v,
-                                                       const float* __restrict__ sl, Coef2 c) {
-    __shared__ float2 P[NST];              // [PP][PW]: (row 2p-4, row 2p-3) of tile column x-3
-    __shared__ float2 FL[NFX], FR[NFX];    // x faces [BY/2][TX+1]
-    const int tx = threadIdx.x, ty = threadIdx.y;
-    const int t = ty * TX + tx;
-    const int i0 = blockIdx.x * TX, j0 = blockIdx.y * BY;
+// Issue the asynchronous copies that stage tile (i0, j0) plus its halo into
+// P (every entry: two rows of one column).  Tiles whose halo lies inside the
+// grid copy with plain offsets, the others through the index map.
+template <typename IDX>
+__device__ __forceinline__ void stage_tile(float2* P, const float* __restrict__ Gin, const Geo& g, int i0, int j0,
+                                           int t) {
     const IDX nx = g.nx;
-
-    // ---- stage the tile and its halo (every entry: two rows of one column);
-    // tiles whose halo lies inside the grid skip the wrap / clamp arithmetic ----
     const bool inner = i0 >= 3 && i0 + PW - 3 <= g.nx && j0 >= 4 && j0 + 2 * PP - 4 <= g.ny;
     if (inner) {
         const float* base = Gin + (IDX)(j0 - 4) * nx + (i0 - 3);
         for (int e = t; e < NST; e += NT) {
             const int pp = e / PW, lx = e - pp * PW;
             const float* q = base + (IDX)(2 * pp) * nx + lx;
-            P[e] = make_float2(__ldg(q), __ldg(q + nx));
+            cp_async4((float*)(P + e), q);
+            cp_async4((float*)(P + e) + 1, q + nx);
         }
     } else {
         for (int e = t; e < NST; e += NT) {
             const int pp = e / PW, lx = e - pp * PW;
             const IDX x = wrapg(i0 + lx - 3, g.nx, g.bcx);
             const int r0 = j0 + 2 * pp - 4;
-            P[e] = make_float2(__ldg(Gin + (IDX)wrapg(r0, g.ny, g.bcy) * nx + x),
-                               __ldg(Gin + (IDX)wrapg(r0 + 1, g.ny, g.bcy) * nx + x));
+            cp_async4((float*)(P + e), Gin + (IDX)wrapg(r0, g.ny, g.bcy) * nx + x);
+            cp_async4((float*)(P + e) + 1, Gin + (IDX)wrapg(r0 + 1, g.ny, g.bcy) * nx + x);
         }
     }
-    // point-wise fields of the own cells (rows clamped into range; rows past
-    // the grid are computed but not stored)
-    const int gxc = wrapg(i0 + tx, g.nx, g.bcx);
-    float2 uu[2], vv[2], gn[2], s_l[2];
-    IDX orow[4];
-#pragma unroll
-    for (int r = 0; r < RPT; ++r) orow[r] = (IDX)min(j0 + RPT * ty + r, g.ny - 1) * nx + gxc;
-#pragma unroll
-    for (int h = 0; h < 2; ++h) {
-        const IDX a = orow[2 * h], b = orow[2 * h + 1];
-        uu[h] = make_float2(__ldg(u + a), __ldg(u + b));
-        vv[h] = make_float2(__ldg(v + a), __ldg(v + b));
-        gn[h] = STAGE > 1 ? make_float2(__ldg(Gn + a), __ldg(Gn + b)) : c2(0.0f);
-        s_l[h] = sl ? make_float2(__ldg(sl + a), __ldg(sl + b)) : c2(c.s_l);
-    }
-    __syncthreads();
+}
 
-    // ---- x faces of the own row pairs; the tile's right-edge faces (column
-    // TX) of all BY/2 row pairs go to the first lanes of the last warp ----
-    const int pa = 2 * ty + 2;  // staged pair of rows 4ty, 4ty+1 (pair pa+1: rows 4ty+2, 4ty+3)
-    {
-        float2 L, R;
-        xface_shfl(P + pa * PW + tx, tx, L, R);
-        FL[(pa - 2) * (TX + 1) + tx] = L;
-        FR[(pa - 2) * (TX + 1) + tx] = R;
-        xface_shfl(P + (pa + 1) * PW + tx, tx, L, R);
-        FL[(pa - 1) * (TX + 1) + tx] = L;
-        FR[(pa - 1) * (TX + 1) + tx] = R;
-        if (ty == TY - 1 && tx < BY / 2) {
-            face6(P + (tx + 2) * PW + TX, 1, L, R);
-            FL[tx * (TX + 1) + TX] = L;
-            FR[tx * (TX + 1) + TX] = R;
+template <int STAGE, typename IDX>
+__global__ void __launch_bounds__(NT, 3) stage2d_f32_rows(Geo g, const float* __restrict__ Gin,
+                                                          const float* __restrict__ Gn, float* __restrict__ Gout,
+                                                          const float* __restrict__ u, const float* __restrict__ v,
+                                                          const float* __restrict__ sl, Coef2 c, int ntx,
+                                                          int ntiles) {
+    __shared__ float2 Pbuf[2][NST];        // [PP][PW]: (row 2p-4, row 2p-3) of tile column x-3
+    __shared__ float2 FL[NFX], FR[NFX];    // x faces [BY/2][TX+1]
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int t = ty * TX + tx;
+    const IDX nx = g.nx;
+    int tile = blockIdx.x;
+    if (tile < ntiles) stage_tile<IDX>(Pbuf[0], Gin, g, (tile % ntx) * TX, (tile / ntx) * BY, t);
+    cp_async_commit();
+    for (int buf = 0; tile < ntiles; tile += gridDim.x, buf ^= 1) {
+        const int i0 = (tile % ntx) * TX, j0 = (tile / ntx) * BY;
+        const float2* P = Pbuf[buf];
+        // point-wise fields of the own cells (rows clamped into range; rows past
+        // the grid are computed but not stored)
+        const int gxc = wrapg(i0 + tx, g.nx, g.bcx);
+        float2 uu[2], vv[2], gn[2], s_l[2];
+        IDX orow[4];
+#pragma unroll
+        for (int r = 0; r < RPT; ++r) orow[r] = (IDX)min(j0 + RPT * ty + r, g.ny - 1) * nx + gxc;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const IDX a = orow[2 * h], b = orow[2 * h + 1];
+            uu[h] = make_float2(__ldg(u + a), __ldg(u + b));
+            vv[h] = make_float2(__ldg(v + a), __ldg(v + b));
+            gn[h] = STAGE > 1 ? make_float2(__ldg(Gn + a), __ldg(Gn + b)) : c2(0.0f);
+            s_l[h] = sl ? make_float2(__ldg(sl + a), __ldg(sl + b)) : c2(c.s_l);
         }
-    }
-    // ---- y: window of tile rows 4ty-4 .. 4ty+7 of column tx; y[m] = row 4ty-4+m ----
-    float y[12];
-#pragma unroll
-    for (int m = 0; m < 6; ++m) {
-        const float2 w = P[(2 * ty + m) * PW + tx + 3];
-        y[2 * m] = w.x;
-        y[2 * m + 1] = w.y;
-    }
-    // indicators q(r) of rows 4ty-2 .. 4ty+6, qy[m] = q(row 4ty-4+m), m = 2 .. 10
-    float qy[11];
-#pragma unroll
-    for (int m = 2; m < 10; m += 2) {
-        const float2 q = qbeta(make_float2(y[m - 1], y[m]), make_float2(y[m], y[m + 1]),
-                               make_float2(y[m + 1], y[m + 2]));
-        qy[m] = q.x;
-        qy[m + 1] = q.y;
-    }
-    qy[10] = qbeta(c2(y[9]), c2(y[10]), c2(y[11])).x;
-    // face pairs (f, f+1), f = 4ty + 2h: samples rows f-3 .. f+3, indicators q(f-2) .. q(f+2)
-    float2 FyL[3], FyR[3];
-#pragma unroll
-    for (int h = 0; h < 3; ++h) {
-        const int m = 2 * h + 1;  // window index of row f-3
-        face(make_float2(y[m], y[m + 1]), make_float2(y[m + 1], y[m + 2]), make_float2(y[m + 2], y[m + 3]),
-             make_float2(y[m + 3], y[m + 4]), make_float2(y[m + 4], y[m + 5]), make_float2(y[m + 5], y[m + 6]),
-             make_float2(qy[m + 1], qy[m + 2]), make_float2(qy[m + 2], qy[m + 3]),
-             make_float2(qy[m + 3], qy[m + 4]), make_float2(qy[m + 4], qy[m + 5]), FyL[h], FyR[h]);
-    }
-    __syncthreads();  // x faces complete
+        // this tile's copies done and visible; every thread is past the previous
+        // tile, so the other buffer and the face arrays are free
+        cp_async_wait<0>();
+        __syncthreads();
+        {
+            const int tn = tile + gridDim.x;
+            if (tn < ntiles) stage_tile<IDX>(Pbuf[buf ^ 1], Gin, g, (tn % ntx) * TX, (tn / ntx) * BY, t);
+            cp_async_commit();
+        }
 
-    // ---- cell update, row pairs A (4ty, 4ty+1) and B (4ty+2, 4ty+3) ----
+        // ---- x faces of the own row pairs; the tile's right-edge faces (column
+        // TX) of all BY/2 row pairs go to the first lanes of the last warp ----
+        const int pa = 2 * ty + 2;  // staged pair of rows 4ty, 4ty+1 (pair pa+1: rows 4ty+2, 4ty+3)
+        {
+            float2 L, R;
+            xface_shfl(P + pa * PW + tx, tx, L, R);
+            FL[(pa - 2) * (TX + 1) + tx] = L;
+            FR[(pa - 2) * (TX + 1) + tx] = R;
+            xface_shfl(P + (pa + 1) * PW + tx, tx, L, R);
+            FL[(pa - 1) * (TX + 1) + tx] = L;
+            FR[(pa - 1) * (TX + 1) + tx] = R;
+            if (ty == TY - 1 && tx < BY / 2) {
+                face6(P + (tx + 2) * PW + TX, 1, L, R);
+                FL[tx * (TX + 1) + TX] = L;
+                FR[tx * (TX + 1) + TX] = R;
+            }
+        }
+        // ---- y: window of tile rows 4ty-4 .. 4ty+7 of column tx; y[m] = row 4ty-4+m ----
+        float y[12];
 #pragma unroll
-    for (int h = 0; h < 2; ++h) {
-        const float2* ctr = P + (pa + h) * PW + tx + 3;
-        const int xf = (pa - 2 + h) * (TX + 1) + tx;
-        const int m = 4 + 2 * h;  // window index of the pair's first row
-        const float2 nextL = make_float2(FyL[h].y, FyL[h + 1].x), nextR = make_float2(FyR[h].y, FyR[h + 1].x);
-        const float2 out = cell2<STAGE>(
-            c, ctr[0], sub2(ctr[1], ctr[-1]), sub2(make_float2(y[m + 1], y[m + 2]), make_float2(y[m - 1], y[m])),
-            uu[h], vv[h], gn[h], s_l[h], sub2(FL[xf + 1], FL[xf]), sub2(FR[xf + 1], FR[xf]), sub2(nextL, FyL[h]),
-            sub2(nextR, FyR[h]));
-        const int r = j0 + RPT * ty + 2 * h;
-        if (i0 + tx < g.nx) {
-            if (r < g.ny) Gout[orow[2 * h]] = out.x;
-            if (r + 1 < g.ny) Gout[orow[2 * h + 1]] = out.y;
+        for (int m = 0; m < 6; ++m) {
+            const float2 w = P[(2 * ty + m) * PW + tx + 3];
+            y[2 * m] = w.x;
+            y[2 * m + 1] = w.y;
+        }
+        // indicators q(r) of rows 4ty-2 .. 4ty+6, qy[m] = q(row 4ty-4+m), m = 2 .. 10
+        float qy[11];
+#pragma unroll
+        for (int m = 2; m < 10; m += 2) {
+            const float2 q = qbeta(make_float2(y[m - 1], y[m]), make_float2(y[m], y[m + 1]),
+                                   make_float2(y[m + 1], y[m + 2]));
+            qy[m] = q.x;
+            qy[m + 1] = q.y;
+        }
+        qy[10] = qbeta(c2(y[9]), c2(y[10]), c2(y[11])).x;
+        // face pairs (f, f+1), f = 4ty + 2h: samples rows f-3 .. f+3, indicators q(f-2) .. q(f+2)
+        float2 FyL[3], FyR[3];
+#pragma unroll
+        for (int h = 0; h < 3; ++h) {
+            const int m = 2 * h + 1;  // window index of row f-3
+            face(make_float2(y[m], y[m + 1]), make_float2(y[m + 1], y[m + 2]), make_float2(y[m + 2], y[m + 3]),
+                 make_float2(y[m + 3], y[m + 4]), make_float2(y[m + 4], y[m + 5]), make_float2(y[m + 5], y[m + 6]),
+                 make_float2(qy[m + 1], qy[m + 2]), make_float2(qy[m + 2], qy[m + 3]),
+                 make_float2(qy[m + 3], qy[m + 4]), make_float2(qy[m + 4], qy[m + 5]), FyL[h], FyR[h]);
+        }
+        __syncthreads();  // x faces complete
+
+        // ---- cell update, row pairs A (4ty, 4ty+1) and B (4ty+2, 4ty+3) ----
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const float2* ctr = P + (pa + h) * PW + tx + 3;
+            const int xf = (pa - 2 + h) * (TX + 1) + tx;
+            const int m = 4 + 2 * h;  // window index of the pair's first row
+            const float2 nextL = make_float2(FyL[h].y, FyL[h + 1].x), nextR = make_float2(FyR[h].y, FyR[h + 1].x);
+            const float2 out = cell2<STAGE>(
+                c, ctr[0], sub2(ctr[1], ctr[-1]), sub2(make_float2(y[m + 1], y[m + 2]), make_float2(y[m - 1], y[m])),
+                uu[h], vv[h], gn[h], s_l[h], sub2(FL[xf + 1], FL[xf]), sub2(FR[xf + 1], FR[xf]), sub2(nextL, FyL[h]),
+                sub2(nextR, FyR[h]));
+            const int r = j0 + RPT * ty + 2 * h;
+            if (i0 + tx < g.nx) {
+                if (r < g.ny) Gout[orow[2 * h]] = out.x;
+                if (r + 1 < g.ny) Gout[orow[2 * h + 1]] = out.y;
+            }
         }
     }
 }
 
 template <int STAGE, typename IDX>
 cudaError_t launch2(const StageArgs& a, const Coef2& c, cudaStream_t st) {
+    // resident CTAs of this instance on the whole GPU (queried once)
+    static const int resident = [] {
+        int dev = 0, sms = 0, per_sm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, stage2d_f32_rows<STAGE, IDX>, NT, 0);
+        return (sms > 0 ? sms : 1) * (per_sm > 0 ? per_sm : 1);
+    }();
+    const int ntx = (a.g.nx + TX - 1) / TX;
+    const int ntiles = ntx * ((a.g.ny + BY - 1) / BY);
     const dim3 block(TX, TY, 1);
-    const dim3 grid((a.g.nx + TX - 1) / TX, (a.g.ny + BY - 1) / BY, 1);
+    const dim3 grid(ntiles < resident ? ntiles : resident, 1, 1);
     stage2d_f32_rows<STAGE, IDX><<<grid, block, 0, st>>>(a.g, (const float*)a.Gin, (const float*)a.Gn,
                                                           (float*)a.Gout, (const float*)a.u, (const float*)a.v,
-                                                          (const float*)a.sl, c);
+                                                          (const float*)a.sl, c, ntx, ntiles);
     return cudaGetLastError();
 }
 

@@ -87,7 +87,6 @@ struct Coef {
 };
 
 // ---- TMA / mbarrier primitives (PTX) ----------------------------------------
-__device__ __forceinline__ uint32_t saddr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
 __device__ __forceinline__ void mbar_init(uint64_t* b, uint32_t count) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(saddr(b)), "r"(count) : "memory");
@@ -118,17 +117,6 @@ __device__ __forceinline__ void tma_load_3d(float* dst, const CUtensorMap* tm, i
         "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];"
         ::"r"(saddr(dst)), "l"(tm), "r"(x), "r"(y), "r"(z), "r"(saddr(b))
         : "memory");
-}
-
-// Ampere-style asynchronous 4-byte copies (the staging of fields whose row
-// pitch rules out bulk tensor copies); completion per thread by groups.
-__device__ __forceinline__ void cp_async4(float* dst, const float* src) {
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(saddr(dst)), "l"(src) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() {
-    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
 }
 
 // Update of one plane pair from its centre values, the neighbour

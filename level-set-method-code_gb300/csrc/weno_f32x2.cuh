@@ -2,7 +2,8 @@
 // (stage3d_f32.cu, stage2d_f32.cu): the per-face WENO-5 reconstructions of
 // weno5_left / weno5_right (Local_code/level-set_MPI_3D/include/weno5.h:28-81)
 // evaluated on pairs of values at once.  The pair is whatever the kernel
-// packs: two z-planes in 3D, two rows in 2D.
+// packs: two z-planes in 3D, two rows in 2D.  Also the asynchronous-copy
+// primitives both kernels stage with.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -57,6 +58,20 @@ __device__ __forceinline__ void face(float2 g0, float2 g1, float2 g2, float2 g3,
     const float2 rw2 = mul2(qp1, q0);
     L = div2(fma2(q12, Pa, fma2(lw1, Pb, mul2(lw2, Pc))), add2(add2(q12, lw1), lw2));
     R = div2(fma2(rw0, Pr, fma2(rw1, Pc, mul2(rw2, Pb))), add2(add2(rw0, rw1), rw2));
+}
+
+// Shared-memory address of a generic pointer into shared memory.
+__device__ __forceinline__ uint32_t saddr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// Ampere-style asynchronous 4-byte copies global -> shared; completion per
+// thread by groups (the copies depend on nothing but the memory system).
+__device__ __forceinline__ void cp_async4(float* dst, const float* src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(saddr(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
 }
 
 // Coordinate map for tile loads: any offset (ragged tiles reach past n).
