@@ -88,27 +88,62 @@ __global__ void scale3_kernel(long long n, double s, double* u, double* v, doubl
 
 // computeDeformationVelocity (Local_code/level-set_MPI_3D/include/
 // initial_conditions.h:232-247) at the cell centres x_i = i * dx, written
-// straight into the compact velocity arrays of the solver.
-template <typename T>
-__global__ void deformation_kernel(Geo g, double dx, double dy, double dz, double t, double Tp,
-                                   T* __restrict__ u, T* __restrict__ v, T* __restrict__ w) {
-    const long long n = g.cells();
-    const long long nxy = (long long)g.nx * g.ny;
+// straight into the compact velocity arrays of the solver.  The field is a
+// product of per-axis factors, so the sines are evaluated once per axis
+// index (deformation_factors_kernel) and every cell forms the reference's
+// products from them in its order.  The FP64 solver gets exactly the values
+// of evaluating the sines at every cell; the FP32 solver forms the products
+// in FP32 from the factors rounded to FP32 (within a few FP32 ulps of the
+// rounded FP64 product).
+//   tab = [sin(pi x_i)][sin(2 pi x_i)] [.. y ..] [.. z ..] [cos(pi t / T)],
+//   the same table in FP64 and in FP32.
+__global__ void deformation_factors_kernel(Geo g, double dx, double dy, double dz, double t, double Tp,
+                                           double* __restrict__ tab, float* __restrict__ tabf) {
     const double pi = 3.14159265358979323846;
-    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n;
-         e += (long long)gridDim.x * blockDim.x) {
-        const int k = (int)(e / nxy);
-        const long long r = e - (long long)k * nxy;
-        const int j = (int)(r / g.nx);
-        const int i = (int)(r - (long long)j * g.nx);
-        const double x = i * dx, y = j * dy, z = k * dz;
-        const double tf = cos(pi * t / Tp);
-        const double spx = sin(pi * x), s2px = sin(2.0 * pi * x);
-        const double spy = sin(pi * y), s2py = sin(2.0 * pi * y);
-        const double spz = sin(pi * z), s2pz = sin(2.0 * pi * z);
-        u[e] = (T)(2.0 * spx * spx * s2py * s2pz * tf);
-        v[e] = (T)(-s2px * spy * spy * s2pz * tf);
-        w[e] = (T)(-s2px * s2py * spz * spz * tf);
+    const int n[3] = {g.nx, g.ny, g.nz};
+    const double h[3] = {dx, dy, dz};
+    int base = 0;
+    for (int a = 0; a < 3; ++a) {
+        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n[a]; i += gridDim.x * blockDim.x) {
+            const double x = i * h[a];
+            const double s1 = sin(pi * x), s2 = sin(2.0 * pi * x);
+            tab[base + i] = s1;
+            tab[base + n[a] + i] = s2;
+            tabf[base + i] = (float)s1;
+            tabf[base + n[a] + i] = (float)s2;
+        }
+        base += 2 * n[a];
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        tab[base] = cos(pi * t / Tp);
+        tabf[base] = (float)tab[base];
+    }
+}
+
+// One thread per cell of a row segment; rows (j, k) strided over gridDim.y.
+// T = the solver's precision, the arithmetic of the products.
+template <typename T>
+__global__ void deformation_kernel(Geo g, const T* __restrict__ tab, T* __restrict__ u, T* __restrict__ v,
+                                   T* __restrict__ w) {
+    const T* s1x = tab;
+    const T* s2x = s1x + g.nx;
+    const T* s1y = s2x + g.nx;
+    const T* s2y = s1y + g.ny;
+    const T* s1z = s2y + g.ny;
+    const T* s2z = s1z + g.nz;
+    const T tf = s2z[g.nz];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= g.nx) return;
+    const T spx = s1x[i], s2px = s2x[i];
+    const long long rows = (long long)g.ny * g.nz;
+    for (long long row = blockIdx.y; row < rows; row += gridDim.y) {
+        const int k = (int)(row / g.ny);
+        const int j = (int)(row - (long long)k * g.ny);
+        const T spy = s1y[j], s2py = s2y[j], spz = s1z[k], s2pz = s2z[k];
+        const long long e = row * g.nx + i;
+        u[e] = (T)2 * spx * spx * s2py * s2pz * tf;
+        v[e] = -s2px * spy * spy * s2pz * tf;
+        w[e] = -s2px * s2py * spz * spz * tf;
     }
 }
 
@@ -116,14 +151,22 @@ __global__ void deformation_kernel(Geo g, double dx, double dy, double dz, doubl
 
 cudaError_t launch_deformation(const Geo& g, double dx, double dy, double dz, double t, double Tp,
                                void* u, void* v, void* w, bool f32, cudaStream_t st) {
-    long long blocks = (g.cells() + 255) / 256;
-    if (blocks > 152 * 32) blocks = 152 * 32;
+    double* tab = nullptr;
+    const size_t ntab = 2 * ((size_t)g.nx + g.ny + g.nz) + 1;
+    cudaError_t e = cudaMallocAsync((void**)&tab, ntab * (sizeof(double) + sizeof(float)), st);
+    if (e != cudaSuccess) return e;
+    float* tabf = (float*)(tab + ntab);
+    deformation_factors_kernel<<<8, 256, 0, st>>>(g, dx, dy, dz, t, Tp, tab, tabf);
+    const long long rows = (long long)g.ny * g.nz;
+    const dim3 block(128), grid((g.nx + 127) / 128, (unsigned)(rows < 65535 ? rows : 65535));
     if (f32)
-        deformation_kernel<float><<<(unsigned)blocks, 256, 0, st>>>(g, dx, dy, dz, t, Tp, (float*)u, (float*)v, (float*)w);
+        deformation_kernel<float><<<grid, block, 0, st>>>(g, tabf, (float*)u, (float*)v, (float*)w);
     else
-        deformation_kernel<double><<<(unsigned)blocks, 256, 0, st>>>(g, dx, dy, dz, t, Tp, (double*)u, (double*)v, (double*)w);
-    count_launches(1);
-    return cudaGetLastError();
+        deformation_kernel<double><<<grid, block, 0, st>>>(g, tab, (double*)u, (double*)v, (double*)w);
+    count_launches(2);
+    e = cudaGetLastError();
+    const cudaError_t f = cudaFreeAsync(tab, st);
+    return e != cudaSuccess ? e : f;
 }
 
 cudaError_t launch_synth(const Geo& g, const lsgb_synth& d, double dx, double dy, double dz,

@@ -94,3 +94,29 @@ def test_f32_2d_vs_f64(cuda, lsgb_mod, n, bc):
         err = float(np.abs(g32 - g64).max())
         print(f"2D n={n} bc={bc} sl_field={field is not None}: linf={err:.3e}")
         assert err <= 5e-5
+
+
+def test_deformation_velocity_f32_vs_f64(cuda, lsgb_mod):
+    """The on-device deformation vortex (computeDeformationVelocity,
+    Local_code/level-set_MPI_3D/include/initial_conditions.h:232-247): the
+    FP64 solver's field is the formula at x_i = i dx (numpy's sines, to 1e-15
+    of max|u|); the FP32 solver forms the products in FP32 and stays within
+    4 FP32 ulps of max|u| of the FP64 field.  Ragged sizes, unequal spacing."""
+    n = (37, 21, 30)
+    h = (1 / 36, 1 / 20, 1 / 29)
+    t, T = 0.37, 1.5
+    p = lsgb_mod.params(3, *n, dx=h[0], dy=h[1], dz=h[2], dt=1e-3)
+    out = {}
+    for prec in ("f64", "f32"):
+        with lsgb_mod.Solver(p, prec) as s:
+            s.set_velocity_deformation(t, T)
+            out[prec] = [s.get_field(f, layout="compact") for f in ("u", "v", "w")]
+    z, y, x = np.meshgrid(*[np.arange(q) * hq for q, hq in zip(n[::-1], h[::-1])], indexing="ij")
+    tf = np.cos(np.pi * t / T)
+    s1 = [np.sin(np.pi * c) for c in (x, y, z)]
+    s2 = [np.sin(2 * np.pi * c) for c in (x, y, z)]
+    ref = [2 * s1[0] ** 2 * s2[1] * s2[2] * tf, -s2[0] * s1[1] ** 2 * s2[2] * tf, -s2[0] * s2[1] * s1[2] ** 2 * tf]
+    for r, a64, a32 in zip(ref, out["f64"], out["f32"]):
+        scale = np.abs(r).max()
+        assert np.abs(a64 - r).max() <= 1e-15 * scale
+        assert np.abs(a32 - a64).max() <= 4 * np.finfo(np.float32).eps * scale
