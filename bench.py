@@ -58,6 +58,7 @@ def parse():
     ap.add_argument("--adjoint-n", type=int, default=192)
     ap.add_argument("--sample-steps", type=int, default=10, help="steps of the sample-surface frequency sweep (0 = skip)")
     ap.add_argument("--plane-n", type=int, default=4096, help="grid of the 2D stage-kernel leg (0 = skip)")
+    ap.add_argument("--deform-steps", type=int, default=20, help="RK3 steps of the live deformation leg (0 = skip)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--json-out", default=None)
     return ap.parse_args()
@@ -362,6 +363,52 @@ def measure_plane(torch, lsgb, syn, n: int, steps: int, peak_gbs: float, dist: D
             "workload": f"{n}^2 periodic plane, config-4 2D instance 0 construction, FP32-bulk, reinit every 5"}
 
 
+def measure_deformation(torch, lsgb, syn, n: int, steps: int, dist: Dist):
+    """The reference's time-dependent case at n^3, FP32: the deformation
+    vortex recomputed every step (Local_code/level-set_MPI_3D/src/main.cpp:
+    291-317), HCR-2 every 5 steps, on the configuration-3 front.  Two forms of
+    the same loop, CUDA events on the solver's stream: the vortex evaluated
+    inside the stage kernel (live mode, one advance call) and the explicit
+    per-step refill of the stored u, v, w (set_velocity_deformation +
+    advance(1)); the two forms give the same bits
+    (tests/test_gpu_live_velocity.py)."""
+    stream = torch.cuda.Stream()
+    s, wl = make_solver(lsgb, syn, n, "f32", stream)
+    dt = 0.5 / (n * (2.0 + 1.0 + 1.0 + wl.s_l))  # CFL 0.5: max |u| + |v| + |w| of the vortex is 4
+    s.set_dt(dt)
+    out = {}
+    for form in ("fused", "refill"):
+        s.step = 0
+        t = 0.0
+        if form == "fused":
+            s.set_velocity_deformation_live(t, 1.5)
+            s.advance(RK_PER_BENCH_STEP)  # warm-up
+        else:
+            for _ in range(RK_PER_BENCH_STEP):
+                s.set_velocity_deformation(t, 1.5)
+                s.advance(1)
+                t += dt
+        torch.cuda.synchronize()
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+        with torch.cuda.stream(stream):
+            ev[0].record(stream)
+            if form == "fused":
+                s.advance(steps)
+            else:
+                for _ in range(steps):
+                    s.set_velocity_deformation(t, 1.5)
+                    s.advance(1)
+                    t += dt
+            ev[1].record(stream)
+        torch.cuda.synchronize()
+        ms = dist.max(ev[0].elapsed_time(ev[1]))
+        out[form] = {"ms_per_step": ms / steps, "value": dist.world * n ** 3 * steps / (ms * 1e-3) / 1e9}
+    s.close()
+    return {"value": out["fused"]["value"], "unit": "Gcell-updates/s", "rk3_steps": steps,
+            "ms_per_step": out["fused"]["ms_per_step"], "refill_per_step": out["refill"],
+            "workload": f"{n}^3 deformation vortex recomputed every step, FP32, HCR-2 every 5, dt {dt:.3g}"}
+
+
 def measure_adjoint(torch, lsgb, n: int, steps: int, dist: Dist):
     """Configuration 5: gradient of the smoothed-Heaviside front mismatch with
     respect to the per-cell flame speed S_L(x) at n^3 (FP32-bulk), through
@@ -550,6 +597,10 @@ def run_ours(args, dist: Dist):
     if args.batch_steps > 0:
         batched = measure_batched(torch, lsgb, syn, args.batch_steps, dist)
 
+    deform = None
+    if args.deform_steps > 0:
+        deform = measure_deformation(torch, lsgb, syn, n, args.deform_steps, dist)
+
     plane = None
     if args.plane_n > 0:
         plane = measure_plane(torch, lsgb, syn, args.plane_n, 20, roofline["peak"], dist)
@@ -591,6 +642,7 @@ def run_ours(args, dist: Dist):
             "precision_vs_fp64": prec,
             "reinit_avg_launch_ms": re_ms / max(re_n, 1),
             "plane2d": plane,
+            "deformation": deform,
             "batched": batched,
             "adjoint": adjoint,
             "sample_sweep": sample,

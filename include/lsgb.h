@@ -346,10 +346,27 @@ LSGB_API int lsgb_adjoint_backward(lsgb_adjoint* a, const double* dL_dGT, int la
 LSGB_API int lsgb_adjoint_get_grad(lsgb_adjoint* a, int which, double* out, int layout, int memory);
 
 /* Deformation-vortex velocity of the reference's default 3D test case at time
- * t with period T, evaluated on the device at the cell centres x_i = i * dx:
- * computeDeformationVelocity / updateDeformationVelocity
- * (Local_code/level-set_MPI_3D/include/initial_conditions.h:232-282). */
+ * t with period T, evaluated on the device at the cell centres x_i = i * dx
+ * into the stored u, v, w: computeDeformationVelocity /
+ * updateDeformationVelocity
+ * (Local_code/level-set_MPI_3D/include/initial_conditions.h:232-282).  FP64
+ * handles get the reference's products of FP64 sines; FP32 handles form the
+ * products in FP32 from factor tables.  Ends live mode (below). */
 LSGB_API int lsgb_solver_set_velocity_deformation(lsgb_solver* s, double t, double T);
+/* Live mode: from now on every step uses the vortex at the handle's time,
+ * which starts at t and advances by dt after each step -- the reference's
+ * loop (src/main.cpp:291-317: velocity at current_time, RK3 step, reinit,
+ * current_time += dt) inside one lsgb_solver_advance.  FP32 3D handles with
+ * nx % 4 == 0 and fewer than 2^31 cells evaluate the vortex inside the stage
+ * kernel (no u, v, w traffic); other handles refill u, v, w before each step.
+ * Either way the fields equal a per-step lsgb_solver_set_velocity_deformation
+ * loop bit for bit.  Calls that read u, v, w (lsgb_solver_max_speed,
+ * lsgb_solver_get_field) see the vortex at the current time.  Setting
+ * velocity arrays ends live mode; batches and the adjoint reject handles in
+ * it (LSGB_ERR_UNSUPPORTED). */
+LSGB_API int lsgb_solver_set_velocity_deformation_live(lsgb_solver* s, double t, double T);
+/* The live-mode time (the t of the next step). */
+LSGB_API int lsgb_solver_get_time(const lsgb_solver* s, double* t);
 
 /* Error and conservation diagnostics of the reference's analysis script
  * (Local_code/level-set_MPI_3D/scripts/analyze_error.m) between the solver's

@@ -343,6 +343,11 @@ struct lsgb_solver {
     double* scratch = nullptr;   // reduction partials + results
     double* h_res = nullptr;     // pinned result slots
     int step = 0;
+    // live deformation velocity (lsgb_solver_set_velocity_deformation_live):
+    // every step uses the vortex at time vel_t, which then advances by dt
+    bool vel_live = false;
+    double vel_t = 0.0, vel_T = 1.0;
+    float* defo_f32 = nullptr;  // FP32 factor tables of the vortex (built once)
     int tile = 0;  // tile-shape choice handed to the stage kernels (0 = default)
     int drop_copies = 0;  // test hook (lsgb_solver_debug_drop_copies)
     bool have_G = false, have_vel = false;
@@ -458,14 +463,62 @@ int launch_stage(lsgb_solver* s, const StageArgs& a) {
     return LSGB_OK;
 }
 
+// ---- deformation vortex (computeDeformationVelocity, Local_code/level-set_MPI_3D/
+// include/initial_conditions.h:232-247; recomputed every step as in src/main.cpp:297-299)
+
+int ensure_defo_tables(lsgb_solver* s) {
+    if (s->defo_f32) return LSGB_OK;
+    const size_t b = sizeof(float) * deformation_table_floats(s->g);
+    cudaError_t e = cudaMalloc((void**)&s->defo_f32, b);
+    if (e != cudaSuccess) { s->defo_f32 = nullptr; return fail(LSGB_ERR_ALLOC, "deformation tables: %s", cudaGetErrorString(e)); }
+    LSGB_CUDA(launch_deformation_tables_f32(s->g, s->p.dx, s->p.dy, s->p.dz, s->defo_f32, s->st));
+    return LSGB_OK;
+}
+
+float defo_time_factor(double t, double T) { return (float)std::cos(3.14159265358979323846 * t / T); }
+
+// Write the vortex at time t into the stored velocity arrays.
+int fill_deformation(lsgb_solver* s, double t, double T) {
+    if (s->prec == LSGB_PREC_F64) {
+        LSGB_CUDA(launch_deformation_f64(s->g, s->p.dx, s->p.dy, s->p.dz, t, T, (double*)s->u, (double*)s->v,
+                                         (double*)s->w, s->st));
+    } else {
+        LSGB_TRY(ensure_defo_tables(s));
+        LSGB_CUDA(launch_deformation_f32(s->g, s->defo_f32, defo_time_factor(t, T), (float*)s->u, (float*)s->v,
+                                         (float*)s->w, s->st));
+    }
+    return LSGB_OK;
+}
+
+// Live vortex evaluated inside the FP32 3D stage kernel (no u, v, w traffic).
+bool live_fused(const lsgb_solver* s) {
+    return s->vel_live && s->prec == LSGB_PREC_F32 && stage3d_f32_fuses_deformation(s->g);
+}
+
+// Velocity operands of a stage launch: the stored arrays, or the fused vortex.
+void velocity_args(const lsgb_solver* s, StageArgs& a) {
+    a.u = s->u; a.v = s->v; a.w = s->w;
+    if (live_fused(s)) {
+        a.defo = s->defo_f32;
+        a.tf = defo_time_factor(s->vel_t, s->vel_T);
+    }
+}
+
+// Bring the stored arrays up to date before a call that reads them.
+int materialize_velocity(lsgb_solver* s) {
+    return s->vel_live ? fill_deformation(s, s->vel_t, s->vel_T) : LSGB_OK;
+}
+
 // One TVD-RK3 step: G -> A (stage 1), A -> B (stage 2), (G, B) -> G (stage 3).
 // Stage 3 writes in place: G^n enters only point-wise, read by the thread that
 // writes the same cell, so every cell's G^n is read before it is replaced.
 // The buffers keep their roles, which makes captured step sequences
 // replayable.
 int rk3_step(lsgb_solver* s) {
+    if (s->vel_live && !live_fused(s)) LSGB_TRY(fill_deformation(s, s->vel_t, s->vel_T));
     StageArgs a = stage_args(s->p, s->g, s->lay);
-    a.u = s->u; a.v = s->v; a.w = s->w; a.sl = s->sl;
+    velocity_args(s, a);
+    a.sl = s->sl;
     a.err = err_flag(s);
     a.tile = s->tile;
     a.drop_copies = s->drop_copies;
@@ -581,7 +634,7 @@ extern "C" int lsgb_solver_destroy(lsgb_solver* s) {
     if (!s) return LSGB_OK;
     if (s->st) cudaStreamSynchronize(s->st);
     snapshots_close(s);
-    void* ptrs[9] = {s->G, s->A, s->B, s->u, s->v, s->w, s->sl, s->stage64, s->scratch};
+    void* ptrs[10] = {s->G, s->A, s->B, s->u, s->v, s->w, s->sl, s->stage64, s->scratch, s->defo_f32};
     for (void* q : ptrs)
         if (q) cudaFree(q);
     if (s->h_res) cudaFreeHost(s->h_res);
@@ -631,6 +684,7 @@ extern "C" int lsgb_solver_set_fields(lsgb_solver* s, const double* G, const dou
     if (v) LSGB_TRY(load_field(s, s->v, v, layout, memory));
     if (w && s->p.dim == 3) LSGB_TRY(load_field(s, s->w, w, layout, memory));
     if (u && v && (w || s->p.dim == 2)) s->have_vel = true;
+    if (u || v || w) s->vel_live = false;
     return LSGB_OK;
 }
 
@@ -681,7 +735,15 @@ extern "C" int lsgb_solver_advance(lsgb_solver* s, int n_steps) {
         if (s->p.enable_reinit && s->step > 0 && s->step % s->p.reinit_interval == 0)
             LSGB_TRY(reinit(s));
         s->step++;
+        if (s->vel_live) s->vel_t += s->p.dt;  // current_time += params.dt (src/main.cpp:316)
     }
+    return LSGB_OK;
+}
+
+extern "C" int lsgb_solver_get_time(const lsgb_solver* s, double* t) {
+    LSGB_TRY(solver_ok(s));
+    if (!t) return fail(LSGB_ERR_INVALID, "t is NULL");
+    *t = s->vel_t;
     return LSGB_OK;
 }
 
@@ -723,6 +785,7 @@ extern "C" int lsgb_solver_max_speed(lsgb_solver* s, double* max_speed) {
     LSGB_TRY(solver_ok(s));
     if (!s->have_vel) return fail(LSGB_ERR_STATE, "velocity has not been set");
     if (!max_speed) return fail(LSGB_ERR_INVALID, "max_speed is NULL");
+    LSGB_TRY(materialize_velocity(s));
     if (s->prec == LSGB_PREC_F64)
         LSGB_CUDA(launch_max_speed<double>(s->g, s->lay, (const double*)s->u, (const double*)s->v,
                                            (const double*)s->w, s->scratch, red_out(s), s->st));
@@ -833,7 +896,7 @@ extern "C" int lsgb_solver_synth(lsgb_solver* s, const lsgb_synth* d) {
         for (int q = 0; q < 4; ++q)
             if (tmp[q]) cudaFreeAsync(tmp[q], s->st);
     }
-    if (rc == LSGB_OK) { s->have_G = true; s->have_vel = true; }
+    if (rc == LSGB_OK) { s->have_G = true; s->have_vel = true; s->vel_live = false; }
     return rc;
 }
 
@@ -841,8 +904,20 @@ extern "C" int lsgb_solver_set_velocity_deformation(lsgb_solver* s, double t, do
     LSGB_TRY(solver_ok(s));
     if (s->p.dim != 3) return fail(LSGB_ERR_INVALID, "the deformation vortex is a 3D field");
     if (!std::isfinite(t) || !std::isfinite(T) || T == 0.0) return fail(LSGB_ERR_INVALID, "bad t / T");
-    LSGB_CUDA(launch_deformation(s->g, s->p.dx, s->p.dy, s->p.dz, t, T, s->u, s->v, s->w,
-                                 s->prec == LSGB_PREC_F32, s->st));
+    LSGB_TRY(fill_deformation(s, t, T));
+    s->vel_live = false;
+    s->have_vel = true;
+    return LSGB_OK;
+}
+
+extern "C" int lsgb_solver_set_velocity_deformation_live(lsgb_solver* s, double t, double T) {
+    LSGB_TRY(solver_ok(s));
+    if (s->p.dim != 3) return fail(LSGB_ERR_INVALID, "the deformation vortex is a 3D field");
+    if (!std::isfinite(t) || !std::isfinite(T) || T == 0.0) return fail(LSGB_ERR_INVALID, "bad t / T");
+    if (s->prec == LSGB_PREC_F32) LSGB_TRY(ensure_defo_tables(s));
+    s->vel_live = true;
+    s->vel_t = t;
+    s->vel_T = T;
     s->have_vel = true;
     return LSGB_OK;
 }
@@ -855,6 +930,7 @@ extern "C" int lsgb_solver_get_field(lsgb_solver* s, int which, double* out, int
             : which == LSGB_FIELD_SL ? s->sl : nullptr;
     if (!f) return fail(LSGB_ERR_INVALID, "field %d is not resident", which);
     if (!out) return fail(LSGB_ERR_INVALID, "out is NULL");
+    if (which == LSGB_FIELD_U || which == LSGB_FIELD_V || which == LSGB_FIELD_W) LSGB_TRY(materialize_velocity(s));
     void* keep = s->G;
     bool had = s->have_G;
     s->G = f;
@@ -951,7 +1027,8 @@ extern "C" int lsgb_solver_autotune(lsgb_solver* s, int reps, int* best_tile, fl
     int rc = LSGB_OK;
     for (int i = 0; i < n && rc == LSGB_OK; ++i) {
         StageArgs a = stage_args(s->p, s->g, s->lay);
-        a.u = s->u; a.v = s->v; a.w = s->w; a.sl = s->sl;
+        velocity_args(s, a);
+        a.sl = s->sl;
         a.err = err_flag(s);
         a.tile = c[i];
         a.Gn = s->G; a.Gin = s->G; a.Gout = s->A; a.stage = 1;
@@ -1159,6 +1236,8 @@ int batch_time_stage1(lsgb_batch* b, int reps, float* ms) {
 // them and long chunks win by their smaller halo overhead.)
 extern "C" int lsgb_batch_autotune(lsgb_batch* b, int reps) {
     LSGB_TRY(batch_ok(b));
+    for (lsgb_solver* s : b->inst)
+        if (s->vel_live) return fail(LSGB_ERR_UNSUPPORTED, "an instance has live velocity (replayed graphs need fixed fields)");
     for (lsgb_solver* s : b->inst) LSGB_TRY(lsgb_solver_autotune(s, reps, nullptr, nullptr));
     batch_drop_graph(b);
     if (b->prec != LSGB_PREC_F32 || b->inst.empty()) return LSGB_OK;
@@ -1195,8 +1274,10 @@ extern "C" int lsgb_batch_advance(lsgb_batch* b, int n_steps) {
     LSGB_TRY(batch_ok(b));
     if (n_steps < 0) return fail(LSGB_ERR_INVALID, "n_steps < 0");
     if (b->inst.empty() || n_steps == 0) return LSGB_OK;
-    for (lsgb_solver* s : b->inst)
+    for (lsgb_solver* s : b->inst) {
         if (!s->have_G || !s->have_vel) return fail(LSGB_ERR_STATE, "an instance has no fields");
+        if (s->vel_live) return fail(LSGB_ERR_UNSUPPORTED, "an instance has live velocity (replayed graphs need fixed fields)");
+    }
     int step, interval, reinit_on;
     LSGB_TRY(batch_uniform(b, &step, &interval, &reinit_on));
     // order the batch after any work queued on the instances' own streams
@@ -1599,6 +1680,7 @@ extern "C" int lsgb_adjoint_forward(lsgb_adjoint* a, int n_steps) {
     lsgb_solver* s = a->s;
     if (n_steps < 1) return fail(LSGB_ERR_INVALID, "n_steps must be >= 1");
     if (!s->have_G || !s->have_vel) return fail(LSGB_ERR_STATE, "fields not set");
+    if (s->vel_live) return fail(LSGB_ERR_UNSUPPORTED, "the adjoint needs a fixed velocity field (live velocity is on)");
     const int nseg = (n_steps + a->ckpt - 1) / a->ckpt;
     if (nseg > a->ckpt_slots) {
         LSGB_CUDA(cudaStreamSynchronize(s->st));

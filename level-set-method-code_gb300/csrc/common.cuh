@@ -85,6 +85,10 @@ struct StageArgs {
     int* err;                // nullable device error flag (bounded waits)
     int tile;                // tile-shape choice (0 = default; see lsgb_solver_set_tile)
     int drop_copies;         // test hook: the TMA-fed kernel issues no bulk copies (its waits time out)
+    // FP32 3D only: when set, the velocity is the deformation vortex evaluated
+    // in the stage kernel from these factor tables at time factor tf (u, v, w unused)
+    const float* defo;
+    float tf;
 };
 
 // HCR-2 pseudo-step arguments (handle path: r~ and flags recomputed from phi0).
@@ -109,6 +113,10 @@ cudaError_t launch_stage_f64(const StageArgs& a, cudaStream_t st);
 cudaError_t launch_stage_f32(const StageArgs& a, cudaStream_t st);
 // err: device flag set when a bounded in-kernel wait gives up (nullable: no TMA path)
 cudaError_t launch_stage3d_f32_tiled(const StageArgs& a, int* err, cudaStream_t st);
+// Grids on which launch_stage3d_f32_tiled evaluates the deformation vortex in
+// the stage kernel (StageArgs::defo): nx % 4 == 0 (bulk-tensor staging) and
+// fewer than 2^31 cells.
+bool stage3d_f32_fuses_deformation(const Geo& g);
 // The 2D FP32 stage (stage2d_f32.cu): row-pair tiles of 32 x 32 cells.
 cudaError_t launch_stage2d_f32_tiled(const StageArgs& a, cudaStream_t st);
 cudaError_t launch_reinit_f64(const ReinitArgs& a, cudaStream_t st);
@@ -155,8 +163,32 @@ cudaError_t launch_nonfinite(const Geo& g, const Lay& lay, const T* G, double* p
 // Synthetic fields: writes FP64 compact arrays G, u, v, w (w ignored in 2D).
 cudaError_t launch_synth(const Geo& g, const lsgb_synth& d, double dx, double dy, double dz,
                          double* G, double* u, double* v, double* w, cudaStream_t st);
-cudaError_t launch_deformation(const Geo& g, double dx, double dy, double dz, double t, double Tp,
-                               void* u, void* v, void* w, bool f32, cudaStream_t st);
+// Deformation vortex (synth.cu).  FP64: the reference's per-cell products at
+// time t.  FP32: time-independent factor tables (deformation_table_floats
+// floats, built once per grid) and the field at tf = cos(pi t / T).
+cudaError_t launch_deformation_f64(const Geo& g, double dx, double dy, double dz, double t, double Tp,
+                                   double* u, double* v, double* w, cudaStream_t st);
+size_t deformation_table_floats(const Geo& g);
+cudaError_t launch_deformation_tables_f32(const Geo& g, double dx, double dy, double dz, float* tab,
+                                          cudaStream_t st);
+cudaError_t launch_deformation_f32(const Geo& g, const float* tab, float tf, float* u, float* v, float* w,
+                                   cudaStream_t st);
+
+// Views into the FP32 factor tables: per axis [sin^2(pi x_i)], [sin(2 pi x_i)],
+// n + 1 entries each (the last 0, so a plane pair may read one past nz).
+struct DeformTables {
+    const float *sqx, *s2x, *sqy, *s2y, *sqz, *s2z;
+};
+__host__ __device__ __forceinline__ DeformTables deform_tables(const Geo& g, const float* tab) {
+    DeformTables d;
+    d.sqx = tab;
+    d.s2x = d.sqx + g.nx + 1;
+    d.sqy = d.s2x + g.nx + 1;
+    d.s2y = d.sqy + g.ny + 1;
+    d.sqz = d.s2y + g.ny + 1;
+    d.s2z = d.sqz + g.nz + 1;
+    return d;
+}
 cudaError_t launch_scale3(long long n, double s, double* u, double* v, double* w, cudaStream_t st);
 
 // Allocation-free interior G < 0 count (noalloc.cu); writes the host double

@@ -84,6 +84,7 @@ struct Coef {
     float inv_dx, inv_dy, inv_dz, inv_2dx, inv_2dy, inv_2dz, s_l, eps, dt;
     int zc;  // z-chunk length (even, <= MAXZC): tile shape chosen per grid by the autotuner
     int drop;  // test hook: issue no bulk copies, so every wait runs into its limit
+    float tf;  // deformation vortex time factor cos(pi t / T) (DEFO kernels)
 };
 
 // ---- TMA / mbarrier primitives (PTX) ----------------------------------------
@@ -193,12 +194,17 @@ __device__ __forceinline__ void zcol_step(ZCol& z, float zn0, float zn1, float2&
 // TMA = bulk tensor copies of the CTA's tile (one thread issues, mbarriers
 // signal arrival); otherwise every thread copies its own four cells with
 // cp.async and waits for its own copies.
-template <int STAGE, bool TMA, typename IDX>
+// DEFO: the velocity is the deformation vortex (computeDeformationVelocity,
+// Local_code/level-set_MPI_3D/include/initial_conditions.h:232-247) formed
+// from the factor tables defo at time factor c.tf -- a per-row factor of the
+// thread's two rows times a per-plane factor -- instead of read from u, v, w
+// (the same FP32 products as launch_deformation_f32 writes).
+template <int STAGE, bool TMA, typename IDX, bool DEFO>
 __global__ void __launch_bounds__(NT, 2)
 stage3d_f32_col2(Geo g, const float* __restrict__ Gin, const float* __restrict__ Gn, float* __restrict__ Gout,
                  const float* __restrict__ u, const float* __restrict__ v, const float* __restrict__ w,
                  const float* __restrict__ sl, Coef c, const __grid_constant__ TmaMaps tm, int* __restrict__ err,
-                 int hsl /* sl != nullptr */) {
+                 int hsl /* sl != nullptr */, const float* __restrict__ defo) {
     __shared__ float2 P2[2][BPH][PW];
     __shared__ float2 FL[BNFX], FR[BNFX];  // x faces [BY][TX+1]
     __shared__ IDX zoff[MAXZC + 10];
@@ -260,11 +266,13 @@ stage3d_f32_col2(Geo g, const float* __restrict__ Gin, const float* __restrict__
     auto issue = [&](int it, int s) {
         const int kz = z0 + 2 * it;
         float* base = stg + s * NFIELD * BFTILE;
-        const uint32_t nf = 3 + (STAGE > 1 ? 1 : 0) + (has_sl ? 1 : 0);
+        const uint32_t nf = (DEFO ? 0 : 3) + (STAGE > 1 ? 1 : 0) + (has_sl ? 1 : 0);
         mbar_expect_tx(&mbar[s], nf * BFTILE * 4);
-        tma_load_3d(base + 0 * BFTILE, &tm.m[0], i0, j0, kz, &mbar[s]);
-        tma_load_3d(base + 1 * BFTILE, &tm.m[1], i0, j0, kz, &mbar[s]);
-        tma_load_3d(base + 2 * BFTILE, &tm.m[2], i0, j0, kz, &mbar[s]);
+        if (!DEFO) {
+            tma_load_3d(base + 0 * BFTILE, &tm.m[0], i0, j0, kz, &mbar[s]);
+            tma_load_3d(base + 1 * BFTILE, &tm.m[1], i0, j0, kz, &mbar[s]);
+            tma_load_3d(base + 2 * BFTILE, &tm.m[2], i0, j0, kz, &mbar[s]);
+        }
         if (STAGE > 1) tma_load_3d(base + 3 * BFTILE, &tm.m[3], i0, j0, kz, &mbar[s]);
         if (has_sl) tma_load_3d(base + 4 * BFTILE, &tm.m[4], i0, j0, kz, &mbar[s]);
     };
@@ -278,9 +286,11 @@ stage3d_f32_col2(Geo g, const float* __restrict__ Gin, const float* __restrict__
             for (int p = 0; p < 2; ++p) {
                 const IDX o = zf[p] + (h ? colB : colA);
                 float* d = base + h * TX + p * BY * TX;
-                cp_async4(d, u + o);
-                cp_async4(d + BFTILE, v + o);
-                cp_async4(d + 2 * BFTILE, w + o);
+                if (!DEFO) {
+                    cp_async4(d, u + o);
+                    cp_async4(d + BFTILE, v + o);
+                    cp_async4(d + 2 * BFTILE, w + o);
+                }
                 if (STAGE > 1) cp_async4(d + 3 * BFTILE, Gn + o);
                 if (has_sl) cp_async4(d + 4 * BFTILE, sl + o);
             }
@@ -297,6 +307,19 @@ stage3d_f32_col2(Geo g, const float* __restrict__ Gin, const float* __restrict__
             if (it < niter) fetch(it, it);
             cp_async_commit();  // one group per iteration, empty ones included
         }
+
+    // deformation vortex: per-row factors of rows A and B (constant over the march)
+    float dfu[2] = {0.0f, 0.0f}, dfv[2] = {0.0f, 0.0f}, dfw[2] = {0.0f, 0.0f};
+    if (DEFO) {
+        const DeformTables d = deform_tables(g, defo);
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int jr = wrapg(j0 + ra + h, g.ny, g.bcy);
+            dfu[h] = 2.0f * __ldg(d.sqx + gxc) * __ldg(d.s2y + jr) * c.tf;
+            dfv[h] = -__ldg(d.s2x + gxc) * __ldg(d.sqy + jr) * c.tf;
+            dfw[h] = -__ldg(d.s2x + gxc) * __ldg(d.s2y + jr) * c.tf;
+        }
+    }
 
     ZCol za, zb;
     zcol_init(za, Gin, zoff, colA);
@@ -405,9 +428,19 @@ stage3d_f32_col2(Geo g, const float* __restrict__ Gin, const float* __restrict__
             const IDX o = zo[0] + (h ? colB : colA);
             const float* f = stg + cs * NFIELD * BFTILE + (ra + h) * TX + tx;
             constexpr int pl = BY * TX;
-            const float2 uu = make_float2(f[0], f[pl]);
-            const float2 vv = make_float2(f[BFTILE], f[BFTILE + pl]);
-            const float2 ww = make_float2(f[2 * BFTILE], f[2 * BFTILE + pl]);
+            float2 uu, vv, ww;
+            if (DEFO) {
+                const DeformTables d = deform_tables(g, defo);
+                const float2 zs2 = make_float2(__ldg(d.s2z + k), __ldg(d.s2z + k + 1));  // entry nz is 0
+                const float2 zsq = make_float2(__ldg(d.sqz + k), __ldg(d.sqz + k + 1));
+                uu = mul2(c2(dfu[h]), zs2);
+                vv = mul2(c2(dfv[h]), zs2);
+                ww = mul2(c2(dfw[h]), zsq);
+            } else {
+                uu = make_float2(f[0], f[pl]);
+                vv = make_float2(f[BFTILE], f[BFTILE + pl]);
+                ww = make_float2(f[2 * BFTILE], f[2 * BFTILE + pl]);
+            }
             const float2 gn = STAGE > 1 ? make_float2(f[3 * BFTILE], f[3 * BFTILE + pl]) : c2(0.0f);
             const float2 s_l = has_sl ? make_float2(f[4 * BFTILE], f[4 * BFTILE + pl]) : c2(c.s_l);
             const int xf = (ra + h) * (TX + 1) + tx;
@@ -457,26 +490,26 @@ bool encode_field(CUtensorMap* m, const float* ptr, const Geo& g, int rows, int 
               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-template <int STAGE, bool TMA, typename IDX>
+template <int STAGE, bool TMA, typename IDX, bool DEFO>
 cudaError_t launch_one(const StageArgs& a, const Coef& c, const TmaMaps& tm, int* err, cudaStream_t st) {
     const dim3 block(TX, TY, 1);
     const dim3 grid((a.g.nx + TX - 1) / TX, (a.g.ny + BY - 1) / BY, (a.g.nz + c.zc - 1) / c.zc);
     const size_t dyn = (size_t)NSTAGE * NFIELD * BFTILE * sizeof(float);
-    auto kern = stage3d_f32_col2<STAGE, TMA, IDX>;
+    auto kern = stage3d_f32_col2<STAGE, TMA, IDX, DEFO>;
     // once per instantiation (thread-safe initialisation of a local static)
     static const cudaError_t attr = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
     if (attr != cudaSuccess) return attr;
     kern<<<grid, block, dyn, st>>>(a.g, (const float*)a.Gin, (const float*)a.Gn, (float*)a.Gout,
                                     (const float*)a.u, (const float*)a.v, (const float*)a.w,
-                                    (const float*)a.sl, c, tm, err, a.sl != nullptr);
+                                    (const float*)a.sl, c, tm, err, a.sl != nullptr, a.defo);
     return cudaGetLastError();
 }
 
-template <bool TMA, typename IDX>
+template <bool TMA, typename IDX, bool DEFO = false>
 cudaError_t launch_stage(const StageArgs& a, const Coef& c, const TmaMaps& tm, int* err, cudaStream_t st) {
-    if (a.stage == 1) return launch_one<1, TMA, IDX>(a, c, tm, err, st);
-    if (a.stage == 2) return launch_one<2, TMA, IDX>(a, c, tm, err, st);
-    return launch_one<3, TMA, IDX>(a, c, tm, err, st);
+    if (a.stage == 1) return launch_one<1, TMA, IDX, DEFO>(a, c, tm, err, st);
+    if (a.stage == 2) return launch_one<2, TMA, IDX, DEFO>(a, c, tm, err, st);
+    return launch_one<3, TMA, IDX, DEFO>(a, c, tm, err, st);
 }
 
 // z-chunk of the default tile shape: the longest chunk that still gives every
@@ -499,6 +532,10 @@ int default_zc(const Geo& g) {
 
 }  // namespace
 
+bool stage3d_f32_fuses_deformation(const Geo& g) {
+    return g.dim == 3 && (g.nx % 4) == 0 && g.cells() < (1LL << 31) - 1;
+}
+
 cudaError_t launch_stage3d_f32_tiled(const StageArgs& a, int* err, cudaStream_t st) {
     Coef c;
     // face values carry a factor 6 (see face())
@@ -513,16 +550,24 @@ cudaError_t launch_stage3d_f32_tiled(const StageArgs& a, int* err, cudaStream_t 
     c.dt = (float)a.dt;
     c.zc = (a.tile == 16 || a.tile == 32 || a.tile == MAXZC) ? a.tile : default_zc(a.g);
     c.drop = a.drop_copies;
+    c.tf = a.tf;
     TmaMaps tm;
     std::memset(&tm, 0, sizeof(tm));
     // bulk tensor copies need 16-byte row pitch and an error flag to report into
     bool tma = err != nullptr && (a.g.nx % 4) == 0;
-    const void* fields[NFIELD] = {a.u, a.v, a.w, a.stage > 1 ? a.Gn : nullptr, a.sl};
+    const bool defo = a.defo != nullptr;
+    const void* fields[NFIELD] = {defo ? nullptr : a.u, defo ? nullptr : a.v, defo ? nullptr : a.w,
+                                  a.stage > 1 ? a.Gn : nullptr, a.sl};
     for (int f = 0; f < NFIELD && tma; ++f)
         if (fields[f] && !encode_field(&tm.m[f], (const float*)fields[f], a.g, BY, 2)) tma = false;
     const bool small = a.g.cells() < (1LL << 31) - 1;
     cudaError_t e;
-    if (tma) e = small ? launch_stage<true, int>(a, c, tm, err, st) : launch_stage<true, long long>(a, c, tm, err, st);
+    if (defo) {
+        // the fused velocity exists in the bulk-tensor form with 32-bit offsets
+        // (stage3d_f32_fuses_deformation); the caller fills u, v, w otherwise
+        if (!tma || !small) return cudaErrorNotSupported;
+        e = launch_stage<true, int, true>(a, c, tm, err, st);
+    } else if (tma) e = small ? launch_stage<true, int>(a, c, tm, err, st) : launch_stage<true, long long>(a, c, tm, err, st);
     else e = small ? launch_stage<false, int>(a, c, tm, err, st) : launch_stage<false, long long>(a, c, tm, err, st);
     count_launches(1);
     return e;

@@ -90,15 +90,13 @@ __global__ void scale3_kernel(long long n, double s, double* u, double* v, doubl
 // initial_conditions.h:232-247) at the cell centres x_i = i * dx, written
 // straight into the compact velocity arrays of the solver.  The field is a
 // product of per-axis factors, so the sines are evaluated once per axis
-// index (deformation_factors_kernel) and every cell forms the reference's
-// products from them in its order.  The FP64 solver gets exactly the values
-// of evaluating the sines at every cell; the FP32 solver forms the products
-// in FP32 from the factors rounded to FP32 (within a few FP32 ulps of the
-// rounded FP64 product).
-//   tab = [sin(pi x_i)][sin(2 pi x_i)] [.. y ..] [.. z ..] [cos(pi t / T)],
-//   the same table in FP64 and in FP32.
-__global__ void deformation_factors_kernel(Geo g, double dx, double dy, double dz, double t, double Tp,
-                                           double* __restrict__ tab, float* __restrict__ tabf) {
+// index and every cell only forms products.
+//
+// FP64: tab = [sin(pi x_i)][sin(2 pi x_i)] [.. y ..] [.. z ..] [cos(pi t / T)]
+// per call, and each cell forms the reference's products in its order:
+// exactly the values of evaluating the sines at every cell.
+__global__ void deformation_factors_f64_kernel(Geo g, double dx, double dy, double dz, double t, double Tp,
+                                               double* __restrict__ tab) {
     const double pi = 3.14159265358979323846;
     const int n[3] = {g.nx, g.ny, g.nz};
     const double h[3] = {dx, dy, dz};
@@ -106,67 +104,112 @@ __global__ void deformation_factors_kernel(Geo g, double dx, double dy, double d
     for (int a = 0; a < 3; ++a) {
         for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n[a]; i += gridDim.x * blockDim.x) {
             const double x = i * h[a];
-            const double s1 = sin(pi * x), s2 = sin(2.0 * pi * x);
-            tab[base + i] = s1;
-            tab[base + n[a] + i] = s2;
-            tabf[base + i] = (float)s1;
-            tabf[base + n[a] + i] = (float)s2;
+            tab[base + i] = sin(pi * x);
+            tab[base + n[a] + i] = sin(2.0 * pi * x);
         }
         base += 2 * n[a];
     }
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        tab[base] = cos(pi * t / Tp);
-        tabf[base] = (float)tab[base];
-    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) tab[base] = cos(pi * t / Tp);
 }
 
 // One thread per cell of a row segment; rows (j, k) strided over gridDim.y.
-// T = the solver's precision, the arithmetic of the products.
-template <typename T>
-__global__ void deformation_kernel(Geo g, const T* __restrict__ tab, T* __restrict__ u, T* __restrict__ v,
-                                   T* __restrict__ w) {
-    const T* s1x = tab;
-    const T* s2x = s1x + g.nx;
-    const T* s1y = s2x + g.nx;
-    const T* s2y = s1y + g.ny;
-    const T* s1z = s2y + g.ny;
-    const T* s2z = s1z + g.nz;
-    const T tf = s2z[g.nz];
+__global__ void deformation_f64_kernel(Geo g, const double* __restrict__ tab, double* __restrict__ u,
+                                       double* __restrict__ v, double* __restrict__ w) {
+    const double* s1x = tab;
+    const double* s2x = s1x + g.nx;
+    const double* s1y = s2x + g.nx;
+    const double* s2y = s1y + g.ny;
+    const double* s1z = s2y + g.ny;
+    const double* s2z = s1z + g.nz;
+    const double tf = s2z[g.nz];
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= g.nx) return;
-    const T spx = s1x[i], s2px = s2x[i];
+    const double spx = s1x[i], s2px = s2x[i];
     const long long rows = (long long)g.ny * g.nz;
     for (long long row = blockIdx.y; row < rows; row += gridDim.y) {
         const int k = (int)(row / g.ny);
         const int j = (int)(row - (long long)k * g.ny);
-        const T spy = s1y[j], s2py = s2y[j], spz = s1z[k], s2pz = s2z[k];
+        const double spy = s1y[j], s2py = s2y[j], spz = s1z[k], s2pz = s2z[k];
         const long long e = row * g.nx + i;
-        u[e] = (T)2 * spx * spx * s2py * s2pz * tf;
+        u[e] = 2.0 * spx * spx * s2py * s2pz * tf;
         v[e] = -s2px * spy * spy * s2pz * tf;
         w[e] = -s2px * s2py * spz * spz * tf;
     }
 }
 
+// FP32: time-independent tables, per axis [sin^2(pi x_i)] and
+// [sin(2 pi x_i)] (n + 1 entries each, the last 0), computed in FP64 and
+// rounded once.  With tf = cos(pi t / T) rounded to FP32 the cell values are
+//   u = (2 sq_x s2_y tf) s2_z,  v = (-s2_x sq_y tf) s2_z,  w = (-s2_x s2_y tf) sq_z,
+// products in FP32 in this order -- the order the fused stage kernel uses
+// (per-row factor times per-plane factor), so both give the same bits.
+__global__ void deformation_tables_f32_kernel(Geo g, double dx, double dy, double dz, float* __restrict__ tab) {
+    const double pi = 3.14159265358979323846;
+    const int n[3] = {g.nx, g.ny, g.nz};
+    const double h[3] = {dx, dy, dz};
+    int base = 0;
+    for (int a = 0; a < 3; ++a) {
+        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i <= n[a]; i += gridDim.x * blockDim.x) {
+            const double x = i * h[a];
+            const double s1 = sin(pi * x);
+            tab[base + i] = i < n[a] ? (float)(s1 * s1) : 0.0f;
+            tab[base + n[a] + 1 + i] = i < n[a] ? (float)sin(2.0 * pi * x) : 0.0f;
+        }
+        base += 2 * (n[a] + 1);
+    }
+}
+
+__global__ void deformation_f32_kernel(Geo g, const float* __restrict__ tab, float tf, float* __restrict__ u,
+                                       float* __restrict__ v, float* __restrict__ w) {
+    const DeformTables d = deform_tables(g, tab);
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= g.nx) return;
+    const long long rows = (long long)g.ny * g.nz;
+    for (long long row = blockIdx.y; row < rows; row += gridDim.y) {
+        const int k = (int)(row / g.ny);
+        const int j = (int)(row - (long long)k * g.ny);
+        const long long e = row * g.nx + i;
+        u[e] = (2.0f * d.sqx[i] * d.s2y[j] * tf) * d.s2z[k];
+        v[e] = (-d.s2x[i] * d.sqy[j] * tf) * d.s2z[k];
+        w[e] = (-d.s2x[i] * d.s2y[j] * tf) * d.sqz[k];
+    }
+}
+
+dim3 deformation_grid(const Geo& g) {
+    const long long rows = (long long)g.ny * g.nz;
+    return dim3((g.nx + 127) / 128, (unsigned)(rows < 65535 ? rows : 65535));
+}
+
 }  // namespace
 
-cudaError_t launch_deformation(const Geo& g, double dx, double dy, double dz, double t, double Tp,
-                               void* u, void* v, void* w, bool f32, cudaStream_t st) {
+cudaError_t launch_deformation_f64(const Geo& g, double dx, double dy, double dz, double t, double Tp,
+                                   double* u, double* v, double* w, cudaStream_t st) {
     double* tab = nullptr;
     const size_t ntab = 2 * ((size_t)g.nx + g.ny + g.nz) + 1;
-    cudaError_t e = cudaMallocAsync((void**)&tab, ntab * (sizeof(double) + sizeof(float)), st);
+    cudaError_t e = cudaMallocAsync((void**)&tab, ntab * sizeof(double), st);
     if (e != cudaSuccess) return e;
-    float* tabf = (float*)(tab + ntab);
-    deformation_factors_kernel<<<8, 256, 0, st>>>(g, dx, dy, dz, t, Tp, tab, tabf);
-    const long long rows = (long long)g.ny * g.nz;
-    const dim3 block(128), grid((g.nx + 127) / 128, (unsigned)(rows < 65535 ? rows : 65535));
-    if (f32)
-        deformation_kernel<float><<<grid, block, 0, st>>>(g, tabf, (float*)u, (float*)v, (float*)w);
-    else
-        deformation_kernel<double><<<grid, block, 0, st>>>(g, tab, (double*)u, (double*)v, (double*)w);
+    deformation_factors_f64_kernel<<<8, 256, 0, st>>>(g, dx, dy, dz, t, Tp, tab);
+    deformation_f64_kernel<<<deformation_grid(g), 128, 0, st>>>(g, tab, u, v, w);
     count_launches(2);
     e = cudaGetLastError();
     const cudaError_t f = cudaFreeAsync(tab, st);
     return e != cudaSuccess ? e : f;
+}
+
+size_t deformation_table_floats(const Geo& g) { return 2 * ((size_t)g.nx + g.ny + g.nz + 3); }
+
+cudaError_t launch_deformation_tables_f32(const Geo& g, double dx, double dy, double dz, float* tab,
+                                          cudaStream_t st) {
+    deformation_tables_f32_kernel<<<8, 256, 0, st>>>(g, dx, dy, dz, tab);
+    count_launches(1);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_deformation_f32(const Geo& g, const float* tab, float tf, float* u, float* v, float* w,
+                                   cudaStream_t st) {
+    deformation_f32_kernel<<<deformation_grid(g), 128, 0, st>>>(g, tab, tf, u, v, w);
+    count_launches(1);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_synth(const Geo& g, const lsgb_synth& d, double dx, double dy, double dz,

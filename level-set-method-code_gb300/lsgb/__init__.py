@@ -315,7 +315,22 @@ def _set_velocity_deformation(self, t: float, T: float):
     _check(lib().lsgb_solver_set_velocity_deformation(self._h, C.c_double(t), C.c_double(T)))
 
 
+def _set_velocity_deformation_live(self, t: float, T: float):
+    """Live deformation vortex: every step of advance() uses the vortex at the
+    handle's time (starting at t, advancing by dt per step)."""
+    _check(lib().lsgb_solver_set_velocity_deformation_live(self._h, C.c_double(t), C.c_double(T)))
+
+
+def _time(self) -> float:
+    """Live-mode time: the t of the next step."""
+    t = C.c_double()
+    _check(lib().lsgb_solver_get_time(self._h, C.byref(t)))
+    return t.value
+
+
 Solver.set_velocity_deformation = _set_velocity_deformation
+Solver.set_velocity_deformation_live = _set_velocity_deformation_live
+Solver.time = _time
 
 
 def _get_field(self, which: str, layout: str = "ghosted", out=None):
