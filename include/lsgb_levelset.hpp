@@ -235,6 +235,17 @@ class Solver {
         check(lsgb_solver_compute_dt(h_, cfl, &dt));
         return dt;
     }
+    // The deformation test's per-step velocity (updateDeformationVelocity before
+    // every rk3TimeStep3D, src/main.cpp:297-299) kept inside advance(): the
+    // vortex at the handle's time, which starts at t and advances by dt a step.
+    void deformationVelocityLive(double t, double t_final) {
+        check(lsgb_solver_set_velocity_deformation_live(h_, t, t_final));
+    }
+    double time() const {
+        double t = 0.0;
+        check(lsgb_solver_get_time(h_, &t));
+        return t;
+    }
     lsgb_solver* handle() { return h_; }
 
   private:
