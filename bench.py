@@ -544,6 +544,19 @@ def run_ours(args, dist: Dist):
             s32.get_field(name, out=t.numpy())
         s32.run_host(host[0].numpy(), host[1].numpy(), host[2].numpy(), host[3].numpy(), args.e2e_rk_steps,
                      host[4].numpy())  # warm
+        # the host link's rate right now (one field each way): the GPU shares
+        # its host's memory and link with a neighbour GPU, so it varies by box
+        link = {}
+        probe = torch.empty(shape, dtype=torch.float64, device="cuda")
+        with torch.cuda.stream(stream):
+            for name, dst, src in (("h2d_gbs", probe, host[0]), ("d2h_gbs", host[4], probe)):
+                e = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+                e[0].record(stream)
+                dst.copy_(src, non_blocking=True)
+                e[1].record(stream)
+                e[1].synchronize()
+                link[name] = probe.numel() * 8 / (e[0].elapsed_time(e[1]) * 1e-3) / 1e9
+        del probe
         torch.cuda.synchronize()
         dist.barrier()
         ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
@@ -559,7 +572,7 @@ def run_ours(args, dist: Dist):
                "unit": "Gcell-updates/s", "h2d_bytes_per_step": 4 * shape[0] ** 3 * 8,
                "d2h_bytes_per_step": shape[0] ** 3 * 8,
                "call": "lsgb_solver_run_host (ghosted FP64 host arrays G,u,v,w in, G out)",
-               "rk3_steps_per_call": args.e2e_rk_steps}
+               "rk3_steps_per_call": args.e2e_rk_steps, "host_link": link}
         del host
 
     # --- plain FP64 form beside it, and the FP32-vs-FP64 error after the same steps ---
