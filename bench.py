@@ -59,6 +59,7 @@ def parse():
     ap.add_argument("--sample-steps", type=int, default=10, help="steps of the sample-surface frequency sweep (0 = skip)")
     ap.add_argument("--plane-n", type=int, default=4096, help="grid of the 2D stage-kernel leg (0 = skip)")
     ap.add_argument("--deform-steps", type=int, default=20, help="RK3 steps of the live deformation leg (0 = skip)")
+    ap.add_argument("--no-config1", dest="config1", action="store_false", help="skip the 128^2 configuration-1 leg")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--json-out", default=None)
     return ap.parse_args()
@@ -363,6 +364,48 @@ def measure_plane(torch, lsgb, syn, n: int, steps: int, peak_gbs: float, dist: D
             "workload": f"{n}^2 periodic plane, config-4 2D instance 0 construction, FP32-bulk, reinit every 5"}
 
 
+def measure_config1(torch, lsgb, syn, dist: Dist, cpu: bool):
+    """Configuration 1, the reference's CPU-runnable case: 2D 128^2 periodic,
+    circle r = 0.25, u = (1, 0), S_L = 0.1, dt = 0.5 dx / 1.1, 400 RK3 steps,
+    HCR-2 every 10 steps x 5 pseudo-steps, plain FP64 (bit-exact to the
+    reference's run: tests/test_gpu_parity.py::test_golden_config1).  The
+    fields stay resident; the 400 steps are timed with CUDA events on the
+    solver's stream.  The CPU figure is the oracle port of the same run."""
+    n, steps = 128, 400
+    G, u, v, _ = syn.host_fields(syn.config1(n))
+    dt = 0.5 * (1.0 / n) / 1.1
+    p = lsgb.params(2, n, n, 1, s_l=0.1, dt=dt, enable_reinit=True, reinit_interval=10, reinit_iterations=5)
+    stream = torch.cuda.Stream()
+    times = []
+    for _ in range(2):  # the first run warms up
+        with lsgb.Solver(p, "f64") as s:
+            s.set_stream(stream)
+            s.set_fields(G, u, v)
+            torch.cuda.synchronize()
+            ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+            with torch.cuda.stream(stream):
+                ev[0].record(stream)
+                s.advance(steps)
+                ev[1].record(stream)
+            torch.cuda.synchronize()
+            times.append(ev[0].elapsed_time(ev[1]))
+    ms = dist.max(times[-1])
+    out = {"value": dist.world * n * n * steps / (ms * 1e-3) / 1e9, "unit": "Gcell-updates/s", "ms": ms,
+           "rk3_steps": steps, "dtype": "f64",
+           "workload": "config1 128^2 periodic circle, u = (1, 0), S_L = 0.1, CFL 0.5, HCR-2 every 10 x 5"}
+    if cpu:
+        from oracle import Oracle, Problem
+        pb = Problem(nx=n, ny=n, dim=2, s_l=0.1, dt=dt, enable_reinit=True, reinit_interval=10,
+                     reinit_iterations=5, periodic_y=True)
+        a = time.perf_counter()
+        Oracle("port").run(pb, steps, G, u, v)
+        el = time.perf_counter() - a
+        out["cpu_baseline"] = {"value": n * n * steps / el / 1e9, "unit": "Gcell-updates/s",
+                               "cores": int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1)),
+                               "kind": "port", "sample": f"the whole run, {el:.2f} s"}
+    return out
+
+
 def measure_deformation(torch, lsgb, syn, n: int, steps: int, dist: Dist):
     """The reference's time-dependent case at n^3, FP32: the deformation
     vortex recomputed every step (Local_code/level-set_MPI_3D/src/main.cpp:
@@ -610,6 +653,11 @@ def run_ours(args, dist: Dist):
     if args.batch_steps > 0:
         batched = measure_batched(torch, lsgb, syn, args.batch_steps, dist)
 
+    config1 = None
+    if args.config1:
+        config1 = measure_config1(torch, lsgb, syn, dist, cpu=not args.no_cpu_baseline and dist.rank == 0
+                                  and dist.world == 1)
+
     deform = None
     if args.deform_steps > 0:
         deform = measure_deformation(torch, lsgb, syn, n, args.deform_steps, dist)
@@ -654,6 +702,7 @@ def run_ours(args, dist: Dist):
             "fp64": fp64,
             "precision_vs_fp64": prec,
             "reinit_avg_launch_ms": re_ms / max(re_n, 1),
+            "config1": config1,
             "plane2d": plane,
             "deformation": deform,
             "batched": batched,

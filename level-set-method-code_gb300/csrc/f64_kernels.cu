@@ -339,7 +339,26 @@ __global__ void unpack_kernel(Geo g, const T* __restrict__ src, double* __restri
 inline dim3 cell_grid(const Geo& g, dim3 b) {
     return dim3((g.nx + b.x - 1) / b.x, (g.ny + b.y - 1) / b.y, (g.nz + b.z - 1) / b.z);
 }
-inline dim3 cell_block(const Geo& g) { return g.dim == 3 ? dim3(32, 4, 2) : dim3(32, 8, 1); }
+// One thread per cell, 32 x 8 (2D) or 32 x 4 x 2 (3D) blocks.  A grid too
+// small to give every SM two blocks gets lower blocks instead, down to single
+// rows: the FP64 work per cell is a long dependent chain (IEEE divisions), so
+// on small grids the time is set by how many SMs share it.  The per-cell
+// arithmetic does not depend on the block shape.
+inline dim3 cell_block(const Geo& g) {
+    static const int sms = [] {
+        int dev = 0, n = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        return n > 0 ? n : 1;
+    }();
+    dim3 b = g.dim == 3 ? dim3(32, 4, 2) : dim3(32, 8, 1);
+    while (b.y * b.z > 1) {
+        const dim3 gr = cell_grid(g, b);
+        if ((long long)gr.x * gr.y * gr.z >= 2LL * sms) break;
+        if (b.z > 1) b.z /= 2; else b.y /= 2;
+    }
+    return b;
+}
 
 inline unsigned flat_blocks(long long n) {
     long long b = (n + 255) / 256;
