@@ -587,18 +587,22 @@ def run_ours(args, dist: Dist):
             s32.get_field(name, out=t.numpy())
         s32.run_host(host[0].numpy(), host[1].numpy(), host[2].numpy(), host[3].numpy(), args.e2e_rk_steps,
                      host[4].numpy())  # warm
-        # the host link's rate right now (one field each way): the GPU shares
-        # its host's memory and link with a neighbour GPU, so it varies by box
+        # the host link's rate right now (one field each way, median of three
+        # copies): it varies by box and sets the end-to-end figure's copy time
         link = {}
         probe = torch.empty(shape, dtype=torch.float64, device="cuda")
         with torch.cuda.stream(stream):
             for name, dst, src in (("h2d_gbs", probe, host[0]), ("d2h_gbs", host[4], probe)):
-                e = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
-                e[0].record(stream)
-                dst.copy_(src, non_blocking=True)
-                e[1].record(stream)
-                e[1].synchronize()
-                link[name] = probe.numel() * 8 / (e[0].elapsed_time(e[1]) * 1e-3) / 1e9
+                rates = []
+                for _ in range(3):
+                    e = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+                    e[0].record(stream)
+                    dst.copy_(src, non_blocking=True)
+                    e[1].record(stream)
+                    e[1].synchronize()
+                    rates.append(probe.numel() * 8 / (e[0].elapsed_time(e[1]) * 1e-3) / 1e9)
+                link[name] = statistics.median(rates)
+                link[name + "_samples"] = rates
         del probe
         torch.cuda.synchronize()
         dist.barrier()
