@@ -16,7 +16,8 @@ and reductions); the plain FP64 form is measured beside it.
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
 --impl reference times the reference's algorithm on the host CPU cores
-(the oracle) on a bounded slab of the same workload.
+(the oracle port under oracle/, pinned bit-exact to the reference's own
+sources) on a bounded slab of the same workload.
 Multi-GPU runs are independent replicas (the path is not sharded); rank 0
 prints the aggregate.
 """
