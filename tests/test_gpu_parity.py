@@ -156,6 +156,48 @@ def test_deformation_64_matches_reference_log(cuda, lsgb_mod, port):
     assert l2 == pytest.approx(gold["l2"], rel=1e-9)
 
 
+@pytest.mark.parametrize("prec", ["f64", "f32"])
+def test_deformation_64_live_velocity(cuda, lsgb_mod, port, prec):
+    """The same case with the velocity in live mode (the handle recomputes the
+    vortex every step; inside the stage kernel for FP32 on this grid).  FP64
+    reproduces the log and the port's L2 as the explicit loop does; FP32 stays
+    within 1e-3 of the log's L2 and within 5 cells of its final volume."""
+    import ctypes as C
+    from oracle import build_port
+    L = C.CDLL(build_port())
+    n, T, dt = 64, 1.5, 1e-3
+    pb = Problem(nx=n, ny=n, nz=n, dim=3, dx=1 / 63, dy=1 / 63, dz=1 / 63, dt=dt)
+    G0 = np.zeros(pb.shape)
+    L.orc3d_sphere(C.byref(pb.c()), C.c_double(0.35), C.c_double(0.35), C.c_double(0.35),
+                   C.c_double(0.15), G0.ctypes.data_as(C.POINTER(C.c_double)))
+    G0 = port.apply_bc(pb, G0)
+    with lsgb_mod.Solver(lsgb_params(lsgb_mod, pb), prec) as s:
+        s.set_fields(G=G0)
+        v0, _ = s.volume()
+        s.set_velocity_deformation_live(0.0, T)
+        s.advance(1400)
+        steps = 1400
+        t = s.time()
+        while t < T and steps < int(T / 1e-3) + 100:  # the reference's loop with its final-step clip
+            if t + dt > T:
+                dt = T - t
+                s.set_dt(dt)
+            s.advance(1)
+            t = s.time()
+            steps += 1
+        v1, _ = s.volume()
+        l2 = s.l2_error(G0)
+    gold = json.load(open(os.path.join(GOLD, "golden_scalars.json")))["deformation_64"]
+    assert steps == gold["log_steps"]
+    if prec == "f64":
+        assert f"{l2:.6e}" == gold["log_l2"]
+        assert f"{v0:.6f}" == gold["log_volume_initial"] and f"{v1:.6f}" == gold["log_volume_final"]
+        assert l2 == pytest.approx(gold["l2"], rel=1e-9)
+    else:
+        assert l2 == pytest.approx(gold["l2"], rel=1e-3)
+        assert abs(v1 - gold["volume_final"]) <= 5 * (1 / 63) ** 3
+
+
 def zalesak_gpu(lsgb, n):
     """The reference's Zalesak loop on the FP64 handle: returns the final
     ghosted G, its L2 error against G0, the final area and cell count, the
