@@ -355,7 +355,7 @@ LSGB_API int lsgb_adjoint_get_grad(lsgb_adjoint* a, int which, double* out, int 
 LSGB_API int lsgb_solver_set_velocity_deformation(lsgb_solver* s, double t, double T);
 /* Live mode: from now on every step uses the vortex at the handle's time,
  * which starts at t and advances by dt after each step -- the reference's
- * loop (src/main.cpp:291-317: velocity at current_time, RK3 step, reinit,
+ * loop (src/main.cpp:291-316: velocity at current_time, RK3 step, reinit,
  * current_time += dt) inside one lsgb_solver_advance.  FP32 3D handles with
  * nx % 4 == 0 and fewer than 2^31 cells evaluate the vortex inside the stage
  * kernel (no u, v, w traffic); other handles refill u, v, w before each step.

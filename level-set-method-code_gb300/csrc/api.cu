@@ -735,7 +735,7 @@ extern "C" int lsgb_solver_advance(lsgb_solver* s, int n_steps) {
         if (s->p.enable_reinit && s->step > 0 && s->step % s->p.reinit_interval == 0)
             LSGB_TRY(reinit(s));
         s->step++;
-        if (s->vel_live) s->vel_t += s->p.dt;  // current_time += params.dt (src/main.cpp:316)
+        if (s->vel_live) s->vel_t += s->p.dt;  // current_time += params.dt (src/main.cpp:315)
     }
     return LSGB_OK;
 }

@@ -1,7 +1,7 @@
 """Live deformation velocity (needs a GB300).
 
 lsgb_solver_set_velocity_deformation_live runs the reference's time loop
-(Local_code/level-set_MPI_3D/src/main.cpp:291-317: velocity at current_time,
+(Local_code/level-set_MPI_3D/src/main.cpp:291-316: velocity at current_time,
 RK3 step, reinit, current_time += dt) inside one advance.  On FP32 3D grids
 with nx % 4 == 0 the vortex is evaluated inside the stage kernel; elsewhere
 u, v, w are refilled before each step.  Both must equal the explicit
