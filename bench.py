@@ -38,6 +38,21 @@ for _p in (ROOT, PKG):
         sys.path.insert(0, _p)
 
 METRIC = "Gcell-updates/s at 512^3 FP32 vs FP64 at stated Linf; adjoint/forward cost ratio"
+
+
+def l2_note(n: int) -> str:
+    """How a stage launch's working set (6 FP32 fields) compares with the 129 MB L2."""
+    ws = 6 * n ** 3 * 4
+    return (f"inputs larger than L2 (each FP32 field {n ** 3 * 4 / 2 ** 20:.0f} MiB, {ws / 2 ** 20:.0f} MiB per stage)"
+            if ws > 129e6 else f"working set {ws / 2 ** 20:.0f} MiB per stage fits in L2 (not flushed)")
+
+
+def workload_config(n: int, world: int) -> dict:
+    """The benchmark's workload, the same for both arms (each states its
+    arithmetic in "form")."""
+    return {"workload": f"config3 {n}^3 periodic, WENO5-RK3 + HCR-2 (every 5 steps, 2 pseudo-steps), "
+                        "S_L=0.2, CFL 0.5",
+            "grid": n, "bench_step": "5 RK3 steps + 1 HCR-2 reinit", "parallelism": f"replicas x{world}"}
 RK_PER_BENCH_STEP = 5      # reinit interval
 REINIT_ITERS = 2
 CFL = 0.5
@@ -285,9 +300,9 @@ def run_reference(args, dist: Dist):
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": step_s * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"config3 {args.n}x{args.n}x{nz} periodic slab of the {args.n}^3 workload "
-                               "(per-cell work identical), FP64, WENO5-RK3 + HCR-2 every 5 steps",
-                   "bench_step": "5 RK3 steps + 1 HCR-2 reinit (2 pseudo-steps)"},
+        "config": {**workload_config(args.n, args.gpus),
+                   "form": f"the reference's FP64 arithmetic (oracle port, OpenMP) on a {args.n}x{args.n}x{nz} "
+                           f"periodic slab of the workload: per-cell work identical"},
         "cpu_baseline": {"value": value, "unit": "Gcell-updates/s", "cores": threads, "kind": "port",
                          "sample": f"{args.n}x{args.n}x{nz} slab, {len(timed)} periods of 5 RK3 steps"},
         "e2e": {"value": value, "unit": "Gcell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -693,11 +708,9 @@ def run_ours(args, dist: Dist):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded config-3 fields generated on the device)",
-            "config": {"workload": f"config3 {n}^3 periodic, FP32-bulk WENO5-RK3 + HCR-2 (every 5 steps, "
-                                   "2 pseudo-steps, FP64 interface constraint), S_L=0.2, CFL 0.5",
-                       "grid": n, "bench_step": "5 RK3 steps + 1 HCR-2 reinit", "dt": dt,
-                       "l2": f"inputs larger than L2 (each FP32 field {n ** 3 * 4 / 2 ** 20:.0f} MiB)",
-                       "parallelism": f"replicas x{dist.world}"},
+            "config": {**workload_config(n, dist.world),
+                       "form": "FP32-bulk WENO5-RK3 + HCR-2, FP64 interface constraint and reductions", "dt": dt,
+                       "l2": l2_note(n)},
             "roofline": roofline,
             "whole_step_algorithmic_GBps": whole_step_gbs,
             "cpu_baseline": cpu,
