@@ -17,7 +17,7 @@ and reductions); the plain FP64 form is measured beside it.
 
 --impl reference times the reference's algorithm on the host CPU cores
 (the oracle port under oracle/, pinned bit-exact to the reference's own
-sources) on a bounded slab of the same workload.
+sources) on the full grid of the same workload, one bench step per step.
 Multi-GPU runs are independent replicas (the path is not sharded); rank 0
 prints the aggregate.
 """
@@ -68,7 +68,8 @@ def parse():
     ap.add_argument("--fp64-steps", type=int, default=2, help="timed FP64 bench steps (0 = skip)")
     ap.add_argument("--e2e-steps", type=int, default=2, help="timed end-to-end calls (0 = skip)")
     ap.add_argument("--e2e-rk-steps", type=int, default=50, help="RK3 steps per end-to-end call")
-    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline sample length")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0,
+                    help="CPU baseline sample length (whole reinit periods on the full grid, at least one)")
     ap.add_argument("--batch-steps", type=int, default=200, help="RK3 steps of the batched form (0 = skip)")
     ap.add_argument("--adjoint-steps", type=int, default=300, help="RK3 steps of the adjoint form (0 = skip)")
     ap.add_argument("--adjoint-n", type=int, default=192)
@@ -78,6 +79,7 @@ def parse():
     ap.add_argument("--no-config1", dest="config1", action="store_false", help="skip the 128^2 configuration-1 leg")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--json-out", default=None)
+    ap.add_argument("--clocks-out", default=None, help="write the nvidia-smi clock samples to this CSV file")
     return ap.parse_args()
 
 
@@ -247,64 +249,89 @@ def time_solver(torch, s, stream, steps: int, warmup: int, dist: Dist | None, sa
 
 
 # -- CPU leg (oracle: the reference's algorithm on the host cores) -------------
-def cpu_sample(n: int, nz_slab: int, target_s: float, max_periods: int | None = None):
-    """Times the oracle (oracle/ls_oracle.c, OpenMP over all host cores) on a
-    512 x 512 x nz_slab periodic slab of the same workload.  Returns
-    (Gcell-updates/s, periods run, seconds, threads, per-period seconds)."""
-    import numpy as np
-    from lsgb import synthetic as syn
-    from oracle import Oracle, Problem
-    orc = Oracle("port")
-    wl = syn.config3(n)
-    wl.n = (n, n, nz_slab)
-    G, u, v, w = syn.host_fields(wl, normalise=False)
-    # same scale as the full grid (max |u| = 1 there): reuse the slab max
-    sp = float(np.sqrt(u * u + v * v + w * w).max())
-    u, v, w = u / sp, v / sp, w / sp
-    dt = syn.cfl_dt(wl, u, v, w, CFL)
-    pb = Problem(nx=n, ny=n, nz=nz_slab, dx=1 / n, dy=1 / n, dz=1 / n, dim=3, s_l=wl.s_l, dt=dt,
-                 enable_reinit=True, reinit_interval=RK_PER_BENCH_STEP, reinit_iterations=REINIT_ITERS)
-    cells = n * n * nz_slab
-    periods, t0, per = 0, time.perf_counter(), []
-    cur = G
-    while True:
-        a = time.perf_counter()
-        # step0 = 1 makes the last of the 5 steps of each call run the reinit
-        cur = orc.run(pb, RK_PER_BENCH_STEP, cur, u, v, w, step0=1)
-        per.append(time.perf_counter() - a)
-        periods += 1
-        el = time.perf_counter() - t0
-        if max_periods is not None:
-            if periods >= max_periods:
+def cpu_info() -> dict:
+    """Host CPU model (lscpu "Model name") and logical CPU count."""
+    import platform
+    model = None
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for l in out.splitlines():
+            if l.startswith("Model name:"):
+                model = l.split(":", 1)[1].strip()
                 break
-        elif el >= target_s:
+    except (OSError, subprocess.SubprocessError):
+        pass
+    return {"cpu_model": model or platform.processor() or platform.machine(), "host_cpus": os.cpu_count()}
+
+
+def omp_threads() -> int:
+    return int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+
+
+class CpuRun:
+    """The reference's algorithm (the oracle port, oracle/ls_oracle.c, OpenMP
+    over all host cores) on the full n^3 grid of the workload: the fields are
+    built on the host (lsgb.synthetic.host_fields, FP64, max |u| = 1), dt from
+    CFL 0.5 with the field-max speed.  One period = 5 RK3 steps + the HCR-2
+    reinitialisation after the 5th (the reference's cadence, steps 1..5)."""
+
+    def __init__(self, n: int):
+        from lsgb import synthetic as syn
+        from oracle import Oracle, Problem
+        self.orc = Oracle("port")
+        wl = syn.config3(n)
+        self.G, self.u, self.v, self.w = syn.host_fields(wl)
+        dt = syn.cfl_dt(wl, self.u, self.v, self.w, CFL)
+        self.pb = Problem(nx=n, ny=n, nz=n, dim=3, s_l=wl.s_l, dt=dt, enable_reinit=True,
+                          reinit_interval=RK_PER_BENCH_STEP, reinit_iterations=REINIT_ITERS)
+        self.cells = n ** 3
+        self.periods = 0
+
+    def period(self) -> float:
+        """Advances one period; returns its wall time in seconds."""
+        a = time.perf_counter()
+        self.orc.run_filled(self.pb, RK_PER_BENCH_STEP, self.G, self.u, self.v, self.w,
+                            step0=1 + RK_PER_BENCH_STEP * self.periods)
+        self.periods += 1
+        return time.perf_counter() - a
+
+
+def cpu_sample(n: int, target_s: float):
+    """Bounded CPU sample on the full grid: whole periods until target_s has
+    passed (at least one).  Returns (Gcell-updates/s, periods, seconds)."""
+    run = CpuRun(n)
+    el = 0.0
+    while True:
+        el += run.period()
+        if el >= target_s:
             break
-    threads = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
-    return cells * RK_PER_BENCH_STEP * periods / el / 1e9, periods, el, threads, per
+    return run.cells * RK_PER_BENCH_STEP * run.periods / el / 1e9, run.periods, el
 
 
 def run_reference(args, dist: Dist):
-    """--impl reference: the reference algorithm on the host cores."""
+    """--impl reference: the reference algorithm on the host cores, on the
+    same full grid and bench steps as the GPU arm."""
     if dist.rank != 0:
         return
     from oracle import build_port
     build_port()
-    nz = 16
-    # warmup + timed steps, each one reinit period on the slab
-    _, _, _, threads, per = cpu_sample(args.n, nz, 0.0, max_periods=args.warmup + args.steps)
-    timed = per[args.warmup:]
+    run = CpuRun(args.n)
+    for _ in range(args.warmup):
+        run.period()
+    timed = [run.period() for _ in range(args.steps)]
     step_s = sum(timed) / len(timed)
-    value = args.n * args.n * nz * RK_PER_BENCH_STEP / step_s / 1e9
+    value = run.cells * RK_PER_BENCH_STEP / step_s / 1e9
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "Gcell-updates/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": step_s * 1e3, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded config-3 fields built on the host)",
         "config": {**workload_config(args.n, args.gpus),
-                   "form": f"the reference's FP64 arithmetic (oracle port, OpenMP) on a {args.n}x{args.n}x{nz} "
-                           f"periodic slab of the workload: per-cell work identical"},
-        "cpu_baseline": {"value": value, "unit": "Gcell-updates/s", "cores": threads, "kind": "port",
-                         "sample": f"{args.n}x{args.n}x{nz} slab, {len(timed)} periods of 5 RK3 steps"},
+                   "form": f"the reference's FP64 arithmetic (oracle port, OpenMP) on the full {args.n}^3 grid"},
+        "cpu_baseline": {"value": value, "unit": "Gcell-updates/s", "cores": omp_threads(), "kind": "port",
+                         "sample": f"full {args.n}^3 grid, {len(timed)} timed periods of 5 RK3 steps + 1 HCR-2 "
+                                   f"after {args.warmup} warm-up periods",
+                         **cpu_info()},
         "e2e": {"value": value, "unit": "Gcell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -567,8 +594,11 @@ def run_ours(args, dist: Dist):
     n = args.n
     cells = n ** 3
     stream = torch.cuda.Stream()
-    os.makedirs(os.path.join(ROOT, "gpurun_out"), exist_ok=True)
-    sampler = ClockSampler(dist.local, os.path.join(ROOT, "gpurun_out", f"clocks_rank{dist.rank}.csv"))
+    clocks_out = None
+    if args.clocks_out:
+        root, ext = os.path.splitext(args.clocks_out)
+        clocks_out = args.clocks_out if dist.world == 1 else f"{root}_rank{dist.rank}{ext}"
+    sampler = ClockSampler(dist.local, clocks_out)
 
     # --- FP32-bulk headline ---
     s32, wl = make_solver(lsgb, syn, n, "f32", stream)
@@ -697,10 +727,10 @@ def run_ours(args, dist: Dist):
 
     cpu = None
     if not args.no_cpu_baseline and dist.rank == 0 and dist.world == 1:
-        rate, periods, el, threads, _ = cpu_sample(n, 16, args.cpu_seconds)
-        cpu = {"value": rate, "unit": "Gcell-updates/s", "cores": threads, "kind": "port",
-               "sample": f"{n}x{n}x16 slab of the workload, {periods} reinit periods "
-                         f"({periods * RK_PER_BENCH_STEP} RK3 steps), {el:.1f} s"}
+        rate, periods, el = cpu_sample(n, args.cpu_seconds)
+        cpu = {"value": rate, "unit": "Gcell-updates/s", "cores": omp_threads(), "kind": "port",
+               "sample": f"full {n}^3 grid of the workload, {periods} reinit periods "
+                         f"({periods * RK_PER_BENCH_STEP} RK3 steps), {el:.1f} s", **cpu_info()}
 
     if dist.rank == 0:
         line = {

@@ -151,8 +151,9 @@ LSGB_API int lsgb_volume_f64(const lsgb_params* p, const double* G, double* volu
  * every GPU that loads the library until the process exits):
  *   - at most LSGB_NOALLOC_MAX_CELLS interior cells (2^30, e.g. 1024^3) per
  *     call; larger grids return LSGB_ERR_INVALID;
- *   - the first call on a device looks the array's address up; make that
- *     first call before any stream capture;
+ *   - the first call on a device (and again the first after a
+ *     cudaDeviceReset, which gives the device a new context) looks the
+ *     array's address up; make that first call before any stream capture;
  *   - all calls share the array: calls that overlap on the GPU race.
  * Synchronises the stream.  Calls no cudaMalloc / cudaFree. */
 #define LSGB_NOALLOC_CHUNK 16384

@@ -350,6 +350,9 @@ struct lsgb_solver {
     float* defo_f32 = nullptr;  // FP32 factor tables of the vortex (built once)
     int tile = 0;  // tile-shape choice handed to the stage kernels (0 = default)
     int drop_copies = 0;  // test hook (lsgb_solver_debug_drop_copies)
+    // set when a kernel gave up with bulk copies still in flight into its
+    // shared memory: every later call fails until the handle is destroyed
+    bool unusable = false;
     bool have_G = false, have_vel = false;
     // kernel timing (lsgb_solver_enable_timing)
     bool timing = false;
@@ -387,9 +390,18 @@ size_t nbytes(const lsgb_solver* s) { return s->esz * (size_t)s->g.cells(); }
 // waits set when a wait gives up; cleared when reported.
 int* err_flag(lsgb_solver* s) { return (int*)(s->scratch + 2 * (RED_BLOCKS + 1) + 2); }
 
+// Flag values: 1 = a wait gave up and the block's issued copies then landed
+// (the handle recovers once the flag is reported and cleared); 2 = even the
+// bounded drain of those copies gave up, so a copy may still write into
+// shared memory that a later block owns: the handle is marked unusable.
 int flag_result(lsgb_solver* s, int flag) {
     if (!flag) return LSGB_OK;
     cudaMemsetAsync(err_flag(s), 0, sizeof(int), s->st);
+    if (flag >= 2) {
+        s->unusable = true;
+        return fail(LSGB_ERR_CUDA, "a bounded in-kernel wait gave up with bulk copies still in flight; the handle "
+                                   "is unusable: synchronise its stream and destroy it");
+    }
     return fail(LSGB_ERR_CUDA, "a bounded in-kernel wait gave up (bulk copy did not arrive); results of the "
                                "last steps are not valid");
 }
@@ -585,6 +597,9 @@ double* red_out(lsgb_solver* s) { return s->scratch + 2 * (RED_BLOCKS + 1); }
 
 int solver_ok(const lsgb_solver* s) {
     if (!s) return fail(LSGB_ERR_INVALID, "solver is NULL");
+    if (s->unusable)
+        return fail(LSGB_ERR_CUDA, "handle unusable after an in-kernel wait gave up with copies in flight; "
+                                   "destroy it");
     return LSGB_OK;
 }
 

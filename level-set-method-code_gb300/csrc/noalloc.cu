@@ -18,13 +18,17 @@
 //     count per LSGB_NOALLOC_CHUNK cells, LSGB_NOALLOC_MAX_PARTIALS partials);
 //     larger grids are rejected with LSGB_ERR_INVALID.
 //   - The first call on a device looks up the array's device address
-//     (cudaGetSymbolAddress, with that device current) and caches it; make
-//     that first call before any stream capture.
+//     (cudaGetSymbolAddress, with that device current) and caches it for
+//     that device's current context; make that first call before any stream
+//     capture.  A call after cudaDeviceReset (a new context) looks it up
+//     again.
 //   - All calls share the one array, which keeps the last call's contents.
 //     Calls whose work overlaps on the GPU (different streams, no ordering
 //     between them) race on it and may return wrong results.
 //   - No cudaMalloc, cudaFree or allocating library routine is called.
 #include "common.cuh"
+
+#include <cuda.h>
 
 #include <mutex>
 
@@ -88,21 +92,53 @@ __global__ void __launch_bounds__(NA_THREADS) noalloc_count_pass2(int nb, double
 constexpr int MAX_DEVICES = 64;
 std::mutex g_setup_mu;
 double* g_scratch_addr[MAX_DEVICES] = {nullptr};
+unsigned long long g_scratch_ctx[MAX_DEVICES] = {0};  // context the address belongs to
+
+// Unique id of the calling thread's current context (cuCtxGetId, through the
+// runtime's driver entry points, so the library needs no -lcuda), or 0 when
+// it cannot be read.  Ids are never reused within a process, unlike context
+// handles.
+unsigned long long current_context_id() {
+    typedef CUresult (*GetCurrent)(CUcontext*);
+    typedef CUresult (*GetId)(CUcontext, unsigned long long*);
+    static GetCurrent get_current = nullptr;
+    static GetId get_id = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_current = (GetCurrent)p;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = (GetId)p;
+    });
+    CUcontext ctx = nullptr;
+    unsigned long long id = 0;
+    if (!get_current || !get_id || get_current(&ctx) != CUDA_SUCCESS || !ctx || get_id(ctx, &id) != CUDA_SUCCESS)
+        return 0;
+    return id;
+}
 
 // Device address of g_noalloc_scratch on the current device, looked up once
-// per device.  In host code the array's name is only a host-side stand-in, so
-// it is never handed to a kernel directly.
+// per device and context: after cudaDeviceReset the primary context is
+// created anew and the array lives at a new address, so a changed context id
+// triggers a fresh lookup.  In host code the array's name is only a
+// host-side stand-in, so it is never handed to a kernel directly.
 cudaError_t scratch_address(double** out) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
     if (dev < 0 || dev >= MAX_DEVICES) return cudaErrorInvalidDevice;
+    const unsigned long long ctx = current_context_id();  // 0 before the device's first runtime call
     std::lock_guard<std::mutex> lock(g_setup_mu);
-    if (!g_scratch_addr[dev]) {
+    if (!g_scratch_addr[dev] || ctx == 0 || ctx != g_scratch_ctx[dev]) {
         double* p = nullptr;
-        e = cudaGetSymbolAddress((void**)&p, g_noalloc_scratch);
+        e = cudaGetSymbolAddress((void**)&p, g_noalloc_scratch);  // creates the context if needed
         if (e != cudaSuccess) return e;
         g_scratch_addr[dev] = p;
+        g_scratch_ctx[dev] = ctx ? ctx : current_context_id();
     }
     *out = g_scratch_addr[dev];
     return cudaSuccess;

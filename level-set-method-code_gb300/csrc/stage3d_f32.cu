@@ -74,7 +74,10 @@ constexpr int BNFX = (TX + 1) * BY;           // x faces of the tile
 constexpr int NSTAGE = 3;                     // TMA pipeline depth (plane pairs in flight)
 constexpr int NFIELD = 5;                     // u, v, w, G^n, S_L
 constexpr int BFTILE = 2 * BY * TX;           // floats of one staged field tile (2 planes)
-constexpr long long WAIT_CYCLES = 2000000000LL;  // bounded mbarrier wait (~1 s of SM clock)
+// bounded mbarrier wait: about 1 s at the full SM clock.  The limit counts SM
+// clock cycles, not wall time, so on a GPU time-sliced between processes a
+// slow but healthy copy can run into it.
+constexpr long long WAIT_CYCLES = 2000000000LL;
 
 struct TmaMaps {
     CUtensorMap m[NFIELD];
@@ -411,9 +414,12 @@ stage3d_f32_col2(Geo g, const float* __restrict__ Gin, const float* __restrict__
                 // still in flight (issued by thread 0) a bounded chance to
                 // land, and leave
                 if (t == 0) {
-                    atomicExch(err, 1);
+                    atomicMax(err, 1);
                     const int issued = c.drop ? 0 : min(niter, it + NSTAGE);  // iterations whose copies went out
-                    for (int j = it; j < issued; ++j) mbar_wait(&mbar[j % NSTAGE], (uint32_t)((j / NSTAGE) & 1));
+                    bool drained = true;
+                    for (int j = it; j < issued; ++j)
+                        drained = mbar_wait(&mbar[j % NSTAGE], (uint32_t)((j / NSTAGE) & 1)) && drained;
+                    if (!drained) atomicMax(err, 2);  // copies may still land in this block's shared memory
                 }
                 return;
             }

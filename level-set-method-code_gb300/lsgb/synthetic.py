@@ -4,8 +4,8 @@ No dataset is involved: every input is generated from a seed.  The mode
 tables are drawn here with numpy's PCG64 (``default_rng``), seed
 ``20261203 + 1000 * config + instance``; the same table drives
 
-* :func:`host_fields` -- the fields evaluated in numpy FP64 on the host (small
-  grids: tests and the CPU baselines), and
+* :func:`host_fields` -- the fields evaluated in numpy FP64 on the host (tests,
+  and the CPU baselines on the full benchmark grid), and
 * :func:`to_device_desc` -- the ``lsgb_synth`` descriptor the device generator
   (csrc/synth.cu) evaluates in FP64 for the large grids.
 
@@ -132,22 +132,20 @@ def config3(n: int = 512) -> Workload:
     return sphere_config(3, n, 24, 0.2)
 
 
-def _coords(wl: Workload, ghosted: bool):
-    g = 3 if ghosted else 0
-    axes = []
-    for q in wl.n:
-        axes.append((np.arange(q + 2 * g, dtype=np.float64) - g) / q)
+def _coords(wl: Workload, lo: int, hi: int):
+    """Cell-centre coordinates of interior slab [lo, hi) along the slowest
+    axis (z in 3D, y in 2D)."""
+    axes = [np.arange(q, dtype=np.float64) / q for q in wl.n]
     if wl.dim == 3:
-        z, y, x = np.meshgrid(axes[2], axes[1], axes[0], indexing="ij")
+        z, y, x = np.meshgrid(axes[2][lo:hi], axes[1], axes[0], indexing="ij")
         return x, y, z
-    y, x = np.meshgrid(axes[1], axes[0], indexing="ij")
+    y, x = np.meshgrid(axes[1][lo:hi], axes[0], indexing="ij")
     return x, y, np.zeros_like(x)
 
 
-def host_fields(wl: Workload, normalise: bool = True):
-    """(G, u, v, w) float64 in the ghosted layout, ghosts = periodic images.
-    w is None in 2D.  Evaluated at interior cells, then wrapped."""
-    x, y, z = _coords(wl, ghosted=False)
+def _slab(wl: Workload, lo: int, hi: int):
+    """(G, u, v, w) of interior slab [lo, hi), velocity not yet normalised."""
+    x, y, z = _coords(wl, lo, hi)
     px, py = x - wl.center[0], y - wl.center[1]
     pz = z - wl.center[2] if wl.dim == 3 else np.zeros_like(x)
     rad = np.sqrt(px * px + py * py + pz * pz)
@@ -164,7 +162,7 @@ def host_fields(wl: Workload, normalise: bool = True):
     if wl.uniform_velocity is not None:
         u = np.full_like(G, wl.uniform_velocity[0])
         v = np.full_like(G, wl.uniform_velocity[1])
-        w = np.zeros_like(G) if wl.dim == 3 else None
+        w = np.zeros_like(G)
     else:
         u = np.zeros_like(G)
         v = np.zeros_like(G)
@@ -175,17 +173,56 @@ def host_fields(wl: Workload, normalise: bool = True):
             u += c[0] * cs
             v += c[1] * cs
             w += c[2] * cs
-        if normalise:
-            sp = np.sqrt(u * u + v * v + (w * w if wl.dim == 3 else 0.0))
-            m = float(sp.max())
-            if m > 0:
-                u /= m
-                v /= m
-                w /= m
-        if wl.dim == 2:
-            w = None
-    wrap = lambda a: None if a is None else np.ascontiguousarray(np.pad(a, 3, mode="wrap"))
-    return wrap(G), wrap(u), wrap(v), wrap(w)
+    return G, u, v, w
+
+
+def _wrap_ghosts(a: np.ndarray, g: int = 3):
+    """Fill the g-deep ghost layers of every axis with periodic images, in
+    place (the same values as np.pad(interior, g, mode="wrap"))."""
+    for ax in range(a.ndim - 1, -1, -1):
+        n = a.shape[ax] - 2 * g
+        idx = lambda s: tuple(s if d == ax else slice(None) for d in range(a.ndim))
+        a[idx(slice(0, g))] = a[idx(slice(n, n + g))]
+        a[idx(slice(n + g, n + 2 * g))] = a[idx(slice(g, 2 * g))]
+
+
+def host_fields(wl: Workload, normalise: bool = True, threads: int | None = None):
+    """(G, u, v, w) float64 in the ghosted layout, ghosts = periodic images.
+    w is None in 2D.  Evaluated at interior cells in slabs along the slowest
+    axis (in parallel threads; every value is an element-wise expression, so
+    the slab size does not change a bit), then wrapped."""
+    import concurrent.futures as cf
+    import os
+
+    shape = tuple(q + 6 for q in reversed(wl.n))
+    G, u, v = (np.empty(shape) for _ in range(3))
+    w = np.empty(shape) if wl.dim == 3 else None
+    nslow = wl.n[-1]
+    per_plane = int(np.prod(wl.n[:-1]))
+    step = max(1, min(nslow, (1 << 21) // max(per_plane, 1)))
+    inner = (slice(3, -3),) * (wl.dim - 1)
+
+    def work(lo):
+        hi = min(nslow, lo + step)
+        g, a, b, c = _slab(wl, lo, hi)
+        sl = (slice(3 + lo, 3 + hi),) + inner
+        G[sl], u[sl], v[sl] = g, a, b
+        if w is not None:
+            w[sl] = c
+        sp = np.sqrt(a * a + b * b + (c * c if wl.dim == 3 else 0.0))
+        return float(sp.max())
+
+    nthr = threads or min(16, os.cpu_count() or 1)
+    with cf.ThreadPoolExecutor(max_workers=nthr) as ex:
+        m = max(ex.map(work, range(0, nslow, step)))
+    if wl.uniform_velocity is None and normalise and m > 0:
+        for a in (u, v, w):
+            if a is not None:
+                a /= m
+    for a in (G, u, v, w):
+        if a is not None:
+            _wrap_ghosts(a)
+    return G, u, v, w
 
 
 def to_device_desc(wl: Workload, normalise: bool = True):

@@ -14,8 +14,13 @@
 # IEEE double operations the reference source spells out.
 set -euo pipefail
 here="$(cd "$(dirname "$0")" && pwd)"
-ref_root="${LSGB_REFERENCE_ROOT:-/root/reference}"
+# the reference tree: first argument, else $LSGB_REFERENCE_ROOT (no default)
+ref_root="${1:-${LSGB_REFERENCE_ROOT:-}}"
 out="$here/_ref"
+if [ -z "$ref_root" ]; then
+    echo "usage: build_ref.sh <reference root>  (or set LSGB_REFERENCE_ROOT)" >&2
+    exit 2
+fi
 if [ ! -d "$ref_root/Local_code/level-set_MPI_3D/include" ]; then
     echo "build_ref.sh: reference tree not found at $ref_root" >&2
     exit 2

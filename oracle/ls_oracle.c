@@ -529,45 +529,82 @@ double orc_cfl_dt(const orc_params* p, int dim, double cfl, double max_speed) {
  * step0 offsets the step counter (a run split in segments keeps the cadence).
  * G is updated in place; velocity arrays are copied.
  * ------------------------------------------------------------------------- */
-static void run_any(const orc_params* p, int dim, int n_steps, int step0, double* G,
-                    const double* u_in, const double* v_in, const double* w_in, const double* sl) {
+/* The loop itself on G in place, with velocities whose ghosts are already
+ * filled (read in place).  Scratch: 5 fields + the flag array.  Stage 2 of
+ * each step writes G2 over G1 (the combination is point-wise, so every cell
+ * reads its own G1 value before overwriting it: the same bits as separate
+ * buffers), and the reinitialisation's ping-pong partner is the rhs buffer,
+ * which holds nothing between steps.  Returns 0, or -1 if the scratch
+ * allocation fails. */
+static int run_core(const orc_params* p, int dim, int n_steps, int step0, double* G,
+                    const double* u, const double* v, const double* w, const double* sl) {
     grid_t g = dim == 3 ? grid3(p) : grid2(p);
     long n = total_of(&g);
     size_t bytes = sizeof(double) * (size_t)n;
-    double* buf = (double*)calloc((size_t)n * 11, sizeof(double));
+    double* buf = (double*)calloc((size_t)n * 5, sizeof(double));
     int* flag = (int*)calloc((size_t)n, sizeof(int));
-    double *Gc = buf, *Gnew = buf + n, *G1 = buf + 2 * n, *G2 = buf + 3 * n, *R = buf + 4 * n;
-    double *u = buf + 5 * n, *v = buf + 6 * n, *w = buf + 7 * n;
-    double *tmp = buf + 8 * n, *phi0 = buf + 9 * n, *rt = buf + 10 * n;
-    memcpy(Gc, G, bytes);
-    memcpy(u, u_in, bytes);
-    memcpy(v, v_in, bytes);
-    if (dim == 3) memcpy(w, w_in, bytes);
-    if (dim == 3) { bc3(&g, Gc); bc3(&g, u); bc3(&g, v); bc3(&g, w); }
-    else { bc2(p, &g, Gc); bc2(p, &g, u); bc2(p, &g, v); }
-    double* a = Gc;
+    if (!buf || !flag) {
+        free(buf);
+        free(flag);
+        return -1;
+    }
+    double *Gnew = buf, *G1 = buf + n, *R = buf + 2 * n, *phi0 = buf + 3 * n, *rt = buf + 4 * n;
+    if (dim == 3) bc3(&g, G); else bc2(p, &g, G);
+    double* a = G;
     double* b = Gnew;
     for (int s = 0; s < n_steps; s++) {
         int step = step0 + s;
-        if (dim == 3) orc3d_rk3_step(p, a, b, G1, G2, R, u, v, w, sl);
-        else orc2d_rk3_step(p, a, b, G1, G2, R, u, v, sl);
+        if (dim == 3) orc3d_rk3_step(p, a, b, G1, G1, R, u, v, w, sl);
+        else orc2d_rk3_step(p, a, b, G1, G1, R, u, v, sl);
         double* t = a; a = b; b = t;
         if (p->enable_reinit && step > 0 && step % p->reinit_interval == 0)
-            reinit_any(p, dim, a, tmp, phi0, rt, flag);
+            reinit_any(p, dim, a, R, phi0, rt, flag);
     }
-    memcpy(G, a, bytes);
+    if (a != G) memcpy(G, a, bytes);
     free(buf);
     free(flag);
+    return 0;
 }
 
-void orc3d_run(const orc_params* p, int n_steps, int step0, double* G, const double* u,
-               const double* v, const double* w, const double* sl) {
-    run_any(p, 3, n_steps, step0, G, u, v, w, sl);
+static int run_any(const orc_params* p, int dim, int n_steps, int step0, double* G,
+                   const double* u_in, const double* v_in, const double* w_in, const double* sl) {
+    grid_t g = dim == 3 ? grid3(p) : grid2(p);
+    long n = total_of(&g);
+    size_t bytes = sizeof(double) * (size_t)n;
+    double* vel = (double*)calloc((size_t)n * 3, sizeof(double));
+    if (!vel) return -1;
+    double *u = vel, *v = vel + n, *w = vel + 2 * n;
+    memcpy(u, u_in, bytes);
+    memcpy(v, v_in, bytes);
+    if (dim == 3) memcpy(w, w_in, bytes);
+    if (dim == 3) { bc3(&g, u); bc3(&g, v); bc3(&g, w); }
+    else { bc2(p, &g, u); bc2(p, &g, v); }
+    int rc = run_core(p, dim, n_steps, step0, G, u, v, dim == 3 ? w : NULL, sl);
+    free(vel);
+    return rc;
 }
 
-void orc2d_run(const orc_params* p, int n_steps, int step0, double* G, const double* u,
-               const double* v, const double* sl) {
-    run_any(p, 2, n_steps, step0, G, u, v, NULL, sl);
+int orc3d_run(const orc_params* p, int n_steps, int step0, double* G, const double* u,
+              const double* v, const double* w, const double* sl) {
+    return run_any(p, 3, n_steps, step0, G, u, v, w, sl);
+}
+
+int orc2d_run(const orc_params* p, int n_steps, int step0, double* G, const double* u,
+              const double* v, const double* sl) {
+    return run_any(p, 2, n_steps, step0, G, u, v, NULL, sl);
+}
+
+/* The same loop for grids too large to copy the velocity: u, v, w must
+ * already hold their boundary images (as bc3 / bc2 leaves them); they are
+ * only read. */
+int orc3d_run_filled(const orc_params* p, int n_steps, int step0, double* G, const double* u,
+                     const double* v, const double* w, const double* sl) {
+    return run_core(p, 3, n_steps, step0, G, u, v, w, sl);
+}
+
+int orc2d_run_filled(const orc_params* p, int n_steps, int step0, double* G, const double* u,
+                     const double* v, const double* sl) {
+    return run_core(p, 2, n_steps, step0, G, u, v, NULL, sl);
 }
 
 /* ---------------------------------------------------------------------------

@@ -108,14 +108,14 @@ def build_port(force: bool = False) -> str:
 
 
 def build_ref(reference_root: str | None = None) -> bool:
-    """Compile the reference's own solver headers (oracle/build_ref.sh).
-    Returns False when the reference tree is absent on this host."""
+    """Compile the reference's own solver headers (oracle/build_ref.sh) from
+    the reference tree at ``reference_root`` (or ``$LSGB_REFERENCE_ROOT``).
+    Returns False when no root is given or the tree is absent there."""
     env = dict(os.environ)
-    if reference_root:
-        env["LSGB_REFERENCE_ROOT"] = reference_root
-    root = env.get("LSGB_REFERENCE_ROOT", "/root/reference")
-    if not os.path.isdir(os.path.join(root, "Local_code")):
+    root = reference_root or env.get("LSGB_REFERENCE_ROOT")
+    if not root or not os.path.isdir(os.path.join(root, "Local_code")):
         return False
+    env["LSGB_REFERENCE_ROOT"] = root
     subprocess.run(["bash", os.path.join(HERE, "build_ref.sh")], check=True, env=env,
                    stdout=subprocess.DEVNULL)
     return True
@@ -248,11 +248,30 @@ class Oracle:
                 self._l2.ref2d_run(C.byref(p), n_steps, _ptr(out), _ptr(u), _ptr(v))
         else:
             if pb.dim == 3:
-                self._l3.orc3d_run(C.byref(p), n_steps, step0, _ptr(out), _ptr(u), _ptr(v), _ptr(w),
-                                   _ptr(sl))
+                rc = self._l3.orc3d_run(C.byref(p), n_steps, step0, _ptr(out), _ptr(u), _ptr(v), _ptr(w),
+                                        _ptr(sl))
             else:
-                self._l2.orc2d_run(C.byref(p), n_steps, step0, _ptr(out), _ptr(u), _ptr(v), _ptr(sl))
+                rc = self._l2.orc2d_run(C.byref(p), n_steps, step0, _ptr(out), _ptr(u), _ptr(v), _ptr(sl))
+            if rc != 0:
+                raise MemoryError("oracle run: scratch allocation failed")
         return out
+
+    def run_filled(self, pb: Problem, n_steps: int, G, u, v, w=None, sl=None, step0: int = 0):
+        """:meth:`run` for grids too large for copies (the port only): G is
+        advanced IN PLACE and u, v, w must already hold their boundary images
+        (e.g. from :meth:`apply_bc`); they are read, not copied.  Scratch is 5
+        fields + one int32 field.  Returns G."""
+        assert self.kind == "port"
+        self._chk(pb, G, u, v, w, sl)
+        p = pb.c()
+        if pb.dim == 3:
+            rc = self._l3.orc3d_run_filled(C.byref(p), n_steps, step0, _ptr(G), _ptr(u), _ptr(v), _ptr(w),
+                                           _ptr(sl))
+        else:
+            rc = self._l2.orc2d_run_filled(C.byref(p), n_steps, step0, _ptr(G), _ptr(u), _ptr(v), _ptr(sl))
+        if rc != 0:
+            raise MemoryError("oracle run: scratch allocation failed")
+        return G
 
     def volume(self, pb: Problem, G):
         """computeInterfaceVolume / computeInterfaceArea."""
