@@ -378,10 +378,17 @@ typedef struct lsgb_diagnostics {
     double volume, volume_ref;      /* cells with G < 0 times the cell volume      (:88-98) */
     double volume_smooth, volume_smooth_ref;  /* smoothed Heaviside of -G, eps = dx (:100-107, :264-271) */
     double grad_mean, grad_std;     /* |grad G| (central differences) where |G| < 3 dx (:109-133) */
-    double iface_mean, iface_max;   /* interface distance: crossing points of each zero set
-                                       against the other, |G(p)| / |grad G(p)| (first order);
-                                       mean and max stand in for the contour mean / Hausdorff (:51-84) */
+    double iface_mean, iface_max;   /* first-order interface distance: each zero set's grid-edge
+                                       crossing points p against the other field, |G(p)| / |grad G(p)|;
+                                       mean and max (a cheap estimate beside the contour metric below) */
     int64_t band_cells, iface_points;
+    double contour_hausdorff;       /* the script's interface position error (:51-84): zero contours
+                                       of G and G_ref as grid-edge crossing points (contourc's
+                                       vertices; in 3D the isosurface's), every point's distance to
+                                       the nearest point of the other set; the largest of them */
+    double contour_mean;            /* their mean over both sets (the "mean interface error") */
+    int64_t contour_points, contour_points_ref;  /* points of G's / G_ref's zero set; when either is
+                                                    0 the two distances above are NaN */
 } lsgb_diagnostics;
 LSGB_API int lsgb_solver_diagnostics(lsgb_solver* s, const double* G_ref, int layout, int memory,
                                      lsgb_diagnostics* out);

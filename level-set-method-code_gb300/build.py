@@ -27,11 +27,12 @@ COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler",
 EXTRA = {
     "f64_kernels.cu": ["--fmad=false"],
     "sample_kernels.cu": ["--fmad=false"],
+    "contour.cu": ["--fmad=false"],
     # host arithmetic of the forced velocity must not contract (aarch64 gcc would)
     "sample_api.cu": ["-Xcompiler", "-ffp-contract=off"],
 }
 SOURCES = ["api.cu", "f64_kernels.cu", "f32_kernels.cu", "reduce.cu", "synth.cu", "noalloc.cu", "stage3d_f32.cu",
-           "stage2d_f32.cu", "adjoint.cu", "sample_kernels.cu", "sample_api.cu", "dump.cu", "diag.cu"]
+           "stage2d_f32.cu", "adjoint.cu", "sample_kernels.cu", "sample_api.cu", "dump.cu", "diag.cu", "contour.cu"]
 
 
 def _nvcc() -> str:

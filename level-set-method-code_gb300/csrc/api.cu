@@ -2125,6 +2125,7 @@ extern "C" int lsgb_solver_diagnostics(lsgb_solver* s, const double* G_ref, int 
     }
     int rc = load_f64_compact(s, ref, G_ref, layout, memory);
     double r[14];
+    ContourDist cd{};
     if (rc == LSGB_OK) {
         const double dz = s->p.dim == 3 ? s->p.dz : s->p.dx;
         e = s->prec == LSGB_PREC_F64
@@ -2134,6 +2135,11 @@ extern "C" int lsgb_solver_diagnostics(lsgb_solver* s, const double* G_ref, int 
             e = cudaMemcpyAsync(r, scr + (diag_scratch_bytes() / sizeof(double) - 14), sizeof(r),
                                 cudaMemcpyDeviceToHost, s->st);
         if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
+        // contour-point distances of the script's interface position error
+        if (e == cudaSuccess)
+            e = s->prec == LSGB_PREC_F64
+                    ? contour_distances<double>(s->g, (const double*)s->G, ref, s->p.dx, s->p.dy, dz, &cd, s->st)
+                    : contour_distances<float>(s->g, (const float*)s->G, ref, s->p.dx, s->p.dy, dz, &cd, s->st);
         if (e != cudaSuccess) rc = fail(LSGB_ERR_CUDA, "diagnostics: %s", cudaGetErrorString(e));
     }
     cudaFreeAsync(ref, s->st);
@@ -2154,5 +2160,9 @@ extern "C" int lsgb_solver_diagnostics(lsgb_solver* s, const double* G_ref, int 
     out->iface_points = (int64_t)r[12];
     out->iface_mean = r[12] > 0.0 ? r[10] / r[12] : 0.0;
     out->iface_max = r[11];
+    out->contour_hausdorff = cd.hausdorff;
+    out->contour_mean = cd.mean;
+    out->contour_points = (int64_t)cd.points;
+    out->contour_points_ref = (int64_t)cd.points_ref;
     return check_flag(s);
 }

@@ -301,6 +301,18 @@ template <typename T>
 cudaError_t launch_diagnostics(const Geo& g, const T* G, const double* Gr, double dx, double dy, double dz,
                                double* scratch, cudaStream_t st);
 
+// Interface position error of analyze_error.m:51-84 (contour.cu): the zero
+// contours of G and Gr as grid-edge crossing points, each point's distance
+// to the nearest point of the other set; Hausdorff = the largest, mean over
+// both sets.  NaN when either set is empty.  Synchronises the stream.
+struct ContourDist {
+    double hausdorff, mean;
+    long long points, points_ref;
+};
+template <typename T>
+cudaError_t contour_distances(const Geo& g, const T* G, const double* Gr, double dx, double dy, double dz,
+                              ContourDist* out, cudaStream_t st);
+
 // Bookkeeping of kernel launches (lsgb_launch_count).
 void count_launches(uint64_t n);
 

@@ -575,7 +575,11 @@ class Diagnostics(C.Structure):
 
     _fields_ = [(n, C.c_double) for n in ("l2", "linf", "l2_rel", "volume", "volume_ref", "volume_smooth",
                                           "volume_smooth_ref", "grad_mean", "grad_std", "iface_mean",
-                                          "iface_max")] + [("band_cells", C.c_int64), ("iface_points", C.c_int64)]
+                                          "iface_max")] + [("band_cells", C.c_int64), ("iface_points", C.c_int64),
+                                                           ("contour_hausdorff", C.c_double),
+                                                           ("contour_mean", C.c_double),
+                                                           ("contour_points", C.c_int64),
+                                                           ("contour_points_ref", C.c_int64)]
 
     def as_dict(self):
         return {n: getattr(self, n) for n, _ in self._fields_}

@@ -1,5 +1,7 @@
 """analyze_error.m diagnostics as a device reduction (needs a GB300), against
-a numpy statement of the same definitions on periodic grids."""
+a numpy statement of the same definitions on periodic grids, including the
+script's interface position error (Local_code/level-set_MPI_3D/scripts/
+analyze_error.m:51-84) by brute-force nearest points."""
 import numpy as np
 import pytest
 
@@ -48,6 +50,46 @@ def np_diagnostics(G, R, h):
             "iface_mean": dists.mean(), "iface_max": dists.max(), "iface_points": dists.size}
 
 
+def np_contour_points(F, h):
+    """The zero contour as analyze_error.m takes it from contourc: the linear-
+    interpolation crossings on the grid edges between interior cells (no
+    wrap-around edge), one point per edge whose values change sign (one < 0,
+    the other >= 0), in coordinates (i dx, j dy, k dz).  Rows (x, y, z)."""
+    dim = F.ndim
+    out = []
+    for ax in range(dim):  # spatial axis 0 = x = the last numpy axis
+        a = dim - 1 - ax
+        lo = tuple(slice(0, -1) if q == a else slice(None) for q in range(dim))
+        hi = tuple(slice(1, None) if q == a else slice(None) for q in range(dim))
+        p0, p1 = F[lo], F[hi]
+        m = (p0 < 0) != (p1 < 0)
+        idx = np.nonzero(m)
+        t = p0[m] / (p0[m] - p1[m])
+        cols = []
+        for sp in range(3):
+            if sp >= dim:
+                cols.append(np.zeros(t.size))
+                continue
+            i = idx[dim - 1 - sp].astype(np.float64)
+            cols.append((i + t) * h[sp] if sp == ax else i * h[sp])
+        out.append(np.stack(cols, 1))
+    return np.concatenate(out)
+
+
+def np_interface_error(A, B):
+    """analyze_error.m:62-77: nearest-point distances both ways (brute force),
+    Hausdorff = the largest, mean over both sets together."""
+    def nearest(P, Q):
+        d = np.empty(len(P))
+        for s in range(0, len(P), 128):
+            e = Q[None, :, :] - P[s:s + 128, None, :]
+            d2 = (e[..., 0] * e[..., 0] + e[..., 1] * e[..., 1]) + e[..., 2] * e[..., 2]
+            d[s:s + 128] = np.sqrt(d2.min(1))
+        return d
+    da, db = nearest(A, B), nearest(B, A)
+    return max(da.max(), db.max()), np.concatenate([da, db]).mean()
+
+
 @pytest.mark.parametrize("dim,n,prec", [(3, (40, 36, 44), "f64"), (3, (40, 36, 44), "f32"), (2, (96, 80, 1), "f64")])
 def test_diagnostics_match_numpy(cuda, lsgb_mod, dim, n, prec):
     from lsgb import synthetic as syn
@@ -74,3 +116,31 @@ def test_diagnostics_match_numpy(cuda, lsgb_mod, dim, n, prec):
             assert d[k] == v, k
         else:
             assert d[k] == pytest.approx(v, rel=1e-9, abs=1e-15), k
+    # the script's interface position error: device bins vs brute force
+    A = np_contour_points(Gt, h)
+    B = np_contour_points(np.ascontiguousarray(G[inner]), h)
+    haus, mean = np_interface_error(A, B)
+    assert (d["contour_points"], d["contour_points_ref"]) == (len(A), len(B))
+    assert d["contour_hausdorff"] == pytest.approx(haus, rel=1e-12)
+    assert d["contour_mean"] == pytest.approx(mean, rel=1e-12)
+    assert 0 < d["contour_mean"] <= d["contour_hausdorff"]
+
+
+def test_contour_distance_far_apart_and_empty(cuda, lsgb_mod):
+    """Two discs far apart (the search must widen past many empty bins), and a
+    field without a zero contour (the script's "could not extract" case: NaN)."""
+    n = 64
+    h = 1.0 / n
+    y, x = np.meshgrid(np.arange(n) * h, np.arange(n) * h, indexing="ij")
+    G = np.sqrt((x - 0.2) ** 2 + (y - 0.25) ** 2) - 0.1
+    R = np.sqrt((x - 0.75) ** 2 + (y - 0.7) ** 2) - 0.15
+    p = lsgb_mod.params(2, n, n, 1)
+    with lsgb_mod.Solver(p, "f64") as s:
+        s.set_fields(np.ascontiguousarray(np.pad(G, 3, mode="wrap")), layout="ghosted")
+        d = s.diagnostics(np.ascontiguousarray(R), layout="compact")
+        haus, mean = np_interface_error(np_contour_points(G, (h, h)), np_contour_points(R, (h, h)))
+        assert d["contour_hausdorff"] == pytest.approx(haus, rel=1e-12)
+        assert d["contour_mean"] == pytest.approx(mean, rel=1e-12)
+        assert d["contour_mean"] > 0.3
+        d = s.diagnostics(np.ascontiguousarray(np.ones((n, n))), layout="compact")
+        assert d["contour_points_ref"] == 0 and np.isnan(d["contour_hausdorff"]) and np.isnan(d["contour_mean"])
