@@ -254,10 +254,11 @@ LSGB_API int lsgb_solver_enable_timing(lsgb_solver* s, int enable);
 LSGB_API int lsgb_solver_kernel_times(lsgb_solver* s, double* stage_ms, int64_t* stage_launches,
                                       double* reinit_ms, int64_t* reinit_launches);
 
-/* Tile shape of the FP32 3D stage kernel: the z-chunk length (16, 32, 64);
- * 0 = default (the chunk length that fills the GPU's SMs best for the grid).
- * Every shape gives bit-identical results; only the speed differs.  The 2D
- * FP32 kernel and the FP64 kernels have one shape: 0 only. */
+/* Tile shape of the FP32 stage kernels.  3D: the z-chunk length (16, 32,
+ * 64); 0 = default (the chunk length that fills the GPU's SMs best for the
+ * grid).  2D: the tile height (32: 32 x 32 tiles, the default; 16: 32 x 16).
+ * Every shape gives bit-identical results; only the speed differs.  The FP64
+ * kernels have one shape: 0 only. */
 LSGB_API int lsgb_solver_set_tile(lsgb_solver* s, int tile);
 LSGB_API int lsgb_solver_get_tile(const lsgb_solver* s, int* tile);
 
@@ -278,11 +279,21 @@ LSGB_API int lsgb_solver_autotune(lsgb_solver* s, int reps, int* best_tile, floa
  * Batches: many independent instances (any mix of 2D and 3D sizes, one
  * precision) advanced together.  Instances keep their own lsgb_solver handle
  * for fields, reductions and output; lsgb_batch_advance runs all of them with
- * one captured CUDA graph per reinit period, the instances spread over
- * n_lanes concurrent streams.  Instances must share the step counter and the
- * reinit cadence.  Each instance's result equals its single-instance run bit
- * for bit.  Not in the reference (its variants run one instance per process).
+ * one captured CUDA graph per reinit period.  Instances must share the step
+ * counter and the reinit cadence.  Each instance's result equals its
+ * single-instance run bit for bit.  Not in the reference (its variants run
+ * one instance per process, e.g. the sweep of sample/submit_all.sh:9-11).
+ * Two forms of the graph:
+ *   LSGB_BATCH_GROUPED (default; FP32, every instance < 2^31 cells, one HCR-2
+ *     pseudo-step count): one kernel launch per RK3 stage, per pseudo-step
+ *     and for the copy back, for all 3D instances, and one for all 2D ones;
+ *     the kernels walk a block / tile list that spans the instances, with
+ *     each instance's fields and coefficients in a descriptor table;
+ *   LSGB_BATCH_LANES (FP64 batches, or on request): each instance's own
+ *     launches, spread over n_lanes concurrent streams.
  * ------------------------------------------------------------------------ */
+#define LSGB_BATCH_GROUPED 0
+#define LSGB_BATCH_LANES 1
 typedef struct lsgb_batch lsgb_batch;
 LSGB_API int lsgb_batch_create(int precision, int n_lanes, lsgb_batch** out);
 LSGB_API int lsgb_batch_destroy(lsgb_batch* b);
@@ -292,8 +303,13 @@ LSGB_API int lsgb_batch_size(const lsgb_batch* b, int* n);
 LSGB_API int lsgb_batch_solver(lsgb_batch* b, int index, lsgb_solver** out);
 /* lsgb_solver_autotune on every instance, then (FP32) each uniform z-chunk
  * (16, 32, 64) for the 3D instances against that, timed as one stage of the
- * whole batch over its lanes; the fastest assignment of tiles stays. */
+ * whole batch, and in the grouped form the 2D tile height (32 x 32 or
+ * 32 x 16 tiles), timed as one grouped 2D stage; the fastest choices stay. */
 LSGB_API int lsgb_batch_autotune(lsgb_batch* b, int reps);
+/* Request a form (LSGB_BATCH_GROUPED / LSGB_BATCH_LANES); get_mode reports
+ * the form the next advance uses (grouped only where it applies). */
+LSGB_API int lsgb_batch_set_mode(lsgb_batch* b, int mode);
+LSGB_API int lsgb_batch_get_mode(const lsgb_batch* b, int* mode);
 /* Advance every instance n_steps steps (asynchronous on the batch stream;
  * later calls on an instance's own handle are ordered after it). */
 LSGB_API int lsgb_batch_advance(lsgb_batch* b, int n_steps);

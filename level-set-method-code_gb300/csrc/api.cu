@@ -991,8 +991,11 @@ namespace {
 
 // Tile shapes the FP32 kernels accept: the z-chunk length of the 3D tiles.
 // The 2D FP32 kernel (32 x 32 tiles) and the FP64 kernels have one shape.
+// Tile choices of the FP32 stage kernels: the 3D z-chunk (16, 32, 64 planes)
+// and the 2D tile height (32: 32 x 32 tiles, 16: 32 x 16).
 int tile_candidates(const lsgb_solver* s, int* c) {
-    if (s->prec != LSGB_PREC_F32 || s->p.dim != 3) return 0;
+    if (s->prec != LSGB_PREC_F32) return 0;
+    if (s->p.dim == 2) { c[0] = 32; c[1] = 16; return 2; }
     c[0] = 16; c[1] = 32; c[2] = 64; return 3;
 }
 
@@ -1081,6 +1084,22 @@ struct lsgb_batch {
     cudaGraphExec_t block = nullptr;  // one reinit period of steps for every instance
     int block_len = 0;
     int64_t graph_launches = 0, graph_kernels = 0;
+    // grouped form (FP32): one launch per stage / pseudo-step / copy for all
+    // instances of one dimensionality, driven by descriptor tables
+    int mode = LSGB_BATCH_GROUPED;
+    bool grouped = false;             // the captured graph uses the grouped launches
+    int shape2 = 32;                  // 2D tile height of the grouped launches
+    std::vector<int> i3, i2;          // instance indices by dimensionality
+    std::vector<char> h_tab;
+    void* d_tab = nullptr;
+    size_t d_tab_bytes = 0;
+    // table layout: descriptors (3D stage, 2D stage, 3D / 2D HCR-2), then the
+    // owner tables (block / tile -> instance) of each launch kind
+    size_t off3 = 0, off2 = 0, offr3 = 0, offr2 = 0;
+    size_t oo3 = 0, oo2 = 0, oor3 = 0, oor2 = 0, ooc3 = 0, ooc2 = 0;
+    long long blk3 = 0, tiles2 = 0, rblk3 = 0, rblk2 = 0, cblk3 = 0, cblk2 = 0;
+    int iters = 0;                    // HCR-2 pseudo-steps (uniform over the batch)
+    std::vector<long long> sig;       // launch shapes the captured graph was made with
 };
 
 namespace {
@@ -1135,6 +1154,153 @@ int batch_launch_steps(lsgb_batch* b, int n_steps) {
     return LSGB_OK;
 }
 
+// The grouped form applies when every instance is FP32 with fewer than 2^31
+// cells and all share the HCR-2 pseudo-step count.
+bool batch_grouped_ok(const lsgb_batch* b) {
+    if (b->mode != LSGB_BATCH_GROUPED || b->prec != LSGB_PREC_F32 || b->inst.empty()) return false;
+    for (const lsgb_solver* s : b->inst) {
+        if (s->g.cells() >= (1LL << 31) - 1 || s->vel_live) return false;
+        if (s->p.enable_reinit && s->p.reinit_iterations != b->inst[0]->p.reinit_iterations) return false;
+    }
+    return true;
+}
+
+size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+// Fill and upload the descriptor tables from the instances' current
+// parameters (dt, S_L, tiles).  Ordered on the batch stream before the
+// launches that read it.  3D instances go longest blocks first (the block
+// scheduler starts blocks roughly in index order, so the short blocks of
+// small instances fill the tail of the launch).
+int batch_tables(lsgb_batch* b) {
+    b->i3.clear();
+    b->i2.clear();
+    for (size_t i = 0; i < b->inst.size(); ++i) (b->inst[i]->p.dim == 3 ? b->i3 : b->i2).push_back((int)i);
+    auto gi = [&](int i) {
+        lsgb_solver* s = b->inst[i];
+        GroupInst e;
+        e.a = stage_args(s->p, s->g, s->lay);
+        velocity_args(s, e.a);
+        e.a.sl = s->sl;
+        e.a.err = err_flag(s);
+        e.a.tile = s->tile;
+        e.G = (float*)s->G;
+        e.A = (float*)s->A;
+        e.B = (float*)s->B;
+        e.dtau = s->p.reinit_dtau;
+        e.beta = s->p.reinit_beta;
+        return e;
+    };
+    std::vector<GroupInst> g3, g2;
+    for (int i : b->i3) g3.push_back(gi(i));
+    for (int i : b->i2) g2.push_back(gi(i));
+    {
+        std::vector<size_t> ord(g3.size());
+        for (size_t q = 0; q < ord.size(); ++q) ord[q] = q;
+        std::stable_sort(ord.begin(), ord.end(), [&](size_t x, size_t y) {
+            const int px = stage3d_chunk_planes(g3[x].a), py = stage3d_chunk_planes(g3[y].a);
+            return px != py ? px > py : g3[x].a.g.cells() > g3[y].a.g.cells();
+        });
+        std::vector<GroupInst> g(g3.size());
+        std::vector<int> ix(g3.size());
+        for (size_t q = 0; q < ord.size(); ++q) { g[q] = g3[ord[q]]; ix[q] = b->i3[ord[q]]; }
+        g3.swap(g);
+        b->i3.swap(ix);
+    }
+    const int n3 = (int)g3.size(), n2 = (int)g2.size();
+    std::vector<char> d3(group3_desc_bytes() * n3 + 64), d2(group2_desc_bytes() * n2 + 64);
+    std::vector<char> r3(groupr_desc_bytes() * n3 + 64), r2(groupr_desc_bytes() * n2 + 64);
+    auto al64 = [](std::vector<char>& v) { return v.data() + ((64 - ((uintptr_t)v.data() & 63)) & 63); };
+    std::vector<int> o3, o2, or3, or2, oc3, oc2;
+    if (n3) group3_fill(g3.data(), n3, al64(d3), o3);
+    if (n2) group2_fill(g2.data(), n2, b->shape2, al64(d2), o2);
+    if (n3) groupr_fill(g3.data(), n3, al64(r3), or3, oc3);
+    if (n2) groupr_fill(g2.data(), n2, al64(r2), or2, oc2);
+    b->blk3 = (long long)o3.size();
+    b->tiles2 = (long long)o2.size();
+    b->rblk3 = (long long)or3.size();
+    b->rblk2 = (long long)or2.size();
+    b->cblk3 = (long long)oc3.size();
+    b->cblk2 = (long long)oc2.size();
+    for (long long x : {b->blk3, b->tiles2, b->rblk3, b->rblk2, b->cblk3, b->cblk2})
+        if (x > 0x7fffffffLL) return fail(LSGB_ERR_UNSUPPORTED, "batch too large for one grouped launch");
+    b->iters = b->inst[0]->p.enable_reinit ? b->inst[0]->p.reinit_iterations : 0;
+    size_t off = 0;
+    auto place = [&](size_t bytes) { const size_t o = off; off = align256(off + bytes); return o; };
+    b->off3 = place(group3_desc_bytes() * n3);
+    b->off2 = place(group2_desc_bytes() * n2);
+    b->offr3 = place(groupr_desc_bytes() * n3);
+    b->offr2 = place(groupr_desc_bytes() * n2);
+    b->oo3 = place(sizeof(int) * o3.size());
+    b->oo2 = place(sizeof(int) * o2.size());
+    b->oor3 = place(sizeof(int) * or3.size());
+    b->oor2 = place(sizeof(int) * or2.size());
+    b->ooc3 = place(sizeof(int) * oc3.size());
+    b->ooc2 = place(sizeof(int) * oc2.size());
+    const size_t total = off;
+    b->h_tab.assign(total + 64, 0);  // the descriptors hold 64-byte aligned tensor maps
+    char* h = al64(b->h_tab);
+    std::memcpy(h + b->off3, al64(d3), group3_desc_bytes() * n3);
+    std::memcpy(h + b->off2, al64(d2), group2_desc_bytes() * n2);
+    std::memcpy(h + b->offr3, al64(r3), groupr_desc_bytes() * n3);
+    std::memcpy(h + b->offr2, al64(r2), groupr_desc_bytes() * n2);
+    std::memcpy(h + b->oo3, o3.data(), sizeof(int) * o3.size());
+    std::memcpy(h + b->oo2, o2.data(), sizeof(int) * o2.size());
+    std::memcpy(h + b->oor3, or3.data(), sizeof(int) * or3.size());
+    std::memcpy(h + b->oor2, or2.data(), sizeof(int) * or2.size());
+    std::memcpy(h + b->ooc3, oc3.data(), sizeof(int) * oc3.size());
+    std::memcpy(h + b->ooc2, oc2.data(), sizeof(int) * oc2.size());
+    if (total > b->d_tab_bytes) {
+        if (b->d_tab) cudaFree(b->d_tab);
+        b->d_tab = nullptr;
+        b->d_tab_bytes = 0;
+        cudaError_t e = cudaMalloc(&b->d_tab, total);
+        if (e != cudaSuccess) return fail(LSGB_ERR_ALLOC, "batch tables: %s", cudaGetErrorString(e));
+        b->d_tab_bytes = total;
+    }
+    LSGB_CUDA(cudaMemcpyAsync(b->d_tab, h, total, cudaMemcpyHostToDevice, b->main));
+    return LSGB_OK;
+}
+
+// Steps of the grouped form, with the reference main loop's reinit cadence
+// (the instances share the step counter).  The 3D and the 2D instances form
+// two independent chains of launches; they run on two of the batch's streams
+// (forked from and joined back into the batch stream), so the 2D launches
+// fill the GPU beside the 3D ones.
+int batch_launch_steps_grouped(lsgb_batch* b, int n_steps) {
+    const char* d = (const char*)b->d_tab;
+    const int n3 = (int)b->i3.size(), n2 = (int)b->i2.size();
+    cudaStream_t s3 = b->lanes[0], s2 = b->lanes.size() > 1 ? b->lanes[1] : b->lanes[0];
+    LSGB_CUDA(cudaEventRecord(b->fork, b->main));
+    LSGB_CUDA(cudaStreamWaitEvent(s3, b->fork, 0));
+    if (s2 != s3) LSGB_CUDA(cudaStreamWaitEvent(s2, b->fork, 0));
+    const int* o3 = (const int*)(d + b->oo3);
+    const int* o2 = (const int*)(d + b->oo2);
+    for (int q = 0; q < n_steps; ++q) {
+        for (int stage = 1; stage <= 3; ++stage) {
+            LSGB_CUDA(launch_stage3d_f32_group(d + b->off3, o3, n3, b->blk3, stage, s3));
+            LSGB_CUDA(launch_stage2d_f32_group(d + b->off2, o2, n2, b->tiles2, stage, b->shape2, s2));
+        }
+        const lsgb_solver* f = b->inst[0];
+        if (f->p.enable_reinit && f->step > 0 && f->step % f->p.reinit_interval == 0 && b->iters > 0) {
+            for (int it = 0; it < b->iters; ++it) {
+                LSGB_CUDA(launch_reinit_f32_group(d + b->offr3, (const int*)(d + b->oor3), n3, b->rblk3, 3, it, s3));
+                LSGB_CUDA(launch_reinit_f32_group(d + b->offr2, (const int*)(d + b->oor2), n2, b->rblk2, 2, it, s2));
+            }
+            LSGB_CUDA(launch_copy_back_group(d + b->offr3, (const int*)(d + b->ooc3), n3, b->cblk3, b->iters, s3));
+            LSGB_CUDA(launch_copy_back_group(d + b->offr2, (const int*)(d + b->ooc2), n2, b->cblk2, b->iters, s2));
+        }
+        for (lsgb_solver* s : b->inst) s->step++;
+    }
+    LSGB_CUDA(cudaEventRecord(b->lane_done[0], s3));
+    LSGB_CUDA(cudaStreamWaitEvent(b->main, b->lane_done[0], 0));
+    if (s2 != s3) {
+        LSGB_CUDA(cudaEventRecord(b->lane_done[1], s2));
+        LSGB_CUDA(cudaStreamWaitEvent(b->main, b->lane_done[1], 0));
+    }
+    return LSGB_OK;
+}
+
 }  // namespace
 
 extern "C" int lsgb_batch_create(int precision, int n_lanes, lsgb_batch** out) {
@@ -1167,6 +1333,7 @@ extern "C" int lsgb_batch_destroy(lsgb_batch* b) {
     if (!b) return LSGB_OK;
     if (b->main) cudaStreamSynchronize(b->main);
     batch_drop_graph(b);
+    if (b->d_tab) cudaFree(b->d_tab);
     for (lsgb_solver* s : b->inst) lsgb_solver_destroy(s);
     for (cudaStream_t l : b->lanes) cudaStreamDestroy(l);
     for (cudaEvent_t ev : b->lane_done) cudaEventDestroy(ev);
@@ -1244,11 +1411,87 @@ int batch_time_stage1(lsgb_batch* b, int reps, float* ms) {
 
 }  // namespace
 
+namespace {
+
+// One grouped RK3 stage-1 launch (G -> A, the state is not touched) of the
+// batch's 3D (dim 3) or 2D instances, `reps` times; CUDA-event time per
+// repetition on the batch stream.
+int batch_time_group(lsgb_batch* b, int dim, int reps, float* ms) {
+    LSGB_TRY(batch_tables(b));
+    cudaEvent_t e0, e1;
+    LSGB_CUDA(cudaEventCreate(&e0));
+    LSGB_CUDA(cudaEventCreate(&e1));
+    const char* d = (const char*)b->d_tab;
+    cudaError_t e = cudaEventRecord(e0, b->main);
+    for (int r = 0; r < reps && e == cudaSuccess; ++r)
+        e = dim == 3 ? launch_stage3d_f32_group(d + b->off3, (const int*)(d + b->oo3), (int)b->i3.size(), b->blk3, 1,
+                                                b->main)
+                     : launch_stage2d_f32_group(d + b->off2, (const int*)(d + b->oo2), (int)b->i2.size(), b->tiles2, 1,
+                                                b->shape2, b->main);
+    if (e == cudaSuccess) e = cudaEventRecord(e1, b->main);
+    if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+    float t = 0.0f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&t, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (e != cudaSuccess) return fail(LSGB_ERR_CUDA, "batch timing: %s", cudaGetErrorString(e));
+    *ms = t / (reps > 0 ? reps : 1);
+    return LSGB_OK;
+}
+
+// Grouped form: the per-instance 3D z-chunks from the single-instance tuning
+// against each uniform chunk, timed as one grouped 3D launch; then the 2D
+// tile height, timed as one grouped 2D launch.  The fastest choices stay.
+int batch_autotune_grouped(lsgb_batch* b, int reps) {
+    std::vector<int> tuned(b->inst.size());
+    for (size_t i = 0; i < b->inst.size(); ++i) tuned[i] = b->inst[i]->tile;
+    bool any3 = false, any2 = false;
+    for (const lsgb_solver* s : b->inst) (s->p.dim == 3 ? any3 : any2) = true;
+    float t = 0.0f, best = 0.0f;
+    if (any3) {
+        std::vector<int> pick = tuned;
+        LSGB_TRY(batch_time_group(b, 3, 1, &t));  // warm-up
+        LSGB_TRY(batch_time_group(b, 3, reps, &best));
+        for (int zc : {16, 32, 64}) {
+            for (lsgb_solver* s : b->inst)
+                if (s->p.dim == 3) s->tile = zc;
+            LSGB_TRY(batch_time_group(b, 3, reps, &t));
+            if (t < best) {
+                best = t;
+                for (size_t i = 0; i < b->inst.size(); ++i) pick[i] = b->inst[i]->tile;
+            }
+        }
+        for (size_t i = 0; i < b->inst.size(); ++i)
+            if (b->inst[i]->p.dim == 3) b->inst[i]->tile = pick[i];
+    }
+    if (any2) {
+        int pick = 32;
+        for (int shape : {32, 16}) {
+            b->shape2 = shape;
+            if (shape == 32) LSGB_TRY(batch_time_group(b, 2, 1, &t));  // warm-up
+            LSGB_TRY(batch_time_group(b, 2, reps, &t));
+            if (shape == 32 || t < best) {
+                best = t;
+                pick = shape;
+            }
+        }
+        b->shape2 = pick;
+        for (lsgb_solver* s : b->inst)
+            if (s->p.dim == 2) s->tile = pick;
+    }
+    LSGB_TRY(batch_tables(b));
+    for (lsgb_solver* s : b->inst) LSGB_TRY(check_flag(s));
+    return LSGB_OK;
+}
+
+}  // namespace
+
 // Tiles for throughput of the whole batch: every instance's fastest shape
-// alone (lsgb_solver_autotune), then each uniform z-chunk for the 3D
-// instances, timed together over the lanes; the fastest assignment stays.
-// (Alone, short chunks win by filling the SMs; run together, the lanes fill
-// them and long chunks win by their smaller halo overhead.)
+// alone (lsgb_solver_autotune), then the choices that apply to the batch as
+// a whole, timed together.  Grouped form: batch_autotune_grouped.  Lanes
+// form: each uniform z-chunk for the 3D instances over the lanes.  (Alone,
+// short chunks win by filling the SMs; run together, the instances fill them
+// and long chunks win by their smaller halo overhead.)
 extern "C" int lsgb_batch_autotune(lsgb_batch* b, int reps) {
     LSGB_TRY(batch_ok(b));
     for (lsgb_solver* s : b->inst)
@@ -1259,6 +1502,7 @@ extern "C" int lsgb_batch_autotune(lsgb_batch* b, int reps) {
     for (lsgb_solver* s : b->inst)
         if (!s->have_G || !s->have_vel) return LSGB_OK;
     if (reps < 1) reps = 3;
+    if (batch_grouped_ok(b)) return batch_autotune_grouped(b, reps);
     std::vector<int> best(b->inst.size());
     for (size_t i = 0; i < b->inst.size(); ++i) best[i] = b->inst[i]->tile;
     float t_best = 0.0f;
@@ -1304,9 +1548,25 @@ extern "C" int lsgb_batch_advance(lsgb_batch* b, int n_steps) {
     // period starts at a step s with s % interval == 1 (the reinit then runs
     // after its last step), so its launch sequence is the same every time and
     // one captured graph replays it.
+    // grouped form: refresh the descriptor tables (dt, S_L, tiles may have
+    // changed); a captured graph stays valid while the launch shapes do
+    const bool grouped = batch_grouped_ok(b);
+    if (grouped) {
+        LSGB_TRY(batch_tables(b));
+        const std::vector<long long> sig = {b->blk3, b->tiles2, b->rblk3, b->rblk2, b->cblk3, b->cblk2,
+                                            (long long)b->shape2, (long long)b->iters,
+                                            (long long)b->i3.size(), (long long)b->i2.size()};
+        if (b->block && (!b->grouped || sig != b->sig)) batch_drop_graph(b);
+        b->sig = sig;
+    } else if (b->block && b->grouped) {
+        batch_drop_graph(b);
+    }
+    auto launch = [&](int n) -> int {
+        return grouped ? batch_launch_steps_grouped(b, n) : batch_launch_steps(b, n);
+    };
     int remaining = n_steps;
     auto direct = [&](int n) -> int {
-        LSGB_TRY(batch_launch_steps(b, n));
+        LSGB_TRY(launch(n));
         remaining -= n;
         return LSGB_OK;
     };
@@ -1323,7 +1583,7 @@ extern "C" int lsgb_batch_advance(lsgb_batch* b, int n_steps) {
             for (lsgb_solver* s : b->inst) steps0.push_back(s->step);
             uint64_t k0 = lsgb_launch_count();
             LSGB_CUDA(cudaStreamBeginCapture(b->main, cudaStreamCaptureModeThreadLocal));
-            int rc = batch_launch_steps(b, L);
+            int rc = launch(L);
             cudaGraph_t graph = nullptr;
             cudaError_t e = cudaStreamEndCapture(b->main, &graph);
             for (size_t i = 0; i < b->inst.size(); ++i) b->inst[i]->step = steps0[i];
@@ -1333,6 +1593,7 @@ extern "C" int lsgb_batch_advance(lsgb_batch* b, int n_steps) {
             cudaGraphDestroy(graph);
             if (e != cudaSuccess) { b->block = nullptr; return fail(LSGB_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e)); }
             b->block_len = L;
+            b->grouped = grouped;
             b->graph_kernels = (int64_t)(lsgb_launch_count() - k0);
             uncount_launches((uint64_t)b->graph_kernels);
         }
@@ -1348,6 +1609,21 @@ extern "C" int lsgb_batch_advance(lsgb_batch* b, int n_steps) {
     // later calls on an instance's own stream see the batch's results
     LSGB_CUDA(cudaEventRecord(b->done, b->main));
     for (lsgb_solver* s : b->inst) LSGB_CUDA(cudaStreamWaitEvent(s->st, b->done, 0));
+    return LSGB_OK;
+}
+
+extern "C" int lsgb_batch_set_mode(lsgb_batch* b, int mode) {
+    LSGB_TRY(batch_ok(b));
+    if (mode != LSGB_BATCH_GROUPED && mode != LSGB_BATCH_LANES) return fail(LSGB_ERR_INVALID, "unknown batch mode %d", mode);
+    if (mode != b->mode) batch_drop_graph(b);
+    b->mode = mode;
+    return LSGB_OK;
+}
+
+extern "C" int lsgb_batch_get_mode(const lsgb_batch* b, int* mode) {
+    LSGB_TRY(batch_ok(b));
+    if (!mode) return fail(LSGB_ERR_INVALID, "mode is NULL");
+    *mode = batch_grouped_ok(b) ? LSGB_BATCH_GROUPED : LSGB_BATCH_LANES;
     return LSGB_OK;
 }
 

@@ -14,6 +14,7 @@
 #include <cuda_runtime.h>
 #include <cstdint>
 #include <cstdio>
+#include <vector>
 
 #include "../../include/lsgb.h"
 
@@ -121,6 +122,43 @@ bool stage3d_f32_fuses_deformation(const Geo& g);
 cudaError_t launch_stage2d_f32_tiled(const StageArgs& a, cudaStream_t st);
 cudaError_t launch_reinit_f64(const ReinitArgs& a, cudaStream_t st);
 cudaError_t launch_reinit_f32(const ReinitArgs& a, cudaStream_t st);
+
+// Grouped launches of a batch (FP32, compact, < 2^31 cells per instance):
+// one launch runs a stage (or an HCR-2 pseudo-step, or the copy back) of
+// every instance of one dimensionality.  The host fills one descriptor per
+// instance (*_fill returns the launch's blocks or tiles), copies the table to
+// the device, and launches with the device table.
+struct GroupInst {
+    StageArgs a;        // geometry, physics, velocity, S_L, tile choice, error flag
+    float *G, *A, *B;   // the instance's fixed buffers (stage 1 G->A, 2 A->B, 3 B->G)
+    double dtau, beta;  // HCR-2 pseudo-step
+};
+// Each *_fill writes the descriptors and appends, for every block (tile) of
+// the launch, the index of its instance to `owner` (a lookup table the
+// kernels read once per block / tile).
+size_t group3_desc_bytes();
+// Planes one CTA of this 3D instance marches (its z-chunk, or nz if shorter)
+int stage3d_chunk_planes(const StageArgs& a);
+void group3_fill(const GroupInst* in, int n, void* host_table, std::vector<int>& owner);
+cudaError_t launch_stage3d_f32_group(const void* table, const int* owner, int n, long long blocks, int stage,
+                                     cudaStream_t st);
+// 2D: shape 32 (32 x 32 tiles) or 16 (32 x 16 tiles), one shape per launch
+size_t group2_desc_bytes();
+void group2_fill(const GroupInst* in, int n, int shape, void* host_table, std::vector<int>& owner);
+cudaError_t launch_stage2d_f32_group(const void* table, const int* owner, int n, long long tiles, int stage,
+                                     int shape, cudaStream_t st);
+// HCR-2 pseudo-step `iter` (0-based) of every instance: iter 0 reads G, iter
+// m > 0 reads the buffer pseudo-step m-1 wrote (A for even m-1, B for odd);
+// iteration m writes A (m even) or B (m odd).  The copy back sets G to the
+// last pseudo-step's buffer (iters pseudo-steps ran).  All instances of one
+// table have the same dimensionality.
+size_t groupr_desc_bytes();
+void groupr_fill(const GroupInst* in, int n, void* host_table, std::vector<int>& owner,
+                 std::vector<int>& copy_owner);
+cudaError_t launch_reinit_f32_group(const void* table, const int* owner, int n, long long blocks, int dim, int iter,
+                                    cudaStream_t st);
+cudaError_t launch_copy_back_group(const void* table, const int* copy_owner, int n, long long copy_blocks, int iters,
+                                   cudaStream_t st);
 
 // Ghost fill of a ghosted FP64 array from its interior (periodic images /
 // zero-gradient copies), the state the reference's boundary fill leaves.

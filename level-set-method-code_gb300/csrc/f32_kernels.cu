@@ -107,12 +107,10 @@ constexpr int RT = 256;  // threads of a pseudo-step block
 // memory and finishes them with dense lanes after the FP32 pass: a warp that
 // holds one forced cell no longer runs the FP64 sequence for all 32 lanes.
 template <int DIM, typename IDX>
-__global__ void __launch_bounds__(RT) reinit_f32_kernel(Geo g, const float* __restrict__ phin,
-                                                        const float* __restrict__ phi0,
-                                                        float* __restrict__ phinew, float inv_dx,
-                                                        float inv_dy, float inv_dz, float dx2,
-                                                        float dtau_f, double dx, double dtau,
-                                                        double beta) {
+__device__ __forceinline__ void reinit_f32_body(const Geo& g, const float* __restrict__ phin,
+                                                const float* __restrict__ phi0, float* __restrict__ phinew,
+                                                float inv_dx, float inv_dy, float inv_dz, float dx2, float dtau_f,
+                                                double dx, double dtau, double beta, int bx, int by, int bz) {
     __shared__ int nq;
     __shared__ IDX q_id[RT];
     __shared__ int q_flag[RT];
@@ -121,9 +119,9 @@ __global__ void __launch_bounds__(RT) reinit_f32_kernel(Geo g, const float* __re
     const int t = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
     if (t == 0) nq = 0;
     __syncthreads();
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    int j = blockIdx.y * blockDim.y + threadIdx.y;
-    int k = DIM == 3 ? blockIdx.z * blockDim.z + threadIdx.z : 0;
+    int i = bx * blockDim.x + threadIdx.x;
+    int j = by * blockDim.y + threadIdx.y;
+    int k = DIM == 3 ? bz * blockDim.z + threadIdx.z : 0;
     if (i < g.nx && j < g.ny && k < g.nz) {
         const IDX sy = g.nx;
         const IDX sz = (IDX)g.nx * g.ny;
@@ -176,6 +174,58 @@ __global__ void __launch_bounds__(RT) reinit_f32_kernel(Geo g, const float* __re
     }
 }
 
+template <int DIM, typename IDX>
+__global__ void __launch_bounds__(RT) reinit_f32_kernel(Geo g, const float* __restrict__ phin,
+                                                        const float* __restrict__ phi0,
+                                                        float* __restrict__ phinew, float inv_dx,
+                                                        float inv_dy, float inv_dz, float dx2,
+                                                        float dtau_f, double dx, double dtau,
+                                                        double beta) {
+    reinit_f32_body<DIM, IDX>(g, phin, phi0, phinew, inv_dx, inv_dy, inv_dz, dx2, dtau_f, dx, dtau, beta,
+                              blockIdx.x, blockIdx.y, blockIdx.z);
+}
+
+// One instance of the grouped HCR-2 and copy-back launches: buffers, the
+// pseudo-step coefficients, its block grid (gx x gy x gz cell blocks) and its
+// first block in the pseudo-step and copy launches.
+struct GroupR {
+    Geo g;
+    float *G, *A, *B;
+    float inv_dx, inv_dy, inv_dz, dx2, dtau_f;
+    double dx, dtau, beta;
+    int gx, gy, blk0, cblk0;
+};
+
+constexpr int CPB = 4096;  // floats per block of the copy back
+
+// Grouped HCR-2 pseudo-step `iter` of every instance (same dimensionality);
+// block b belongs to instance owner[b].
+template <int DIM>
+__global__ void __launch_bounds__(RT) reinit_f32_group(const GroupR* __restrict__ ins, const int* __restrict__ owner,
+                                                       int iter) {
+    const GroupR* d = ins + owner[blockIdx.x];
+    int l = (int)blockIdx.x - d->blk0;
+    const int bx = l % d->gx;
+    l /= d->gx;
+    const int by = l % d->gy;
+    const int bz = l / d->gy;
+    const float* in = iter == 0 ? d->G : ((iter - 1) & 1 ? d->B : d->A);
+    float* out = iter & 1 ? d->B : d->A;
+    reinit_f32_body<DIM, int>(d->g, in, d->G, out, d->inv_dx, d->inv_dy, d->inv_dz, d->dx2, d->dtau_f, d->dx,
+                              d->dtau, d->beta, bx, by, bz);
+}
+
+// G <- the buffer the last of `iters` pseudo-steps wrote, every instance.
+__global__ void __launch_bounds__(256) copy_back_group(const GroupR* __restrict__ ins, const int* __restrict__ owner,
+                                                       int iters) {
+    const GroupR* d = ins + owner[blockIdx.x];
+    const float* src = (iters - 1) & 1 ? d->B : d->A;
+    const long long cells = d->g.cells();
+    const long long e0 = (long long)((int)blockIdx.x - d->cblk0) * CPB;
+    const long long e1 = e0 + CPB < cells ? e0 + CPB : cells;
+    for (long long e = e0 + threadIdx.x; e < e1; e += 256) d->G[e] = src[e];
+}
+
 inline dim3 cell_block(const Geo& g) { return g.dim == 3 ? dim3(32, 4, 2) : dim3(32, 8, 1); }
 inline dim3 cell_grid(const Geo& g, dim3 b) {
     return dim3((g.nx + b.x - 1) / b.x, (g.ny + b.y - 1) / b.y, (g.nz + b.z - 1) / b.z);
@@ -206,6 +256,63 @@ cudaError_t launch_reinit_f32(const ReinitArgs& a, cudaStream_t st) {
         if (small) LSGB_R32(2, int); else LSGB_R32(2, long long);
     }
 #undef LSGB_R32
+    count_launches(1);
+    return cudaGetLastError();
+}
+
+size_t groupr_desc_bytes() { return sizeof(GroupR); }
+
+void groupr_fill(const GroupInst* in, int n, void* host_table, std::vector<int>& owner,
+                 std::vector<int>& copy_owner) {
+    GroupR* d = (GroupR*)host_table;
+    long long blk = 0, cblk = 0;
+    for (int q = 0; q < n; ++q) {
+        GroupR e;
+        memset(&e, 0, sizeof(e));
+        const StageArgs& a = in[q].a;
+        e.g = a.g;
+        e.G = in[q].G;
+        e.A = in[q].A;
+        e.B = in[q].B;
+        const double dz = a.g.dim == 3 ? a.dz : a.dx;
+        e.inv_dx = (float)(1.0 / a.dx);
+        e.inv_dy = (float)(1.0 / a.dy);
+        e.inv_dz = (float)(1.0 / dz);
+        e.dx2 = (float)(a.dx * a.dx);
+        e.dtau_f = (float)in[q].dtau;
+        e.dx = a.dx;
+        e.dtau = in[q].dtau;
+        e.beta = in[q].beta;
+        const dim3 b = cell_block(a.g), gr = cell_grid(a.g, b);
+        e.gx = (int)gr.x;
+        e.gy = (int)gr.y;
+        e.blk0 = (int)blk;
+        e.cblk0 = (int)cblk;
+        const long long nb = (long long)gr.x * gr.y * gr.z, nc = (a.g.cells() + CPB - 1) / CPB;
+        blk += nb;
+        cblk += nc;
+        owner.insert(owner.end(), (size_t)nb, q);
+        copy_owner.insert(copy_owner.end(), (size_t)nc, q);
+        d[q] = e;
+    }
+}
+
+cudaError_t launch_reinit_f32_group(const void* table, const int* owner, int n, long long blocks, int dim, int iter,
+                                    cudaStream_t st) {
+    if (n <= 0 || blocks <= 0) return cudaSuccess;
+    if (blocks > 0x7fffffffLL) return cudaErrorInvalidValue;
+    const GroupR* d = (const GroupR*)table;
+    if (dim == 3) reinit_f32_group<3><<<(unsigned)blocks, dim3(32, 4, 2), 0, st>>>(d, owner, iter);
+    else reinit_f32_group<2><<<(unsigned)blocks, dim3(32, 8, 1), 0, st>>>(d, owner, iter);
+    count_launches(1);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_copy_back_group(const void* table, const int* copy_owner, int n, long long copy_blocks, int iters,
+                                   cudaStream_t st) {
+    if (n <= 0 || copy_blocks <= 0 || iters <= 0) return cudaSuccess;
+    if (copy_blocks > 0x7fffffffLL) return cudaErrorInvalidValue;
+    copy_back_group<<<(unsigned)copy_blocks, 256, 0, st>>>((const GroupR*)table, copy_owner, iters);
     count_launches(1);
     return cudaGetLastError();
 }

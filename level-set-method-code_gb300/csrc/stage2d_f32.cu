@@ -6,11 +6,14 @@
 // (rk3.h:104-150).  Compact arrays, periodic / zero-gradient neighbours by
 // index mapping.
 //
-// Shape: a CTA of 32 x 8 threads works on 32 x 32 tiles; thread (x, ty) owns
-// rows 4 ty .. 4 ty + 3 of column x as two row pairs, and every per-cell
-// quantity is a float2 over a row pair (packed f32x2 arithmetic).  The grid
-// is persistent (as many CTAs as fit on the GPU, at most one per tile); a CTA
-// takes tiles blockIdx.x, blockIdx.x + gridDim.x, ...
+// Shape: a CTA of 32 x TY threads works on 32 x 4 TY tiles (TY = 8: 32 x 32,
+// the default; TY = 4: 32 x 16, more tiles for small grids -- the two tile
+// shapes the autotuner picks from); thread (x, ty) owns rows 4 ty .. 4 ty + 3
+// of column x as two row pairs, and every per-cell quantity is a float2 over
+// a row pair (packed f32x2 arithmetic).  The grid is persistent (as many CTAs
+// as fit on the GPU, at most one per tile); a CTA takes tiles blockIdx.x,
+// blockIdx.x + gridDim.x, ...  In the grouped form (one launch for every 2D
+// instance of a batch) the tile list runs over all instances.
 //   - The tile plus a halo (3 columns left and right, 4 rows above and below)
 //     is staged in shared memory as row pairs by asynchronous copies, double
 //     buffered: the next tile's copies are in flight while this one computes.
@@ -25,23 +28,49 @@
 #include "common.cuh"
 #include "weno_f32x2.cuh"
 
+#include <cstring>
+
 namespace lsgb {
 namespace {
 
 using namespace wf;
 
 constexpr int TX = 32;                 // tile columns (one warp's lanes)
-constexpr int TY = 8;                  // thread rows of a CTA
-constexpr int NT = TX * TY;
 constexpr int RPT = 4;                 // cell rows per thread (two row pairs)
-constexpr int BY = TY * RPT;           // tile rows
 constexpr int PW = TX + 6;             // staged columns: tile x -3 .. TX+2
-constexpr int PP = (BY + 8) / 2;       // staged row pairs: tile rows -4 .. BY+3
-constexpr int NST = PP * PW;           // staged float2 entries
-constexpr int NFX = (TX + 1) * (BY / 2);  // x faces of the tile, per row pair
+
+// Tile shape for TY thread rows per CTA.
+template <int TYV>
+struct Shape {
+    static constexpr int TY = TYV;                  // thread rows of a CTA
+    static constexpr int NT = TX * TY;
+    static constexpr int BY = TY * RPT;             // tile rows
+    static constexpr int PP = (BY + 8) / 2;         // staged row pairs: tile rows -4 .. BY+3
+    static constexpr int NST = PP * PW;             // staged float2 entries
+    static constexpr int NFX = (TX + 1) * (BY / 2); // x faces of the tile, per row pair
+};
 
 struct Coef2 {
     float inv_dx, inv_dy, inv_2dx, inv_2dy, s_l, eps, dt;
+};
+
+// One tile's work: the instance's fields and coefficients, the tile origin.
+struct Tile2 {
+    Geo g;
+    const float *Gin, *Gn, *u, *v, *sl;
+    float* Gout;
+    Coef2 c;
+    int i0, j0;
+};
+
+// One instance of a grouped launch: fixed buffers (stage 1 G -> A, 2 A -> B,
+// 3 B -> G), coefficients, tile columns and its first tile in the list.
+struct Group2 {
+    Geo g;
+    float *G, *A, *B;
+    const float *u, *v, *sl;
+    Coef2 c;
+    int ntx, tile0;
 };
 
 // Stage update of one row pair from its centre values, the neighbour
@@ -68,9 +97,10 @@ __device__ __forceinline__ float2 cell2(const Coef2& c, float2 gc, float2 gxd, f
 // Issue the asynchronous copies that stage tile (i0, j0) plus its halo into
 // P (every entry: two rows of one column).  Tiles whose halo lies inside the
 // grid copy with plain offsets, the others through the index map.
-template <typename IDX>
+template <typename IDX, typename S>
 __device__ __forceinline__ void stage_tile(float2* P, const float* __restrict__ Gin, const Geo& g, int i0, int j0,
                                            int t) {
+    constexpr int NST = S::NST, NT = S::NT, PP = S::PP;
     const IDX nx = g.nx;
     const bool inner = i0 >= 3 && i0 + PW - 3 <= g.nx && j0 >= 4 && j0 + 2 * PP - 4 <= g.ny;
     if (inner) {
@@ -92,22 +122,69 @@ __device__ __forceinline__ void stage_tile(float2* P, const float* __restrict__ 
     }
 }
 
-template <int STAGE, typename IDX>
-__global__ void __launch_bounds__(NT, 3) stage2d_f32_rows(Geo g, const float* __restrict__ Gin,
-                                                          const float* __restrict__ Gn, float* __restrict__ Gout,
-                                                          const float* __restrict__ u, const float* __restrict__ v,
-                                                          const float* __restrict__ sl, Coef2 c, int ntx,
-                                                          int ntiles) {
+// Tile sources: tile index -> Tile2.  One instance (tiles in row-major
+// order of ntx tile columns) ...
+struct OneSrc {
+    static constexpr bool kShared = false;  // cheap to evaluate: every thread does
+    Geo g;
+    const float *Gin, *Gn, *u, *v, *sl;
+    float* Gout;
+    Coef2 c;
+    int ntx, by;
+    __device__ __forceinline__ Tile2 operator()(int tile) const {
+        return Tile2{g, Gin, Gn, u, v, sl, Gout, c, (tile % ntx) * TX, (tile / ntx) * by};
+    }
+};
+
+// ... or every instance of a batch: tile t belongs to instance owner[t],
+// whose tiles start at its tile0; for RK3 stage STAGE.
+// Evaluating it costs a chain of global loads, so one thread evaluates each
+// tile's entry ahead of time and the CTA reads it from shared memory.
+template <int STAGE>
+struct GroupSrc {
+    static constexpr bool kShared = true;
+    const Group2* ins;
+    const int* owner;
+    int by;
+    __device__ __forceinline__ Tile2 operator()(int tile) const {
+        const Group2* d = ins + __ldg(owner + tile);
+        const int l = tile - d->tile0;
+        return Tile2{d->g, STAGE == 1 ? d->G : (STAGE == 2 ? d->A : d->B), d->G, d->u, d->v, d->sl,
+                     STAGE == 1 ? d->A : (STAGE == 2 ? d->B : d->G), d->c, (l % d->ntx) * TX, (l / d->ntx) * by};
+    }
+};
+
+template <int STAGE, typename IDX, int TYV, typename SRC>
+__device__ __forceinline__ void stage2d_body(const SRC& src, int ntiles) {
+    using S = Shape<TYV>;
+    constexpr int TY = S::TY, BY = S::BY, NST = S::NST, NFX = S::NFX;
     __shared__ float2 Pbuf[2][NST];        // [PP][PW]: (row 2p-4, row 2p-3) of tile column x-3
     __shared__ float2 FL[NFX], FR[NFX];    // x faces [BY/2][TX+1]
+    __shared__ Tile2 tinfo[2];             // entries of this and the next tile (kShared sources)
     const int tx = threadIdx.x, ty = threadIdx.y;
     const int t = ty * TX + tx;
-    const IDX nx = g.nx;
     int tile = blockIdx.x;
-    if (tile < ntiles) stage_tile<IDX>(Pbuf[0], Gin, g, (tile % ntx) * TX, (tile / ntx) * BY, t);
+    if (tile < ntiles) {
+        const Tile2 f = src(tile);
+        if (SRC::kShared && t == 0) tinfo[0] = f;
+        stage_tile<IDX, S>(Pbuf[0], f.Gin, f.g, f.i0, f.j0, t);
+    }
     cp_async_commit();
+    if (SRC::kShared) __syncthreads();  // tinfo[0] visible
     for (int buf = 0; tile < ntiles; tile += gridDim.x, buf ^= 1) {
-        const int i0 = (tile % ntx) * TX, j0 = (tile / ntx) * BY;
+        // the next tile's entry, read after this iteration's first barrier;
+        // its slot was last read before the previous iteration's barriers
+        if (SRC::kShared && t == 0 && tile + (int)gridDim.x < ntiles) tinfo[buf ^ 1] = src(tile + gridDim.x);
+        const Tile2 T = SRC::kShared ? tinfo[buf] : src(tile);
+        const Geo& g = T.g;
+        const Coef2& c = T.c;
+        const float* __restrict__ u = T.u;
+        const float* __restrict__ v = T.v;
+        const float* __restrict__ Gn = T.Gn;
+        const float* __restrict__ sl = T.sl;
+        float* __restrict__ Gout = T.Gout;
+        const IDX nx = g.nx;
+        const int i0 = T.i0, j0 = T.j0;
         const float2* P = Pbuf[buf];
         // point-wise fields of the own cells (rows clamped into range; rows past
         // the grid are computed but not stored)
@@ -130,7 +207,10 @@ __global__ void __launch_bounds__(NT, 3) stage2d_f32_rows(Geo g, const float* __
         __syncthreads();
         {
             const int tn = tile + gridDim.x;
-            if (tn < ntiles) stage_tile<IDX>(Pbuf[buf ^ 1], Gin, g, (tn % ntx) * TX, (tn / ntx) * BY, t);
+            if (tn < ntiles) {
+                const Tile2 f = SRC::kShared ? tinfo[buf ^ 1] : src(tn);
+                stage_tile<IDX, S>(Pbuf[buf ^ 1], f.Gin, f.g, f.i0, f.j0, t);
+            }
             cp_async_commit();
         }
 
@@ -201,29 +281,52 @@ __global__ void __launch_bounds__(NT, 3) stage2d_f32_rows(Geo g, const float* __
     }
 }
 
-template <int STAGE, typename IDX>
+template <int STAGE, typename IDX, int TYV>
+__global__ void __launch_bounds__(Shape<TYV>::NT, 24 / TYV) stage2d_f32_rows(OneSrc src, int ntiles) {
+    stage2d_body<STAGE, IDX, TYV>(src, ntiles);
+}
+
+template <int STAGE, int TYV>
+__global__ void __launch_bounds__(Shape<TYV>::NT, 24 / TYV) stage2d_f32_group(const Group2* __restrict__ ins,
+                                                                              const int* __restrict__ owner,
+                                                                              int ntiles) {
+    stage2d_body<STAGE, int, TYV>(GroupSrc<STAGE>{ins, owner, Shape<TYV>::BY}, ntiles);
+}
+
+// Resident CTAs of a kernel on the whole GPU.
+int resident_ctas(const void* kern, int threads) {
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, 0);
+    return (sms > 0 ? sms : 1) * (per_sm > 0 ? per_sm : 1);
+}
+
+template <int STAGE, typename IDX, int TYV>
 cudaError_t launch2(const StageArgs& a, const Coef2& c, cudaStream_t st) {
-    // resident CTAs of this instance on the whole GPU (queried once)
-    static const int resident = [] {
-        int dev = 0, sms = 0, per_sm = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, stage2d_f32_rows<STAGE, IDX>, NT, 0);
-        return (sms > 0 ? sms : 1) * (per_sm > 0 ? per_sm : 1);
-    }();
+    using S = Shape<TYV>;
+    static const int resident = resident_ctas((const void*)stage2d_f32_rows<STAGE, IDX, TYV>, S::NT);
     const int ntx = (a.g.nx + TX - 1) / TX;
-    const int ntiles = ntx * ((a.g.ny + BY - 1) / BY);
-    const dim3 block(TX, TY, 1);
+    const int ntiles = ntx * ((a.g.ny + S::BY - 1) / S::BY);
+    const dim3 block(TX, S::TY, 1);
     const dim3 grid(ntiles < resident ? ntiles : resident, 1, 1);
-    stage2d_f32_rows<STAGE, IDX><<<grid, block, 0, st>>>(a.g, (const float*)a.Gin, (const float*)a.Gn,
-                                                          (float*)a.Gout, (const float*)a.u, (const float*)a.v,
-                                                          (const float*)a.sl, c, ntx, ntiles);
+    OneSrc src{a.g, (const float*)a.Gin, (const float*)a.Gn, (const float*)a.u, (const float*)a.v,
+               (const float*)a.sl, (float*)a.Gout, c, ntx, S::BY};
+    stage2d_f32_rows<STAGE, IDX, TYV><<<grid, block, 0, st>>>(src, ntiles);
     return cudaGetLastError();
 }
 
-}  // namespace
+template <int STAGE, int TYV>
+cudaError_t launch2_group(const Group2* d, const int* owner, int ntiles, cudaStream_t st) {
+    using S = Shape<TYV>;
+    static const int resident = resident_ctas((const void*)stage2d_f32_group<STAGE, TYV>, S::NT);
+    const dim3 block(TX, S::TY, 1);
+    const dim3 grid(ntiles < resident ? ntiles : resident, 1, 1);
+    stage2d_f32_group<STAGE, TYV><<<grid, block, 0, st>>>(d, owner, ntiles);
+    return cudaGetLastError();
+}
 
-cudaError_t launch_stage2d_f32_tiled(const StageArgs& a, cudaStream_t st) {
+Coef2 make_coef2(const StageArgs& a) {
     Coef2 c;
     // face values carry a factor 6 (see face())
     c.inv_dx = (float)(1.0 / (6.0 * a.dx));
@@ -233,11 +336,68 @@ cudaError_t launch_stage2d_f32_tiled(const StageArgs& a, cudaStream_t st) {
     c.s_l = (float)a.s_l;
     c.eps = (float)a.eps;
     c.dt = (float)a.dt;
+    return c;
+}
+
+}  // namespace
+
+// Tile shape of a tile choice: 16 -> 32 x 16 tiles, anything else 32 x 32.
+cudaError_t launch_stage2d_f32_tiled(const StageArgs& a, cudaStream_t st) {
+    const Coef2 c = make_coef2(a);
     const bool small = a.g.cells() < (1LL << 31) - 1;
+    const bool t16 = a.tile == 16;
     cudaError_t e;
-    if (a.stage == 1) e = small ? launch2<1, int>(a, c, st) : launch2<1, long long>(a, c, st);
-    else if (a.stage == 2) e = small ? launch2<2, int>(a, c, st) : launch2<2, long long>(a, c, st);
-    else e = small ? launch2<3, int>(a, c, st) : launch2<3, long long>(a, c, st);
+#define LSGB_L2(ST) (small ? (t16 ? launch2<ST, int, 4>(a, c, st) : launch2<ST, int, 8>(a, c, st)) \
+                           : (t16 ? launch2<ST, long long, 4>(a, c, st) : launch2<ST, long long, 8>(a, c, st)))
+    if (a.stage == 1) e = LSGB_L2(1);
+    else if (a.stage == 2) e = LSGB_L2(2);
+    else e = LSGB_L2(3);
+#undef LSGB_L2
+    count_launches(1);
+    return e;
+}
+
+size_t group2_desc_bytes() { return sizeof(Group2); }
+
+void group2_fill(const GroupInst* in, int n, int shape, void* out, std::vector<int>& owner) {
+    Group2* d = (Group2*)out;
+    const int by = shape == 16 ? Shape<4>::BY : Shape<8>::BY;
+    long long tiles = 0;
+    for (int q = 0; q < n; ++q) {
+        Group2 e;
+        memset(&e, 0, sizeof(e));
+        const StageArgs& a = in[q].a;
+        e.g = a.g;
+        e.G = in[q].G;
+        e.A = in[q].A;
+        e.B = in[q].B;
+        e.u = (const float*)a.u;
+        e.v = (const float*)a.v;
+        e.sl = (const float*)a.sl;
+        e.c = make_coef2(a);
+        e.ntx = (a.g.nx + TX - 1) / TX;
+        e.tile0 = (int)tiles;
+        const long long nt = (long long)e.ntx * ((a.g.ny + by - 1) / by);
+        tiles += nt;
+        owner.insert(owner.end(), (size_t)nt, q);
+        d[q] = e;
+    }
+}
+
+cudaError_t launch_stage2d_f32_group(const void* table, const int* owner, int n, long long tiles, int stage,
+                                     int shape, cudaStream_t st) {
+    if (n <= 0 || tiles <= 0) return cudaSuccess;
+    if (tiles > 0x7fffffffLL) return cudaErrorInvalidValue;
+    const Group2* d = (const Group2*)table;
+    const int nt = (int)tiles;
+    cudaError_t e;
+    if (shape == 16) {
+        e = stage == 1 ? launch2_group<1, 4>(d, owner, nt, st)
+                       : (stage == 2 ? launch2_group<2, 4>(d, owner, nt, st) : launch2_group<3, 4>(d, owner, nt, st));
+    } else {
+        e = stage == 1 ? launch2_group<1, 8>(d, owner, nt, st)
+                       : (stage == 2 ? launch2_group<2, 8>(d, owner, nt, st) : launch2_group<3, 8>(d, owner, nt, st));
+    }
     count_launches(1);
     return e;
 }

@@ -90,6 +90,19 @@ struct Coef {
     float tf;  // deformation vortex time factor cos(pi t / T) (DEFO kernels)
 };
 
+// One instance of a grouped launch (stage3d_f32_group): its fields, stage
+// coefficients, tile grid (gx x gy column tiles, z-chunks of c.zc planes)
+// and its first block in the launch.
+struct Group3 {
+    CUtensorMap m[NFIELD];  // u, v, w, G^n (= G), S_L; bulk-tensor staging where tma != 0
+    Geo g;
+    float *G, *A, *B;
+    const float *u, *v, *w, *sl;
+    int* err;
+    Coef c;
+    int gx, gy, blk0, tma;
+};
+
 // ---- TMA / mbarrier primitives (PTX) ----------------------------------------
 
 __device__ __forceinline__ void mbar_init(uint64_t* b, uint32_t count) {
@@ -202,22 +215,36 @@ __device__ __forceinline__ void zcol_step(ZCol& z, float zn0, float zn1, float2&
 // from the factor tables defo at time factor c.tf -- a per-row factor of the
 // thread's two rows times a per-plane factor -- instead of read from u, v, w
 // (the same FP32 products as launch_deformation_f32 writes).
+// Static shared memory of one CTA (the staging ring of the point-wise fields
+// is the dynamic part).
+template <typename IDX>
+struct StageSmem {
+    float2 P2[2][BPH][PW];
+    float2 FL[BNFX], FR[BNFX];  // x faces [BY][TX+1]
+    IDX zoff[MAXZC + 10];
+    uint64_t mbar[NSTAGE];
+};
+
+// The CTA's work: the column tile (bx, by) of z-chunk bz.  tmaps: the five
+// fields' tensor maps (TMA form only).
 template <int STAGE, bool TMA, typename IDX, bool DEFO>
-__global__ void __launch_bounds__(NT, 2)
-stage3d_f32_col2(Geo g, const float* __restrict__ Gin, const float* __restrict__ Gn, float* __restrict__ Gout,
-                 const float* __restrict__ u, const float* __restrict__ v, const float* __restrict__ w,
-                 const float* __restrict__ sl, Coef c, const __grid_constant__ TmaMaps tm, int* __restrict__ err,
-                 int hsl /* sl != nullptr */, const float* __restrict__ defo) {
-    __shared__ float2 P2[2][BPH][PW];
-    __shared__ float2 FL[BNFX], FR[BNFX];  // x faces [BY][TX+1]
-    __shared__ IDX zoff[MAXZC + 10];
-    __shared__ __align__(8) uint64_t mbar[NSTAGE];
+__device__ __forceinline__ void
+stage3d_body(const Geo& g, const float* __restrict__ Gin, const float* __restrict__ Gn, float* __restrict__ Gout,
+             const float* __restrict__ u, const float* __restrict__ v, const float* __restrict__ w,
+             const float* __restrict__ sl, const Coef& c, const CUtensorMap* tmaps, int* __restrict__ err,
+             int hsl /* sl != nullptr */, const float* __restrict__ defo, int bx, int by, int bz,
+             StageSmem<IDX>& sm, bool global_maps = false) {
+    auto& P2 = sm.P2;
+    float2* FL = sm.FL;
+    float2* FR = sm.FR;
+    IDX* zoff = sm.zoff;
+    uint64_t* mbar = sm.mbar;
     extern __shared__ __align__(128) float stg[];  // NSTAGE x NFIELD x BFTILE
 
     const int tx = threadIdx.x, ty = threadIdx.y;
     const int t = ty * TX + tx;
-    const int i0 = blockIdx.x * TX, j0 = blockIdx.y * BY;
-    const int z0 = blockIdx.z * c.zc;
+    const int i0 = bx * TX, j0 = by * BY;
+    const int z0 = bz * c.zc;
     const int z1 = min(z0 + c.zc, g.nz);
     const int niter = (z1 - z0 + 1) / 2;
     const IDX sz = (IDX)g.nx * g.ny;
@@ -272,12 +299,12 @@ stage3d_f32_col2(Geo g, const float* __restrict__ Gin, const float* __restrict__
         const uint32_t nf = (DEFO ? 0 : 3) + (STAGE > 1 ? 1 : 0) + (has_sl ? 1 : 0);
         mbar_expect_tx(&mbar[s], nf * BFTILE * 4);
         if (!DEFO) {
-            tma_load_3d(base + 0 * BFTILE, &tm.m[0], i0, j0, kz, &mbar[s]);
-            tma_load_3d(base + 1 * BFTILE, &tm.m[1], i0, j0, kz, &mbar[s]);
-            tma_load_3d(base + 2 * BFTILE, &tm.m[2], i0, j0, kz, &mbar[s]);
+            tma_load_3d(base + 0 * BFTILE, tmaps + 0, i0, j0, kz, &mbar[s]);
+            tma_load_3d(base + 1 * BFTILE, tmaps + 1, i0, j0, kz, &mbar[s]);
+            tma_load_3d(base + 2 * BFTILE, tmaps + 2, i0, j0, kz, &mbar[s]);
         }
-        if (STAGE > 1) tma_load_3d(base + 3 * BFTILE, &tm.m[3], i0, j0, kz, &mbar[s]);
-        if (has_sl) tma_load_3d(base + 4 * BFTILE, &tm.m[4], i0, j0, kz, &mbar[s]);
+        if (STAGE > 1) tma_load_3d(base + 3 * BFTILE, tmaps + 3, i0, j0, kz, &mbar[s]);
+        if (has_sl) tma_load_3d(base + 4 * BFTILE, tmaps + 4, i0, j0, kz, &mbar[s]);
     };
     // plain form: this thread's cells of rows ra, ra + 1, planes k, k + 1
     auto fetch = [&](int it, int s) {
@@ -301,6 +328,11 @@ stage3d_f32_col2(Geo g, const float* __restrict__ Gin, const float* __restrict__
     if (TMA && t == 0) {
         for (int s = 0; s < NSTAGE; ++s) mbar_init(&mbar[s], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        // tensor maps that a copy wrote into global memory: make them visible
+        // to the bulk-copy unit before the first copy reads them
+        if (global_maps)
+            for (int f = 0; f < NFIELD; ++f)
+                asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(tmaps + f) : "memory");
     }
     __syncthreads();  // zoff table and barriers ready
     if (TMA && t == 0 && !c.drop)
@@ -469,6 +501,46 @@ stage3d_f32_col2(Geo g, const float* __restrict__ Gin, const float* __restrict__
     }
 }
 
+template <int STAGE, bool TMA, typename IDX, bool DEFO>
+__global__ void __launch_bounds__(NT, 2)
+stage3d_f32_col2(Geo g, const float* __restrict__ Gin, const float* __restrict__ Gn, float* __restrict__ Gout,
+                 const float* __restrict__ u, const float* __restrict__ v, const float* __restrict__ w,
+                 const float* __restrict__ sl, Coef c, const __grid_constant__ TmaMaps tm, int* __restrict__ err,
+                 int hsl /* sl != nullptr */, const float* __restrict__ defo) {
+    __shared__ StageSmem<IDX> sm;
+    stage3d_body<STAGE, TMA, IDX, DEFO>(g, Gin, Gn, Gout, u, v, w, sl, c, tm.m, err, hsl, defo, blockIdx.x,
+                                        blockIdx.y, blockIdx.z, sm);
+}
+
+// Grouped form: one launch advances one RK3 stage of every 3D instance of a
+// batch.  Block b belongs to instance owner[b], whose blocks start at its
+// blk0; within it, blocks run over (x tile, y tile, z chunk) as the
+// single-instance grid does.  Fixed buffer roles: stage 1 reads G and
+// writes A, stage 2 A -> B, stage 3 B -> G (G^n = G throughout).  Staging per
+// instance: bulk tensor copies from the descriptor's tensor maps where the
+// row pitch allows (nx % 4 == 0), per-thread cp.async copies otherwise;
+// 32-bit offsets.
+template <int STAGE>
+__global__ void __launch_bounds__(NT, 2) stage3d_f32_group(const Group3* __restrict__ ins,
+                                                            const int* __restrict__ owner) {
+    const Group3* d = ins + owner[blockIdx.x];
+    int l = (int)blockIdx.x - d->blk0;
+    const int bx = l % d->gx;
+    l /= d->gx;
+    const int by = l % d->gy;
+    const int bz = l / d->gy;
+    const float* Gin = STAGE == 1 ? d->G : (STAGE == 2 ? d->A : d->B);
+    float* Gout = STAGE == 1 ? d->A : (STAGE == 2 ? d->B : d->G);
+    const Coef c = d->c;
+    __shared__ StageSmem<int> sm;
+    if (d->tma)
+        stage3d_body<STAGE, true, int, false>(d->g, Gin, d->G, Gout, d->u, d->v, d->w, d->sl, c, d->m, d->err,
+                                              d->sl != nullptr, nullptr, bx, by, bz, sm, true);
+    else
+        stage3d_body<STAGE, false, int, false>(d->g, Gin, d->G, Gout, d->u, d->v, d->w, d->sl, c, nullptr, d->err,
+                                               d->sl != nullptr, nullptr, bx, by, bz, sm);
+}
+
 // cuTensorMapEncodeTiled through the runtime's driver entry point (no -lcuda).
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
     static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
@@ -542,7 +614,9 @@ bool stage3d_f32_fuses_deformation(const Geo& g) {
     return g.dim == 3 && (g.nx % 4) == 0 && g.cells() < (1LL << 31) - 1;
 }
 
-cudaError_t launch_stage3d_f32_tiled(const StageArgs& a, int* err, cudaStream_t st) {
+namespace {
+
+Coef make_coef(const StageArgs& a) {
     Coef c;
     // face values carry a factor 6 (see face())
     c.inv_dx = (float)(1.0 / (6.0 * a.dx));
@@ -557,6 +631,79 @@ cudaError_t launch_stage3d_f32_tiled(const StageArgs& a, int* err, cudaStream_t 
     c.zc = (a.tile == 16 || a.tile == 32 || a.tile == MAXZC) ? a.tile : default_zc(a.g);
     c.drop = a.drop_copies;
     c.tf = a.tf;
+    return c;
+}
+
+}  // namespace
+
+size_t group3_desc_bytes() { return sizeof(Group3); }
+
+void group3_fill(const GroupInst* in, int n, void* out, std::vector<int>& owner) {
+    Group3* d = (Group3*)out;
+    long long blk = 0;
+    for (int q = 0; q < n; ++q) {
+        Group3 e;
+        std::memset(&e, 0, sizeof(e));
+        const StageArgs& a = in[q].a;
+        e.g = a.g;
+        e.G = in[q].G;
+        e.A = in[q].A;
+        e.B = in[q].B;
+        e.u = (const float*)a.u;
+        e.v = (const float*)a.v;
+        e.w = (const float*)a.w;
+        e.sl = (const float*)a.sl;
+        e.err = a.err;
+        e.c = make_coef(a);
+        e.c.drop = 0;
+        // bulk-tensor staging needs a 16-byte row pitch and an error flag for
+        // its bounded waits
+        bool tma = a.err != nullptr && (a.g.nx % 4) == 0;
+        const float* fields[NFIELD] = {e.u, e.v, e.w, e.G, e.sl};
+        for (int f = 0; f < NFIELD && tma; ++f)
+            if (fields[f] && !encode_field(&e.m[f], fields[f], a.g, BY, 2)) tma = false;
+        e.tma = tma ? 1 : 0;
+        e.gx = (a.g.nx + TX - 1) / TX;
+        e.gy = (a.g.ny + BY - 1) / BY;
+        e.blk0 = (int)blk;
+        const long long nb = (long long)e.gx * e.gy * ((a.g.nz + e.c.zc - 1) / e.c.zc);
+        blk += nb;
+        owner.insert(owner.end(), (size_t)nb, q);
+        d[q] = e;
+    }
+}
+
+// Planes a CTA of this instance marches (its z-chunk, or the whole grid when
+// shorter): the block-length key the batch orders its 3D instances by.
+int stage3d_chunk_planes(const StageArgs& a) {
+    const int zc = (a.tile == 16 || a.tile == 32 || a.tile == MAXZC) ? a.tile : default_zc(a.g);
+    return a.g.nz < zc ? a.g.nz : zc;
+}
+
+cudaError_t launch_stage3d_f32_group(const void* desc, const int* owner, int n, long long blocks, int stage,
+                                     cudaStream_t st) {
+    if (n <= 0 || blocks <= 0) return cudaSuccess;
+    if (blocks > 0x7fffffffLL) return cudaErrorInvalidValue;
+    const size_t dyn = (size_t)NSTAGE * NFIELD * BFTILE * sizeof(float);
+    auto set = [dyn](const void* k) { return cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn); };
+    static const cudaError_t attr = [&] {
+        cudaError_t e = set((const void*)stage3d_f32_group<1>);
+        if (e == cudaSuccess) e = set((const void*)stage3d_f32_group<2>);
+        if (e == cudaSuccess) e = set((const void*)stage3d_f32_group<3>);
+        return e;
+    }();
+    if (attr != cudaSuccess) return attr;
+    const dim3 block(TX, TY, 1), grid((unsigned)blocks, 1, 1);
+    const Group3* d = (const Group3*)desc;
+    if (stage == 1) stage3d_f32_group<1><<<grid, block, dyn, st>>>(d, owner);
+    else if (stage == 2) stage3d_f32_group<2><<<grid, block, dyn, st>>>(d, owner);
+    else stage3d_f32_group<3><<<grid, block, dyn, st>>>(d, owner);
+    count_launches(1);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_stage3d_f32_tiled(const StageArgs& a, int* err, cudaStream_t st) {
+    Coef c = make_coef(a);
     TmaMaps tm;
     std::memset(&tm, 0, sizeof(tm));
     // bulk tensor copies need 16-byte row pitch and an error flag to report into

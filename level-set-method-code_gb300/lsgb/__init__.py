@@ -433,6 +433,17 @@ class Batch:
         _check(lib().lsgb_batch_stats(self._h, C.byref(a), C.byref(b)))
         return a.value, b.value
 
+    def set_mode(self, mode: str):
+        """"grouped" (one launch per stage for all instances of a
+        dimensionality; FP32) or "lanes" (per-instance launches on streams)."""
+        _check(lib().lsgb_batch_set_mode(self._h, {"grouped": 0, "lanes": 1}[mode]))
+
+    @property
+    def mode(self) -> str:
+        m = C.c_int()
+        _check(lib().lsgb_batch_get_mode(self._h, C.byref(m)))
+        return "grouped" if m.value == 0 else "lanes"
+
     def stream_handle(self) -> int:
         p = C.c_void_p()
         _check(lib().lsgb_batch_stream(self._h, C.byref(p)))
