@@ -254,11 +254,13 @@ LSGB_API int lsgb_solver_enable_timing(lsgb_solver* s, int enable);
 LSGB_API int lsgb_solver_kernel_times(lsgb_solver* s, double* stage_ms, int64_t* stage_launches,
                                       double* reinit_ms, int64_t* reinit_launches);
 
-/* Tile shape of the FP32 stage kernels.  3D: the z-chunk length (16, 32,
- * 64); 0 = default (the chunk length that fills the GPU's SMs best for the
- * grid).  2D: the tile height (32: 32 x 32 tiles, the default; 16: 32 x 16).
- * Every shape gives bit-identical results; only the speed differs.  The FP64
- * kernels have one shape: 0 only. */
+/* Tile shape of the stage kernels; 0 = default.  FP32 3D: the z-chunk
+ * length (16, 32, 64; default: the chunk length that fills the GPU's SMs
+ * best for the grid).  FP32 2D: the tile height (32: 32 x 32 tiles, the
+ * default; 16: 32 x 16).  FP64: 1 = one thread per cell, 2 = face-shared
+ * tiles (each WENO face value computed once for the cells on both sides;
+ * default where the grid gives every SM two tiles).  Every shape gives
+ * bit-identical results; only the speed differs. */
 LSGB_API int lsgb_solver_set_tile(lsgb_solver* s, int tile);
 LSGB_API int lsgb_solver_get_tile(const lsgb_solver* s, int* tile);
 

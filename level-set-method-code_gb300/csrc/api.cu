@@ -991,10 +991,11 @@ namespace {
 
 // Tile shapes the FP32 kernels accept: the z-chunk length of the 3D tiles.
 // The 2D FP32 kernel (32 x 32 tiles) and the FP64 kernels have one shape.
-// Tile choices of the FP32 stage kernels: the 3D z-chunk (16, 32, 64 planes)
-// and the 2D tile height (32: 32 x 32 tiles, 16: 32 x 16).
+// Tile choices of the stage kernels: FP32 3D z-chunk (16, 32, 64 planes),
+// FP32 2D tile height (32: 32 x 32 tiles, 16: 32 x 16), FP64 kernel form
+// (1: one thread per cell, 2: face-shared tiles).
 int tile_candidates(const lsgb_solver* s, int* c) {
-    if (s->prec != LSGB_PREC_F32) return 0;
+    if (s->prec != LSGB_PREC_F32) { c[0] = 1; c[1] = 2; return 2; }
     if (s->p.dim == 2) { c[0] = 32; c[1] = 16; return 2; }
     c[0] = 16; c[1] = 32; c[2] = 64; return 3;
 }

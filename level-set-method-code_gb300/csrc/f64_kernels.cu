@@ -169,6 +169,259 @@ __global__ void __launch_bounds__(256) stage_f64_kernel(StageArgs a) {
     ((double*)a.Gout)[a.lay.off + id] = out;
 }
 
+// ---- face-shared FP64 stage ------------------------------------------------
+//
+// The same stage, computing each WENO face value once.  Cell i's right face
+// and cell i+1's left face are the same reconstruction of the same five
+// values when both cells are upwinded the same way, so the value is shared;
+// a face between cells of opposite upwind directions needs both biases.  A
+// CTA owns a tile of cells (3D 32 x 8 x 2, 2D 32 x 16; block 32 x 8, two
+// cells per thread) and works in four phases over the tile staged with its
+// 3-cell halo in shared memory:
+//   1. u_eff of every cell (the reference's operations), its upwind bias per
+//      axis into shared memory;
+//   2. the list of (face, bias) reconstructions the tile's cells use, one
+//      entry per needed value, compacted by a block scan;
+//   3. the list evaluated densely, one entry per thread at a time (about 3.5
+//      reconstructions per cell in place of 6, each with 9 IEEE divisions);
+//   4. per cell, (face right - face left) / h per axis, the rhs and the stage
+//      combination, as stage_f64_kernel.
+// Every face value is the reference's weno5_left / weno5_right of the same
+// five samples (weno_either), so the fields are bit-identical to
+// stage_f64_kernel's.
+
+// weno5_left(v) (right = false) or weno5_right(v) (right = true) in one code
+// path: weno5_right evaluates the indicators on the mirrored stencil m with
+// the linear weights (0.3, 0.6, 0.1), and its candidate polynomials group
+// their terms differently; each polynomial's two operand orders are picked
+// per bias, so every rounding is the reference's.
+__device__ __forceinline__ double weno_either(double v0, double v1, double v2, double v3, double v4, bool right) {
+    const double m0 = right ? v4 : v0, m1 = right ? v3 : v1, m2 = v2, m3 = right ? v1 : v3, m4 = right ? v0 : v4;
+    const double b0 = sm_beta(m0, m1, m2);
+    const double b1 = sm_beta(m1, m2, m3);
+    const double b2 = sm_beta(m2, m3, m4);
+    const double d0 = right ? 0.3 : 0.1, d2 = right ? 0.1 : 0.3;
+    const double a0 = d0 / ((WENO_EPS + b0) * (WENO_EPS + b0));
+    const double a1 = 0.6 / ((WENO_EPS + b1) * (WENO_EPS + b1));
+    const double a2 = d2 / ((WENO_EPS + b2) * (WENO_EPS + b2));
+    const double s = a0 + a1 + a2;
+    const double w0 = a0 / s, w1 = a1 / s, w2 = a2 / s;
+    // left (2 v0 - 7 v1) + 11 v2; right (11 v2 - 7 v3) + 2 v4
+    const double t0 = 2.0 * m0, t2 = 11.0 * m2;
+    const double p0 = ((right ? t2 : t0) - 7.0 * m1 + (right ? t0 : t2)) / 6.0;
+    // left (-v1 + 5 v2) + 2 v3; right (2 v1 + 5 v2) - v3
+    const double n1 = -m1, u3 = 2.0 * m3;
+    const double p1 = ((right ? u3 : n1) + 5.0 * m2 + (right ? n1 : u3)) / 6.0;
+    // left (2 v2 + 5 v3) - v4; right (-v0 + 5 v1) + 2 v2
+    const double u2 = 2.0 * m2, n4 = -m4;
+    const double p2 = ((right ? n4 : u2) + 5.0 * m3 + (right ? u2 : n4)) / 6.0;
+    return w0 * p0 + w1 * p1 + w2 * p2;
+}
+
+template <int DIM>
+struct FaceTile {
+    static constexpr int TX = 32, TY = DIM == 3 ? 8 : 16, TZ = DIM == 3 ? 2 : 1;
+    static constexpr int NT = 256, CPT = TX * TY * TZ / NT;  // threads, cells per thread
+    static constexpr int SX = TX + 6, SY = TY + 6, SZ = DIM == 3 ? TZ + 6 : 1;
+    static constexpr int NFX = (TX + 1) * TY * TZ, NFY = TX * (TY + 1) * TZ;
+    static constexpr int NFZ = DIM == 3 ? TX * TY * (TZ + 1) : 0;
+    static constexpr int NF = NFX + NFY + NFZ;
+    static constexpr int NCELL = TX * TY * TZ;
+    // dynamic shared memory: staged G, face values [NF][2], task list, biases, scan
+    static constexpr size_t OFF_FV = sizeof(double) * SX * SY * SZ;
+    static constexpr size_t OFF_TASK = OFF_FV + sizeof(double) * 2 * NF;
+    static constexpr size_t OFF_BIAS = OFF_TASK + sizeof(int) * 2 * NF;
+    static constexpr size_t OFF_SCAN = OFF_BIAS + NCELL;
+    static constexpr size_t BYTES = OFF_SCAN + sizeof(int) * (NT + 1);
+};
+
+// Tile-local face f: its axis and the tile coordinates of the cell on its
+// low side (which may be -1 on the axis).
+template <int DIM>
+__device__ __forceinline__ void face_of(int f, int& ax, int& cx, int& cy, int& cz) {
+    using T = FaceTile<DIM>;
+    if (f < T::NFX) {
+        ax = 0;
+        cx = f % (T::TX + 1) - 1;
+        const int r = f / (T::TX + 1);
+        cy = r % T::TY;
+        cz = r / T::TY;
+    } else if (f < T::NFX + T::NFY) {
+        const int q = f - T::NFX;
+        ax = 1;
+        cx = q % T::TX;
+        const int r = q / T::TX;
+        cy = r % (T::TY + 1) - 1;
+        cz = r / (T::TY + 1);
+    } else {
+        const int q = f - T::NFX - T::NFY;
+        ax = 2;
+        cx = q % T::TX;
+        const int r = q / T::TX;
+        cy = r % T::TY;
+        cz = r / T::TY - 1;
+    }
+}
+
+// Face ids on the low and high side of cell (cx, cy, cz) along axis ax.
+template <int DIM>
+__device__ __forceinline__ int face_id(int ax, int cx, int cy, int cz, int hi) {
+    using T = FaceTile<DIM>;
+    if (ax == 0) return (cz * T::TY + cy) * (T::TX + 1) + cx + hi;
+    if (ax == 1) return T::NFX + (cz * (T::TY + 1) + cy + hi) * T::TX + cx;
+    return T::NFX + T::NFY + ((cz + hi) * T::TY + cy) * T::TX + cx;
+}
+
+template <int DIM, int STAGE, bool GH>
+__global__ void __launch_bounds__(256) stage_f64_faces(StageArgs a) {
+    using T = FaceTile<DIM>;
+    extern __shared__ __align__(16) unsigned char fsm[];
+    double* Gs = (double*)fsm;                    // [SZ][SY][SX], tile origin at (3, 3, 3)
+    double* fv = (double*)(fsm + T::OFF_FV);      // [NF][2]: bias 0 = left-biased, 1 = right-biased
+    int* task = (int*)(fsm + T::OFF_TASK);
+    unsigned char* bias = fsm + T::OFF_BIAS;      // per cell: bit ax set = u_eff(ax) < 0 (right-biased)
+    int* scan = (int*)(fsm + T::OFF_SCAN);
+    const Geo g = a.g;
+    const int t = threadIdx.y * 32 + threadIdx.x;
+    const int i0 = blockIdx.x * T::TX, j0 = blockIdx.y * T::TY, k0 = DIM == 3 ? blockIdx.z * T::TZ : 0;
+    const double* __restrict__ G = (const double*)a.Gin + a.lay.off;
+    const long long sy = a.lay.sy, sz = a.lay.sz;
+
+    // ---- stage the tile and its halo.  Coordinates within 3 of the grid come
+    // from the ghost cells (ghosted layout) or wrap / clamp (compact); positions
+    // further out belong only to cells past the grid edge and are clamped.
+    auto coord = [](int x, int n, int bc) {
+        if (GH) return x < -NG ? -NG : (x > n + NG - 1 ? n + NG - 1 : x);
+        if (x < -NG || x > n + NG - 1) return x < 0 ? 0 : n - 1;
+        return map_axis(x, n, bc);
+    };
+    for (int e = t; e < T::SX * T::SY * T::SZ; e += T::NT) {
+        const int lx = e % T::SX, ly = (e / T::SX) % T::SY, lz = e / (T::SX * T::SY);
+        const int x = coord(i0 + lx - 3, g.nx, g.bcx), y = coord(j0 + ly - 3, g.ny, g.bcy);
+        const int z = DIM == 3 ? coord(k0 + lz - 3, g.nz, g.bcz) : 0;
+        Gs[e] = G[(long long)z * sz + (long long)y * sy + x];
+    }
+    __syncthreads();
+
+    // ---- 1. u_eff and the upwind bias of the own cells (stage_f64_kernel's operations)
+    double ue[T::CPT], ve[T::CPT], we[T::CPT];
+#pragma unroll
+    for (int q = 0; q < T::CPT; ++q) {
+        const int c = t + q * T::NT;
+        const int cx = c % T::TX, cy = (c / T::TX) % T::TY, cz = c / (T::TX * T::TY);
+        const int i = i0 + cx, j = j0 + cy, k = k0 + cz;
+        ue[q] = ve[q] = we[q] = 0.0;
+        unsigned char b = 0;
+        if (i < g.nx && j < g.ny && k < g.nz) {
+            const double* P = Gs + ((cz + (DIM == 3 ? 3 : 0)) * T::SY + cy + 3) * T::SX + cx + 3;
+            const long long id = (long long)k * sz + (long long)j * sy + i;
+            const double s_l = a.sl ? ((const double*)a.sl)[a.lay.off + id] : a.s_l;
+            double gx = 0.0, gy = 0.0, gz = 0.0, gm = 1.0;
+            if (s_l > a.eps) {
+                gx = (P[1] - P[-1]) / (2.0 * a.dx);
+                gy = (P[T::SX] - P[-T::SX]) / (2.0 * a.dy);
+                if (DIM == 3) {
+                    gz = (P[T::SX * T::SY] - P[-T::SX * T::SY]) / (2.0 * a.dz);
+                    gm = sqrt(gx * gx + gy * gy + gz * gz + a.eps);
+                } else {
+                    gm = sqrt(gx * gx + gy * gy + a.eps);
+                }
+            }
+            ue[q] = ((const double*)a.u)[a.lay.off + id] - s_l * gx / gm;
+            ve[q] = ((const double*)a.v)[a.lay.off + id] - s_l * gy / gm;
+            if (DIM == 3) we[q] = ((const double*)a.w)[a.lay.off + id] - s_l * gz / gm;
+            b = (ue[q] >= 0.0 ? 0 : 1) | (ve[q] >= 0.0 ? 0 : 2) | (DIM == 3 && !(we[q] >= 0.0) ? 4 : 0);
+        }
+        bias[c] = b;
+    }
+    __syncthreads();
+
+    // ---- 2. the needed (face, bias) values: a face serves the tile cells on
+    // either side that lie in the grid, each with its own bias
+    auto in_grid = [&](int cx, int cy, int cz) {
+        return cx >= 0 && cx < T::TX && cy >= 0 && cy < T::TY && cz >= 0 && cz < T::TZ && i0 + cx < g.nx &&
+               j0 + cy < g.ny && k0 + cz < g.nz;
+    };
+    auto needs = [&](int f) {
+        int ax, cx, cy, cz;
+        face_of<DIM>(f, ax, cx, cy, cz);
+        const int dx = ax == 0, dy = ax == 1, dz = ax == 2;
+        int m = 0;
+        if (in_grid(cx, cy, cz)) m |= 1 << ((bias[(cz * T::TY + cy) * T::TX + cx] >> ax) & 1);
+        if (in_grid(cx + dx, cy + dy, cz + dz))
+            m |= 1 << ((bias[((cz + dz) * T::TY + cy + dy) * T::TX + cx + dx] >> ax) & 1);
+        return m;  // bit 0: left-biased value, bit 1: right-biased value
+    };
+    int cnt = 0;
+    for (int f = t; f < T::NF; f += T::NT) cnt += __popc(needs(f));
+    scan[t] = cnt;
+    __syncthreads();
+    for (int o = 1; o < T::NT; o <<= 1) {  // inclusive scan of the counts
+        const int add = t >= o ? scan[t - o] : 0;
+        __syncthreads();
+        scan[t] += add;
+        __syncthreads();
+    }
+    int pos = scan[t] - cnt;
+    const int ntask = scan[T::NT - 1];
+    for (int f = t; f < T::NF; f += T::NT) {
+        const int m = needs(f);
+        if (m & 1) task[pos++] = 2 * f;
+        if (m & 2) task[pos++] = 2 * f + 1;
+    }
+    __syncthreads();
+
+    // ---- 3. the values: face f between tile cells c and c + e_ax; the
+    // left-biased value reads G[c-2 .. c+2], the right-biased G[c-1 .. c+3]
+    for (int q = t; q < ntask; q += T::NT) {
+        const int f = task[q] >> 1;
+        const bool right = task[q] & 1;
+        int ax, cx, cy, cz;
+        face_of<DIM>(f, ax, cx, cy, cz);
+        const int st = ax == 0 ? 1 : (ax == 1 ? T::SX : T::SX * T::SY);
+        const double* P = Gs + ((cz + (DIM == 3 ? 3 : 0)) * T::SY + cy + 3) * T::SX + cx + 3 + (right ? st : 0);
+        fv[2 * f + (right ? 1 : 0)] = weno_either(P[-2 * st], P[-st], P[0], P[st], P[2 * st], right);
+    }
+    __syncthreads();
+
+    // ---- 4. derivatives, rhs, stage combination
+    const double dt = a.dt;
+#pragma unroll
+    for (int q = 0; q < T::CPT; ++q) {
+        const int c = t + q * T::NT;
+        const int cx = c % T::TX, cy = (c / T::TX) % T::TY, cz = c / (T::TX * T::TY);
+        const int i = i0 + cx, j = j0 + cy, k = k0 + cz;
+        if (!(i < g.nx && j < g.ny && k < g.nz)) continue;
+        const int b = bias[c];
+        auto deriv = [&](int ax, double h) {
+            const int r = (b >> ax) & 1;
+            return (fv[2 * face_id<DIM>(ax, cx, cy, cz, 1) + r] - fv[2 * face_id<DIM>(ax, cx, cy, cz, 0) + r]) / h;
+        };
+        double rhs;
+        if (DIM == 3) {
+            const double dgx = deriv(0, a.dx), dgy = deriv(1, a.dy), dgz = deriv(2, a.dz);
+            rhs = -(ue[q] * dgx + ve[q] * dgy + we[q] * dgz);
+        } else {
+            const double dgx = deriv(0, a.dx), dgy = deriv(1, a.dy);
+            rhs = -(ue[q] * dgx + ve[q] * dgy);
+        }
+        const long long id = (long long)k * sz + (long long)j * sy + i;
+        const double gc = Gs[((cz + (DIM == 3 ? 3 : 0)) * T::SY + cy + 3) * T::SX + cx + 3];
+        double out;
+        if (STAGE == 1) {
+            out = gc + dt * rhs;
+        } else if (STAGE == 2) {
+            const double gn = ((const double*)a.Gn)[a.lay.off + id];
+            out = 0.75 * gn + 0.25 * gc + 0.25 * dt * rhs;
+        } else {
+            const double gn = ((const double*)a.Gn)[a.lay.off + id];
+            const double a0 = 1.0 / 3.0, a2 = 2.0 / 3.0, b3 = 2.0 / 3.0;
+            out = a0 * gn + a2 * gc + b3 * dt * rhs;
+        }
+        ((double*)a.Gout)[a.lay.off + id] = out;
+    }
+}
+
 // Godunov first-order |grad phi|^2 term of one axis by sign(S),
 // weno5_gradient_magnitude_3d (weno5.h:202-248).
 __device__ __forceinline__ double godunov_axis(double dm, double dp, bool pos) {
@@ -367,9 +620,53 @@ inline unsigned flat_blocks(long long n) {
 
 }  // namespace
 
+namespace {
+
+template <int DIM, int STAGE, bool GH>
+cudaError_t launch_faces(const StageArgs& a, cudaStream_t st) {
+    using T = FaceTile<DIM>;
+    auto kern = stage_f64_faces<DIM, STAGE, GH>;
+    static const cudaError_t attr =
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)T::BYTES);
+    if (attr != cudaSuccess) return attr;
+    const dim3 grid((a.g.nx + T::TX - 1) / T::TX, (a.g.ny + T::TY - 1) / T::TY,
+                    DIM == 3 ? (a.g.nz + T::TZ - 1) / T::TZ : 1);
+    kern<<<grid, dim3(32, 8, 1), T::BYTES, st>>>(a);
+    return cudaGetLastError();
+}
+
+// Face-shared tiles (tile 2), or one thread per cell (tile 1); by default the
+// tiles where they give every SM at least two CTAs, the per-cell kernel on
+// grids too small for that (its lower blocks spread them over every SM).
+bool use_faces(const StageArgs& a) {
+    if (a.tile == 1) return false;
+    if (a.tile == 2) return true;
+    static const int sms = [] {
+        int dev = 0, n = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        return n > 0 ? n : 1;
+    }();
+    const long long tiles = a.g.dim == 3 ? (long long)((a.g.nx + 31) / 32) * ((a.g.ny + 7) / 8) * ((a.g.nz + 1) / 2)
+                                         : (long long)((a.g.nx + 31) / 32) * ((a.g.ny + 15) / 16);
+    return tiles >= 2LL * sms;
+}
+
+}  // namespace
+
 cudaError_t launch_stage_f64(const StageArgs& a, cudaStream_t st) {
-    dim3 b = cell_block(a.g), gr = cell_grid(a.g, b);
     const bool gh = a.lay.ghosted != 0;
+    if (use_faces(a)) {
+        cudaError_t e;
+#define LSGB_FACES(D, GHV) (a.stage == 1 ? launch_faces<D, 1, GHV>(a, st) \
+                                         : (a.stage == 2 ? launch_faces<D, 2, GHV>(a, st) : launch_faces<D, 3, GHV>(a, st)))
+        if (a.g.dim == 3) e = gh ? LSGB_FACES(3, true) : LSGB_FACES(3, false);
+        else e = gh ? LSGB_FACES(2, true) : LSGB_FACES(2, false);
+#undef LSGB_FACES
+        count_launches(1);
+        return e;
+    }
+    dim3 b = cell_block(a.g), gr = cell_grid(a.g, b);
 #define LSGB_STAGE(D, S, GHV) stage_f64_kernel<D, S, GHV><<<gr, b, 0, st>>>(a)
     if (a.g.dim == 3) {
         if (gh) {

@@ -62,8 +62,9 @@ def dropin_reinit(lsgb, p, G):
     return host(res), host(phi0), host(rt), host(flag)
 
 
-def solver_run(lsgb, p, n, G, u, v, w=None, sl=None, precision="f64"):
+def solver_run(lsgb, p, n, G, u, v, w=None, sl=None, precision="f64", tile=0):
     with lsgb.Solver(p, precision) as s:
+        s.set_tile(tile)
         s.set_fields(G, u, v, w)
         if sl is not None:
             s.set_sl_field(sl)
@@ -290,6 +291,37 @@ def test_against_port(cuda, lsgb_mod, port, dim, periodic, s_l, nx, ny, nz):
     assert cnt == int((interior < 0).sum())
     out, _ = solver_run(lsgb_mod, p, 5, G, vel[0], vel[1], w, sl=sl)
     assert np.array_equal(out, port.run(pb, 5, G, *vel, sl=sl))
+
+
+@pytest.mark.parametrize("dim,periodic,s_l,nx,ny,nz", CASES)
+@pytest.mark.parametrize("tile", [1, 2])
+def test_fp64_kernel_forms_match_port(cuda, lsgb_mod, port, dim, periodic, s_l, nx, ny, nz, tile):
+    """Both FP64 stage kernels -- one thread per cell (tile 1) and the
+    face-shared tiles (tile 2, each face value computed once) -- on ragged
+    grids, uniform and per-cell S_L, periodic and zero-gradient Y."""
+    pb = Problem(nx=nx, ny=ny, nz=nz, dim=dim, s_l=s_l, dt=1.3e-3, enable_reinit=True,
+                 reinit_interval=2, reinit_iterations=3, periodic_y=periodic)
+    p = lsgb_params(lsgb_mod, pb)
+    G, vel, sl = seeded(pb, nx * 1000 + ny * 10 + nz + 7)
+    w = vel[2] if dim == 3 else None
+    out, _ = solver_run(lsgb_mod, p, 5, G, vel[0], vel[1], w, tile=tile)
+    assert np.array_equal(out, port.run(pb, 5, G, *vel))
+    out, _ = solver_run(lsgb_mod, p, 4, G, vel[0], vel[1], w, sl=sl, tile=tile)
+    assert np.array_equal(out, port.run(pb, 4, G, *vel, sl=sl))
+
+
+@pytest.mark.parametrize("dim,periodic,n", [(3, True, (97, 45, 41)), (2, True, (650, 261, 1)),
+                                            (2, False, (650, 261, 1))])
+def test_dropin_face_shared_tiles_match_port(cuda, lsgb_mod, port, dim, periodic, n):
+    """The drop-in step on ghosted arrays at sizes where the face-shared FP64
+    kernel is the default (every SM gets two tiles), ragged tiles at the edges."""
+    pb = Problem(nx=n[0], ny=n[1], nz=n[2], dim=dim, s_l=0.15, dt=1e-3, periodic_y=periodic)
+    p = lsgb_params(lsgb_mod, pb)
+    G, vel, sl = seeded(pb, 91)
+    G, vel = port.apply_bc(pb, G), [port.apply_bc(pb, a) for a in vel]
+    w = vel[2] if dim == 3 else None
+    assert np.array_equal(dropin_step(lsgb_mod, p, G, vel[0], vel[1], w), port.rk3_step(pb, G, *vel))
+    assert np.array_equal(dropin_step(lsgb_mod, p, G, vel[0], vel[1], w, sl=sl), port.rk3_step(pb, G, *vel, sl=sl))
 
 
 def test_reductions_match_port(cuda, lsgb_mod, port):
