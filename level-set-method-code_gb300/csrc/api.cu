@@ -390,10 +390,12 @@ size_t nbytes(const lsgb_solver* s) { return s->esz * (size_t)s->g.cells(); }
 // waits set when a wait gives up; cleared when reported.
 int* err_flag(lsgb_solver* s) { return (int*)(s->scratch + 2 * (RED_BLOCKS + 1) + 2); }
 
-// Flag values: 1 = a wait gave up and the block's issued copies then landed
-// (the handle recovers once the flag is reported and cleared); 2 = even the
-// bounded drain of those copies gave up, so a copy may still write into
-// shared memory that a later block owns: the handle is marked unusable.
+// Flag values: 2 = a wait gave up while the block's bulk copies were in
+// flight; the kernel drains them with bounded waits, but a copy that missed
+// its limit may still write into shared memory that a later block owns, so
+// the handle is marked unusable.  1 = a wait gave up with no copy in flight
+// (the drop-copies test hook): the handle recovers once the flag is reported
+// and cleared.
 int flag_result(lsgb_solver* s, int flag) {
     if (!flag) return LSGB_OK;
     cudaMemsetAsync(err_flag(s), 0, sizeof(int), s->st);
