@@ -215,6 +215,19 @@ __device__ __forceinline__ void zcol_step(ZCol& z, float zn0, float zn1, float2&
 // from the factor tables defo at time factor c.tf -- a per-row factor of the
 // thread's two rows times a per-plane factor -- instead of read from u, v, w
 // (the same FP32 products as launch_deformation_f32 writes).
+// Static shared memory of one CTA (the staging ring of the point-wise fields
+// is the dynamic part).  The grouped kernel, which runs either staging form,
+// holds it once in this struct; the single-instance kernel declares the same
+// arrays separately (passing the struct's members there cost 3 % at 512^3,
+// measured A/B).
+template <typename IDX>
+struct StageSmem {
+    float2 P2[2][BPH][PW];
+    float2 FL[BNFX], FR[BNFX];  // x faces [BY][TX+1]
+    IDX zoff[MAXZC + 10];
+    uint64_t mbar[NSTAGE];
+};
+
 // The CTA's work: the column tile (bx, by) of z-chunk bz.  tmaps: the five
 // fields' tensor maps (TMA form only).
 template <int STAGE, bool TMA, typename IDX, bool DEFO>
@@ -223,11 +236,7 @@ stage3d_body(const Geo& g, const float* __restrict__ Gin, const float* __restric
              const float* __restrict__ u, const float* __restrict__ v, const float* __restrict__ w,
              const float* __restrict__ sl, const Coef& c, const CUtensorMap* tmaps, int* __restrict__ err,
              int hsl /* sl != nullptr */, const float* __restrict__ defo, int bx, int by, int bz,
-             bool global_maps = false) {
-    __shared__ float2 P2[2][BPH][PW];
-    __shared__ float2 FL[BNFX], FR[BNFX];  // x faces [BY][TX+1]
-    __shared__ IDX zoff[MAXZC + 10];
-    __shared__ __align__(8) uint64_t mbar[NSTAGE];
+             float2 (*P2)[BPH][PW], float2* FL, float2* FR, IDX* zoff, uint64_t* mbar, bool global_maps = false) {
     extern __shared__ __align__(128) float stg[];  // NSTAGE x NFIELD x BFTILE
 
     const int tx = threadIdx.x, ty = threadIdx.y;
@@ -498,8 +507,12 @@ stage3d_f32_col2(Geo g, const float* __restrict__ Gin, const float* __restrict__
                  const float* __restrict__ u, const float* __restrict__ v, const float* __restrict__ w,
                  const float* __restrict__ sl, Coef c, const __grid_constant__ TmaMaps tm, int* __restrict__ err,
                  int hsl /* sl != nullptr */, const float* __restrict__ defo) {
+    __shared__ float2 P2[2][BPH][PW];
+    __shared__ float2 FL[BNFX], FR[BNFX];
+    __shared__ IDX zoff[MAXZC + 10];
+    __shared__ __align__(8) uint64_t mbar[NSTAGE];
     stage3d_body<STAGE, TMA, IDX, DEFO>(g, Gin, Gn, Gout, u, v, w, sl, c, tm.m, err, hsl, defo, blockIdx.x,
-                                        blockIdx.y, blockIdx.z);
+                                        blockIdx.y, blockIdx.z, P2, FL, FR, zoff, mbar);
 }
 
 // Grouped form: one launch advances one RK3 stage of every 3D instance of a
@@ -522,14 +535,13 @@ __global__ void __launch_bounds__(NT, 2) stage3d_f32_group(const Group3* __restr
     const float* Gin = STAGE == 1 ? d->G : (STAGE == 2 ? d->A : d->B);
     float* Gout = STAGE == 1 ? d->A : (STAGE == 2 ? d->B : d->G);
     const Coef c = d->c;
-    // (each staging form brings its own static shared arrays: 2 x 22 KB, with
-    // the 60 KB staging ring still two CTAs per SM)
+    __shared__ StageSmem<int> sm;
     if (d->tma)
         stage3d_body<STAGE, true, int, false>(d->g, Gin, d->G, Gout, d->u, d->v, d->w, d->sl, c, d->m, d->err,
-                                              d->sl != nullptr, nullptr, bx, by, bz, true);
+                                              d->sl != nullptr, nullptr, bx, by, bz, sm.P2, sm.FL, sm.FR, sm.zoff, sm.mbar, true);
     else
         stage3d_body<STAGE, false, int, false>(d->g, Gin, d->G, Gout, d->u, d->v, d->w, d->sl, c, nullptr, d->err,
-                                               d->sl != nullptr, nullptr, bx, by, bz);
+                                               d->sl != nullptr, nullptr, bx, by, bz, sm.P2, sm.FL, sm.FR, sm.zoff, sm.mbar);
 }
 
 // cuTensorMapEncodeTiled through the runtime's driver entry point (no -lcuda).
