@@ -134,8 +134,7 @@ def fd_check(prob: Problem, sl, n_steps: int, n_dirs: int, rel_step=1e-3, seed: 
     steps = [rel_step] if np.isscalar(rel_step) else list(rel_step)
     rows = []
     for q in range(n_dirs):
-        d = fourier_field(sl.shape[::-1], seed * 1000 + q)
-        d /= np.linalg.norm(d)
+        d = direction(sl.shape[::-1], q, seed)
         ad = float(np.sum(g * d))
         for rs in steps:
             h = rs * float(np.linalg.norm(sl))
@@ -145,6 +144,31 @@ def fd_check(prob: Problem, sl, n_steps: int, n_dirs: int, rel_step=1e-3, seed: 
             rows.append({"dir": q, "rel_step": rs, "fd": fd, "adjoint": ad,
                          "rel_err": abs(fd - ad) / max(abs(fd), 1e-300)})
     return L, g, rows
+
+
+def direction(shape_xyz, q: int, seed: int = 7) -> np.ndarray:
+    """The q-th smooth random unit direction of the finite-difference checks
+    (an 8-mode Fourier field, ||d||_2 = 1 over the cells)."""
+    d = fourier_field(shape_xyz, seed * 1000 + q)
+    return d / np.linalg.norm(d)
+
+
+def directional(n: int = 192, steps: int = 300, dirs: int = 32, checkpoint: int = 20, seed: int = 7) -> dict:
+    """<dL/dS_L, d_q> of the FP64 adjoint on the adjoint workload for the
+    directions d_0 .. d_{dirs-1}, with the loss.  The discrete adjoint holds
+    the forward's switching decisions fixed at the base run (the upwind
+    branches, the Godunov choices, the crossing flags and the stability
+    mask), so these are derivatives of the forward map with those decisions
+    frozen."""
+    p, G0, u, v, w, sl, sl_t = workload(n, steps)
+    prob = Problem(p, G0, u, v, w, "f64", checkpoint)
+    prob.a.set_grads(sl=True, velocity=False)
+    prob.target(sl_t, steps)
+    L, g = prob.gradient(sl, steps)
+    prob.close()
+    ad = [float(np.sum(g * direction(sl.shape[::-1], q, seed))) for q in range(dirs)]
+    return {"n": n, "steps": steps, "checkpoint": checkpoint, "dt": p.dt, "seed": seed, "loss_f64": L,
+            "adjoint": ad, "grad_l2": float(np.linalg.norm(g))}
 
 
 # -- torch ------------------------------------------------------------------
@@ -272,9 +296,18 @@ def main():
     ap.add_argument("--no-reinit", action="store_true", help="drop HCR-2 (its crossing flags and stability "
                     "mask make the forward map discontinuous)")
     ap.add_argument("--json", default=None)
+    ap.add_argument("--directional", action="store_true",
+                    help="only the FP64 adjoint's directional derivatives and the loss")
     a = ap.parse_args()
     import __graft_entry__
     __graft_entry__.build_library()
+    if a.directional:
+        r = directional(a.n, a.steps, a.dirs, a.checkpoint)
+        if a.json:
+            with open(a.json, "w") as f:
+                json.dump(r, f, indent=2)
+        print(json.dumps(r))
+        return
     r = report(a.n, a.steps, a.dirs, a.checkpoint, a.rel_step if len(a.rel_step) > 1 else a.rel_step[0],
                reinit=not a.no_reinit)
     if a.json:

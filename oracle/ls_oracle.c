@@ -58,6 +58,50 @@ static grid_t grid2(const orc_params* p) {
 }
 
 /* ---------------------------------------------------------------------------
+ * Decision tape (3D; an addition for checking the discrete adjoint, not in
+ * the reference).  The forward map has switching decisions: the upwind
+ * branch u_eff >= 0 per axis (weno5.h:99), the Godunov one-sided choice per
+ * axis of the pseudo-step (weno5.h:202-248), the crossing flags of
+ * computeInterfaceCrossings3D (reinitialization.h:46-89) and the stability
+ * test (:95-130).  Mode 1 records them per interior cell while computing as
+ * usual (same bits); mode 2 replays recorded ones in place of the tests, so a
+ * perturbed run follows the base run's branches and is a smooth function of
+ * its inputs: the map whose derivative the discrete adjoint computes.
+ *   stage  [calls of rhs3][cells]: bit a = axis a right-biased (u_eff < 0)
+ *   pseudo [pseudo-steps][cells]:  bits 2a..2a+1 = axis a choice (0 none, 1
+ *          the backward difference, 2 the forward one), bit 6 = stable
+ *   flags  [reinitialisations][cells]: the crossing flags
+ * ------------------------------------------------------------------------- */
+static struct {
+    int mode;                 /* 0 off, 1 record, 2 replay */
+    unsigned char *stage, *pseudo, *flags;
+    long n_stage, n_pseudo, n_flags;  /* capacities in calls */
+    long c_stage, c_pseudo, c_flags;  /* calls so far */
+    int overflow;
+} tape;
+
+void orc_tape_set(int mode, unsigned char* stage, long n_stage, unsigned char* pseudo, long n_pseudo,
+                  unsigned char* flags, long n_flags) {
+    tape.mode = mode;
+    tape.stage = stage; tape.pseudo = pseudo; tape.flags = flags;
+    tape.n_stage = n_stage; tape.n_pseudo = n_pseudo; tape.n_flags = n_flags;
+    tape.c_stage = tape.c_pseudo = tape.c_flags = 0;
+    tape.overflow = 0;
+}
+
+/* calls used so far (stage, pseudo-step, reinitialisation) and the overflow flag */
+void orc_tape_counts(long* out) {
+    out[0] = tape.c_stage; out[1] = tape.c_pseudo; out[2] = tape.c_flags; out[3] = tape.overflow;
+}
+
+/* The tape row of the next call of a kind (NULL when off or full). */
+static unsigned char* tape_row(unsigned char* base, long* used, long cap, long cells) {
+    if (tape.mode == 0) return NULL;
+    if (*used >= cap) { tape.overflow = 1; return NULL; }
+    return base + (*used)++ * cells;
+}
+
+/* ---------------------------------------------------------------------------
  * WENO-5 reconstruction, weno5.h:28-81 (3D) == weno5.h:39-122 (2D).
  * beta uses the reference's non-standard second term 1/4 (v[k+2]-v[k])^2 for
  * all three sub-stencils, and weights d_k / (eps + beta_k)^2.
@@ -104,9 +148,9 @@ static inline double weno_right(const double v[5]) {
 /* Upwind WENO-5 derivative along one axis, weno5.h:90-122 (x), :127 (y),
  * :164 (z): c points at the cell, s is the stride along the axis.
  * Branch on vel >= 0 (not > 0), weno5.h:99. */
-static inline double weno_deriv(const double* c, long s, double vel, double h) {
+static inline double weno_deriv_b(const double* c, long s, int left, double h) {
     double v[5] = {c[-2 * s], c[-s], c[0], c[s], c[2 * s]};
-    if (vel >= 0.0) {
+    if (left) {
         double vl[5] = {c[-3 * s], c[-2 * s], c[-s], c[0], c[s]};
         double gl = weno_left(vl);
         double gr = weno_left(v);
@@ -119,6 +163,10 @@ static inline double weno_deriv(const double* c, long s, double vel, double h) {
     }
 }
 
+static inline double weno_deriv(const double* c, long s, double vel, double h) {
+    return weno_deriv_b(c, s, vel >= 0.0, h);
+}
+
 /* ---------------------------------------------------------------------------
  * Spatial operator: computeRHS3D (rk3.h:31-81), computeRHS (2D rk3.h:54-98).
  * rhs = -(u_eff * Dx + v_eff * Dy [+ w_eff * Dz]) on interior cells, with
@@ -128,6 +176,8 @@ static inline double weno_deriv(const double* c, long s, double vel, double h) {
 static void rhs3(const orc_params* p, const grid_t* g, const double* G, double* R,
                  const double* u, const double* v, const double* w, const double* sl) {
     int k;
+    unsigned char* trow = tape_row(tape.stage, &tape.c_stage, tape.n_stage, (long)g->nx * g->ny * g->nz);
+    const int tmode = trow ? tape.mode : 0;
 #pragma omp parallel for schedule(static)
     for (k = NG; k < g->nz + NG; k++) {
         for (int j = NG; j < g->ny + NG; j++) {
@@ -145,9 +195,15 @@ static void rhs3(const orc_params* p, const grid_t* g, const double* G, double* 
                 double ue = u[id] - s_l * gx / gm;
                 double ve = v[id] - s_l * gy / gm;
                 double we = w[id] - s_l * gz / gm;
-                double dgx = weno_deriv(c, 1, ue, p->dx);
-                double dgy = weno_deriv(c, g->sy, ve, p->dy);
-                double dgz = weno_deriv(c, g->sz, we, p->dz);
+                int lx = ue >= 0.0, ly = ve >= 0.0, lz = we >= 0.0;
+                if (tmode) {
+                    unsigned char* t = trow + ((long)(k - NG) * g->ny + (j - NG)) * g->nx + (i - NG);
+                    if (tmode == 1) *t = (unsigned char)(!lx | (!ly << 1) | (!lz << 2));
+                    else { lx = !(*t & 1); ly = !(*t & 2); lz = !(*t & 4); }
+                }
+                double dgx = weno_deriv_b(c, 1, lx, p->dx);
+                double dgy = weno_deriv_b(c, g->sy, ly, p->dy);
+                double dgz = weno_deriv_b(c, g->sz, lz, p->dz);
                 R[id] = -(ue * dgx + ve * dgy + we * dgz);
             }
         }
@@ -337,6 +393,9 @@ static void crossings(const grid_t* g, int dim, const double* phi0, double* rt, 
     int k0 = dim == 3 ? NG : 0;
     long st[6] = {-1, 1, -g->sy, g->sy, -g->sz, g->sz};
     int nnb = 2 * dim;
+    unsigned char* trow = dim == 3 ? tape_row(tape.flags, &tape.c_flags, tape.n_flags,
+                                              (long)g->nx * g->ny * g->nz) : NULL;
+    const int tmode = trow ? tape.mode : 0;
 #pragma omp parallel for schedule(static)
     for (k = k0; k < k0 + nz; k++) {
         for (int j = NG; j < g->ny + NG; j++) {
@@ -346,10 +405,13 @@ static void crossings(const grid_t* g, int dim, const double* phi0, double* rt, 
                 double sum = 0.0;
                 int cnt = 0, f = 0;
                 rt[id] = 0.0;
+                unsigned char* t = tmode ? trow + ((long)(k - NG) * g->ny + (j - NG)) * g->nx + (i - NG) : NULL;
                 for (int n = 0; n < nnb; n++) {
                     double pn = phi0[id + st[n]];
-                    if (pc * pn < 0.0) { sum += pn; cnt++; f |= 1 << n; }
+                    int cross = tmode == 2 ? (*t >> n) & 1 : pc * pn < 0.0;
+                    if (cross) { sum += pn; cnt++; f |= 1 << n; }
                 }
+                if (tmode == 1) *t = (unsigned char)f;
                 flag[id] = f;
                 if (cnt > 0 && fabs(sum) > 1e-15) rt[id] = pc / sum;
             }
@@ -378,6 +440,9 @@ static void reinit_step(const orc_params* p, const grid_t* g, int dim, const dou
     long st[6] = {-1, 1, -g->sy, g->sy, -g->sz, g->sz};
     int nnb = 2 * dim;
     double dtau = p->reinit_dtau;
+    unsigned char* trow = dim == 3 ? tape_row(tape.pseudo, &tape.c_pseudo, tape.n_pseudo,
+                                              (long)g->nx * g->ny * g->nz) : NULL;
+    const int tmode = trow ? tape.mode : 0;
 #pragma omp parallel for schedule(static)
     for (k = k0; k < k0 + nz; k++) {
         for (int j = NG; j < g->ny + NG; j++) {
@@ -388,10 +453,38 @@ static void reinit_step(const orc_params* p, const grid_t* g, int dim, const dou
                 double S = ph0 / sqrt(ph0 * ph0 + p->dx * p->dx);
                 const double* c = phin + id;
                 int pos = S > 0.0;
-                double gsq = godunov_axis((c[0] - c[-1]) / p->dx, (c[1] - c[0]) / p->dx, pos)
-                           + godunov_axis((c[0] - c[-g->sy]) / p->dy, (c[g->sy] - c[0]) / p->dy, pos);
-                if (dim == 3)
-                    gsq = gsq + godunov_axis((c[0] - c[-g->sz]) / p->dz, (c[g->sz] - c[0]) / p->dz, pos);
+                double gsq;
+                unsigned char* t = tmode ? trow + ((long)(k - NG) * g->ny + (j - NG)) * g->nx + (i - NG) : NULL;
+                if (tmode == 0) {
+                    gsq = godunov_axis((c[0] - c[-1]) / p->dx, (c[1] - c[0]) / p->dx, pos)
+                        + godunov_axis((c[0] - c[-g->sy]) / p->dy, (c[g->sy] - c[0]) / p->dy, pos);
+                    if (dim == 3)
+                        gsq = gsq + godunov_axis((c[0] - c[-g->sz]) / p->dz, (c[g->sz] - c[0]) / p->dz, pos);
+                } else {
+                    /* per axis: record which one-sided difference the Godunov
+                     * maximum took (none when the selected term is zero), or
+                     * use the recorded one; the sum is formed as above */
+                    const double hh[3] = {p->dx, p->dy, p->dz};
+                    const long ss[3] = {1, g->sy, g->sz};
+                    double term3[3];
+                    unsigned char code = tmode == 2 ? *t : 0;
+                    for (int ax = 0; ax < 3; ax++) {
+                        double dm = (c[0] - c[-ss[ax]]) / hh[ax], dp = (c[ss[ax]] - c[0]) / hh[ax];
+                        int sel;
+                        if (tmode == 1) {
+                            double a, b;
+                            if (pos) { a = fmax(dm, 0.0); b = fmin(dp, 0.0); }
+                            else { a = fmin(dm, 0.0); b = fmax(dp, 0.0); }
+                            sel = a * a >= b * b ? (a != 0.0 ? 1 : 0) : 2;
+                            code |= (unsigned char)(sel << (2 * ax));
+                        } else {
+                            sel = (code >> (2 * ax)) & 3;
+                        }
+                        term3[ax] = sel == 1 ? dm * dm : (sel == 2 ? dp * dp : 0.0);
+                    }
+                    gsq = term3[0] + term3[1] + term3[2];
+                    if (tmode == 1) *t = code;
+                }
                 double gm = sqrt(gsq);
                 double term = -S * (gm - 1.0);
                 double forcing = 0.0;
@@ -401,6 +494,8 @@ static void reinit_step(const orc_params* p, const grid_t* g, int dim, const dou
                     for (int n = 0; n < nnb && stable; n++)
                         if (f & (1 << n))
                             if ((phin[id + st[n]] > 0.0) != (phi0[id + st[n]] > 0.0)) stable = 0;
+                    if (tmode == 1) *t |= (unsigned char)(stable << 6);
+                    if (tmode == 2) stable = (*t >> 6) & 1;
                     if (stable) {
                         double sum = 0.0;
                         for (int n = 0; n < nnb; n++)

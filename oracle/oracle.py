@@ -273,6 +273,28 @@ class Oracle:
             raise MemoryError("oracle run: scratch allocation failed")
         return G
 
+    # -- decision tape (3D port only): see the tape section of ls_oracle.c ----
+    def tape(self, mode: str, stage=None, pseudo=None, flags=None):
+        """mode "off", "record" or "replay"; stage / pseudo / flags are uint8
+        arrays of shape (calls, nz * ny * nx) holding one row per rhs
+        evaluation, HCR-2 pseudo-step and reinitialisation."""
+        assert self.kind == "port"
+        m = {"off": 0, "record": 1, "replay": 2}[mode]
+        arrs = (stage, pseudo, flags)
+        for a in arrs:
+            assert a is None or (a.dtype == np.uint8 and a.flags.c_contiguous and a.ndim == 2)
+        ptr = lambda a: None if a is None else a.ctypes.data_as(C.POINTER(C.c_ubyte))
+        rows = lambda a: 0 if a is None else a.shape[0]
+        self._l3.orc_tape_set(m, ptr(stage), C.c_long(rows(stage)), ptr(pseudo), C.c_long(rows(pseudo)),
+                              ptr(flags), C.c_long(rows(flags)))
+        self._tape_refs = arrs
+
+    def tape_counts(self):
+        """(rhs rows, pseudo-step rows, reinit rows used, overflow)."""
+        out = (C.c_long * 4)()
+        self._l3.orc_tape_counts(out)
+        return tuple(int(x) for x in out)
+
     def volume(self, pb: Problem, G):
         """computeInterfaceVolume / computeInterfaceArea."""
         self._chk(pb, G)
