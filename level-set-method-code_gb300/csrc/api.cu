@@ -560,6 +560,24 @@ int reinit(lsgb_solver* s) {
     r.dz = s->p.dim == 3 ? s->p.dz : s->p.dx;
     r.dtau = s->p.reinit_dtau;
     r.beta = s->p.reinit_beta;
+    const int M = s->p.reinit_iterations;
+    if (s->prec == LSGB_PREC_F32 && M % 2 == 0) {
+        // Even pseudo-step counts end in G without a copy: the first step
+        // (phi = phi0 = G) writes A and keeps phi0 in B, so G is free; the
+        // others alternate A -> G, G -> A and read phi0 from B.  The values
+        // are those of the copy form below.
+        for (int it = 0; it < M; ++it) {
+            r.phin = it == 0 ? s->G : (it % 2 ? s->A : s->G);
+            r.phi0 = it == 0 ? s->G : s->B;
+            r.phinew = it % 2 ? s->G : s->A;
+            r.phi0_copy = it == 0 ? s->B : nullptr;
+            size_t ev = 0;
+            LSGB_TRY(timed_begin(s, 1, &ev));
+            LSGB_CUDA(launch_reinit_f32(r, s->st));
+            LSGB_TRY(timed_end(s, ev));
+        }
+        return LSGB_OK;
+    }
     void* cur = s->G;
     void* bufs[2] = {s->A, s->B};
     for (int it = 0; it < s->p.reinit_iterations; ++it) {

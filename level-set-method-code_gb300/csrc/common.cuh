@@ -100,6 +100,9 @@ struct ReinitArgs {
     const void* phi0;
     void* phinew;
     double dx, dy, dz, dtau, beta;
+    // FP32 only, nullable: the pseudo-step also stores phi0 here (a copy that
+    // lets a later pseudo-step write its result into phi0's buffer)
+    void* phi0_copy = nullptr;
 };
 
 // Drop-in (ghosted, FP64) reinit pieces with stored r~ and flags.

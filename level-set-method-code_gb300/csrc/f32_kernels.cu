@@ -106,11 +106,15 @@ constexpr int RT = 256;  // threads of a pseudo-step block
 // are rare and their FP64 update is long, so a block queues them in shared
 // memory and finishes them with dense lanes after the FP32 pass: a warp that
 // holds one forced cell no longer runs the FP64 sequence for all 32 lanes.
-template <int DIM, typename IDX>
+// SAME: phin and phi0 are one array (the first pseudo-step of a
+// reinitialisation), so each neighbour is loaded once.  phi0_copy (nullable)
+// receives phi0 at every cell.
+template <int DIM, typename IDX, bool SAME = false>
 __device__ __forceinline__ void reinit_f32_body(const Geo& g, const float* __restrict__ phin,
                                                 const float* __restrict__ phi0, float* __restrict__ phinew,
                                                 float inv_dx, float inv_dy, float inv_dz, float dx2, float dtau_f,
-                                                double dx, double dtau, double beta, int bx, int by, int bz) {
+                                                double dx, double dtau, double beta, int bx, int by, int bz,
+                                                float* __restrict__ phi0_copy = nullptr) {
     __shared__ int nq;
     __shared__ IDX q_id[RT];
     __shared__ int q_flag[RT];
@@ -135,14 +139,15 @@ __device__ __forceinline__ void reinit_f32_body(const Geo& g, const float* __res
             nb[4] = id + nb_off<IDX>(k, g.nz, g.bcz, sz, false);
             nb[5] = id + nb_off<IDX>(k, g.nz, g.bcz, sz, true);
         }
-        const float phi = __ldg(phin + id);
         const float ph0 = __ldg(phi0 + id);
+        const float phi = SAME ? ph0 : __ldg(phin + id);
         float pn[6], p0[6];
 #pragma unroll
         for (int q = 0; q < 2 * DIM; ++q) {
-            pn[q] = __ldg(phin + nb[q]);
             p0[q] = __ldg(phi0 + nb[q]);
+            pn[q] = SAME ? p0[q] : __ldg(phin + nb[q]);
         }
+        if (phi0_copy) phi0_copy[id] = ph0;
         int flag;
         bool forced;
         const float term = reinit_cell_f32<DIM>(phi, ph0, pn, p0, inv_dx, inv_dy, inv_dz, dx2, flag, forced);
@@ -174,15 +179,15 @@ __device__ __forceinline__ void reinit_f32_body(const Geo& g, const float* __res
     }
 }
 
-template <int DIM, typename IDX>
+template <int DIM, typename IDX, bool SAME>
 __global__ void __launch_bounds__(RT) reinit_f32_kernel(Geo g, const float* __restrict__ phin,
                                                         const float* __restrict__ phi0,
                                                         float* __restrict__ phinew, float inv_dx,
                                                         float inv_dy, float inv_dz, float dx2,
                                                         float dtau_f, double dx, double dtau,
-                                                        double beta) {
-    reinit_f32_body<DIM, IDX>(g, phin, phi0, phinew, inv_dx, inv_dy, inv_dz, dx2, dtau_f, dx, dtau, beta,
-                              blockIdx.x, blockIdx.y, blockIdx.z);
+                                                        double beta, float* __restrict__ phi0_copy) {
+    reinit_f32_body<DIM, IDX, SAME>(g, phin, phi0, phinew, inv_dx, inv_dy, inv_dz, dx2, dtau_f, dx, dtau, beta,
+                                    blockIdx.x, blockIdx.y, blockIdx.z, phi0_copy);
 }
 
 // One instance of the grouped HCR-2 and copy-back launches: buffers, the
@@ -200,7 +205,7 @@ constexpr int CPB = 4096;  // floats per block of the copy back
 
 // Grouped HCR-2 pseudo-step `iter` of every instance (same dimensionality);
 // block b belongs to instance owner[b].
-template <int DIM>
+template <int DIM, bool FIRST>
 __global__ void __launch_bounds__(RT) reinit_f32_group(const GroupR* __restrict__ ins, const int* __restrict__ owner,
                                                        int iter) {
     const GroupR* d = ins + owner[blockIdx.x];
@@ -209,10 +214,11 @@ __global__ void __launch_bounds__(RT) reinit_f32_group(const GroupR* __restrict_
     l /= d->gx;
     const int by = l % d->gy;
     const int bz = l / d->gy;
-    const float* in = iter == 0 ? d->G : ((iter - 1) & 1 ? d->B : d->A);
+    // iteration 0 (FIRST) reads G as both fields
     float* out = iter & 1 ? d->B : d->A;
-    reinit_f32_body<DIM, int>(d->g, in, d->G, out, d->inv_dx, d->inv_dy, d->inv_dz, d->dx2, d->dtau_f, d->dx,
-                              d->dtau, d->beta, bx, by, bz);
+    const float* in = FIRST ? d->G : ((iter - 1) & 1 ? d->B : d->A);
+    reinit_f32_body<DIM, int, FIRST>(d->g, in, d->G, out, d->inv_dx, d->inv_dy, d->inv_dz, d->dx2, d->dtau_f,
+                                     d->dx, d->dtau, d->beta, bx, by, bz);
 }
 
 // G <- the buffer the last of `iters` pseudo-steps wrote, every instance.
@@ -248,12 +254,16 @@ cudaError_t launch_reinit_f32(const ReinitArgs& a, cudaStream_t st) {
     const float ix = (float)(1.0 / a.dx), iy = (float)(1.0 / a.dy), iz = (float)(1.0 / a.dz);
     const float dx2 = (float)(a.dx * a.dx);
     const bool small = a.g.cells() < (1LL << 31) - 1;  // 32-bit element offsets
-#define LSGB_R32(D, I) reinit_f32_kernel<D, I><<<gr, b, 0, st>>>(a.g, pn, p0, out, ix, iy, iz, dx2, (float)a.dtau, \
-                                                                  a.dx, a.dtau, a.beta)
+    const bool same = pn == p0;
+    float* cp = (float*)a.phi0_copy;
+#define LSGB_R32(D, I, SM) reinit_f32_kernel<D, I, SM><<<gr, b, 0, st>>>(a.g, pn, p0, out, ix, iy, iz, dx2, \
+                                                                          (float)a.dtau, a.dx, a.dtau, a.beta, cp)
     if (a.g.dim == 3) {
-        if (small) LSGB_R32(3, int); else LSGB_R32(3, long long);
+        if (small) { if (same) LSGB_R32(3, int, true); else LSGB_R32(3, int, false); }
+        else { if (same) LSGB_R32(3, long long, true); else LSGB_R32(3, long long, false); }
     } else {
-        if (small) LSGB_R32(2, int); else LSGB_R32(2, long long);
+        if (small) { if (same) LSGB_R32(2, int, true); else LSGB_R32(2, int, false); }
+        else { if (same) LSGB_R32(2, long long, true); else LSGB_R32(2, long long, false); }
     }
 #undef LSGB_R32
     count_launches(1);
@@ -302,8 +312,14 @@ cudaError_t launch_reinit_f32_group(const void* table, const int* owner, int n, 
     if (n <= 0 || blocks <= 0) return cudaSuccess;
     if (blocks > 0x7fffffffLL) return cudaErrorInvalidValue;
     const GroupR* d = (const GroupR*)table;
-    if (dim == 3) reinit_f32_group<3><<<(unsigned)blocks, dim3(32, 4, 2), 0, st>>>(d, owner, iter);
-    else reinit_f32_group<2><<<(unsigned)blocks, dim3(32, 8, 1), 0, st>>>(d, owner, iter);
+    const unsigned nb = (unsigned)blocks;
+    if (dim == 3) {
+        if (iter == 0) reinit_f32_group<3, true><<<nb, dim3(32, 4, 2), 0, st>>>(d, owner, iter);
+        else reinit_f32_group<3, false><<<nb, dim3(32, 4, 2), 0, st>>>(d, owner, iter);
+    } else {
+        if (iter == 0) reinit_f32_group<2, true><<<nb, dim3(32, 8, 1), 0, st>>>(d, owner, iter);
+        else reinit_f32_group<2, false><<<nb, dim3(32, 8, 1), 0, st>>>(d, owner, iter);
+    }
     count_launches(1);
     return cudaGetLastError();
 }
