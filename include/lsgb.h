@@ -329,7 +329,10 @@ LSGB_API int lsgb_batch_stream(lsgb_batch* b, void** stream);
  * (every RK3 stage input and every HCR-2 pseudo-step input) and runs the
  * vector-Jacobian products of the stage kernels and the pseudo-steps in
  * reverse.  Upwind branches, Godunov selections, crossing flags and the
- * stability mask are taken from the forward state.  Periodic boundaries only.
+ * stability mask are taken from the forward state.  Periodic and
+ * zero-gradient axes in any mix (on a zero-gradient axis the transpose of the
+ * clamped neighbour map adds the clamped stencil points back onto the edge
+ * cells).
  * Gradients are deterministic (no atomics) and independent of the checkpoint
  * interval.
  * ------------------------------------------------------------------------ */

@@ -19,8 +19,13 @@
 //                arrays), plus the point-wise parameter sensitivities;
 //   gather pass  one thread per cell m sums plane o at m - o over all o in a
 //                fixed order.
-// Boundaries are periodic on every axis (the wrapped neighbour map is a
-// bijection, so the gather is the exact transpose).
+// Boundaries: periodic axes wrap, zero-gradient axes clamp (map_axis, as in
+// the forward kernels).  The wrapped map is a bijection, so on periodic axes
+// the gather reads one source per offset.  The clamped map is not: cell m
+// receives plane o from c = m - o only when c lies inside the grid, and the
+// first / last cell of a clamped axis also receives plane o of every cell
+// whose stencil point c + o was clamped onto it (c + o < 0 or >= n).  The
+// gather kernels add those terms in their ZG form.
 #include "common.cuh"
 
 #include <type_traits>
@@ -42,6 +47,17 @@ __device__ __forceinline__ int wrap(int i, int n) { return i < 0 ? i + n : (i >=
 __device__ __forceinline__ int wrapn(int i, int n) {
     i %= n;
     return i < 0 ? i + n : i;
+}
+// z plane of an unwrapped slab index: wrapped (periodic) or clamped
+__device__ __forceinline__ int zmap(int k, int n, int bc) {
+    return bc == LSGB_BC_PERIODIC ? wrapn(k, n) : (k < 0 ? 0 : (k >= n ? n - 1 : k));
+}
+// cells of a clamped axis whose stencil point c + o lands on the edge cell e
+// (0 or n-1) only by clamping: c in [lo, hi]
+__device__ __forceinline__ void clamped_sources(int e, int o, int n, int& lo, int& hi) {
+    if (e == 0 && o < 0) { lo = 0; hi = min(-o - 1, n - 1); }
+    else if (e == n - 1 && o > 0) { lo = max(n - o, 0); hi = n - 1; }
+    else { lo = 1; hi = 0; }
 }
 
 // Reciprocal: IEEE in the FP64 adjoint; the approximate MUFU reciprocal in
@@ -139,19 +155,27 @@ __global__ void __launch_bounds__(256) stage_adj_coef_kernel(AdjStageArgs a) {
     const int kl = DIM == 3 ? blockIdx.z * blockDim.z + threadIdx.z : 0;  // slab-local plane
     if (i >= g.nx || j >= g.ny || kl >= (DIM == 3 ? a.zn + 6 : 1)) return;
     const int ku = DIM == 3 ? a.z0 - 3 + kl : 0;  // unwrapped plane
-    const int k = DIM == 3 ? wrapn(ku, g.nz) : 0;
+    const long long sy = g.nx, sz = (long long)g.nx * g.ny;
+    const long long P = DIM == 3 ? (long long)(a.zn + 6) * sz : g.cells();
+    T* cp = (T*)a.coef + (i + sy * j + sz * kl);  // plane 0 of this cell; plane o at cp + o P
+    if (DIM == 3 && g.bcz != LSGB_BC_PERIODIC && (ku < 0 || ku >= g.nz)) {
+        // a plane outside a clamped z axis: no cell, no coefficients
+#pragma unroll
+        for (int o = 0; o < ADJ_PLANES; ++o) cp[o * P] = (T)0;
+        return;
+    }
+    const int k = DIM == 3 ? zmap(ku, g.nz, g.bcz) : 0;
     const bool own = DIM == 2 || (ku >= a.z0 && ku < a.z0 + a.zn);  // parameter gradients
     typedef T R;
     const T* __restrict__ G = (const T*)a.Gin;
-    const long long sy = g.nx, sz = (long long)g.nx * g.ny;
     const long long c = i + sy * j + sz * k;
     const T* Gc = G + c;
     R s[3][7];
 #pragma unroll
     for (int d = -3; d <= 3; ++d) {
-        s[0][d + 3] = Gc[wrap(i + d, g.nx) - i];
-        s[1][d + 3] = Gc[(long long)(wrap(j + d, g.ny) - j) * sy];
-        if (DIM == 3) s[2][d + 3] = Gc[(long long)(wrap(k + d, g.nz) - k) * sz];
+        s[0][d + 3] = Gc[map_axis(i + d, g.nx, g.bcx) - i];
+        s[1][d + 3] = Gc[(long long)(map_axis(j + d, g.ny, g.bcy) - j) * sy];
+        if (DIM == 3) s[2][d + 3] = Gc[(long long)(map_axis(k + d, g.nz, g.bcz) - k) * sz];
     }
     const R S = a.sl ? ((const T*)a.sl)[c] : (R)a.s_l;
     const R ih[3] = {(R)(1.0 / a.dx), (R)(1.0 / a.dy), (R)(1.0 / a.dz)};
@@ -180,8 +204,6 @@ __global__ void __launch_bounds__(256) stage_adj_coef_kernel(AdjStageArgs a) {
 #pragma unroll
     for (int ax = 0; ax < DIM; ++ax) dg += D[ax] * gr[ax];
     const R wc = (R)(a.cdt) * ((const T*)a.lam)[c];
-    const long long P = DIM == 3 ? (long long)(a.zn + 6) * sz : g.cells();
-    T* cp = (T*)a.coef + (i + sy * j + sz * kl);  // plane 0 of this cell; plane o at cp + o P
     R centre = (R)0;
 #pragma unroll
     for (int ax = 0; ax < DIM; ++ax) {
@@ -286,7 +308,10 @@ __global__ void __launch_bounds__(256, 2) stage_adj_coef_pair_kernel(AdjStageArg
     if (i >= g.nx || j >= g.ny || kl >= nl) return;
     const bool two = kl + 1 < nl;  // an odd slab leaves the last thread one plane
     const int ku = a.z0 - 3 + kl;
-    const int k = wrapn(ku, g.nz), k1 = wrapn(ku + 1, g.nz);
+    const int k = zmap(ku, g.nz, g.bcz), k1 = zmap(ku + 1, g.nz, g.bcz);
+    // planes outside a clamped z axis hold no cell: their coefficients are 0
+    const bool zper = g.bcz == LSGB_BC_PERIODIC;
+    const bool in0 = zper || (ku >= 0 && ku < g.nz), in1 = zper || (ku + 1 >= 0 && ku + 1 < g.nz);
     const bool own0 = ku >= a.z0 && ku < a.z0 + a.zn;
     const bool own1 = two && ku + 1 >= a.z0 && ku + 1 < a.z0 + a.zn;
     const float* __restrict__ G = (const float*)a.Gin;
@@ -297,14 +322,14 @@ __global__ void __launch_bounds__(256, 2) stage_adj_coef_pair_kernel(AdjStageArg
     float2 s[3][7];
 #pragma unroll
     for (int d = -3; d <= 3; ++d) {
-        const int xo = wrap(i + d, g.nx) - i;
-        const long long yo = (long long)(wrap(j + d, g.ny) - j) * sy;
+        const int xo = map_axis(i + d, g.nx, g.bcx) - i;
+        const long long yo = (long long)(map_axis(j + d, g.ny, g.bcy) - j) * sy;
         s[0][d + 3] = make_float2(Gc[xo], G[c1 + xo]);
         s[1][d + 3] = make_float2(Gc[yo], G[c1 + yo]);
     }
     float zq[8];
 #pragma unroll
-    for (int d = 0; d < 8; ++d) zq[d] = G[i + sy * j + sz * wrapn(ku - 3 + d, g.nz)];
+    for (int d = 0; d < 8; ++d) zq[d] = G[i + sy * j + sz * zmap(ku - 3 + d, g.nz, g.bcz)];
 #pragma unroll
     for (int d = 0; d < 7; ++d) s[2][d] = make_float2(zq[d], zq[d + 1]);
     const float* sl = (const float*)a.sl;
@@ -332,7 +357,7 @@ __global__ void __launch_bounds__(256, 2) stage_adj_coef_pair_kernel(AdjStageArg
 #pragma unroll
     for (int ax = 0; ax < 3; ++ax) dg = fma2(D[ax], gr[ax], dg);
     const float* lam = (const float*)a.lam;
-    const float2 wc = f2((float)a.cdt) * make_float2(lam[c], lam[c1]);
+    const float2 wc = f2((float)a.cdt) * make_float2(in0 ? lam[c] : 0.0f, in1 ? lam[c1] : 0.0f);
     const long long P = (long long)nl * sz;  // plane stride of the slab buffer
     float* cp0 = (float*)a.coef + (i + sy * j + sz * kl);
     float* cp1 = cp0 + sz;
@@ -377,7 +402,9 @@ __global__ void __launch_bounds__(256, 2) stage_adj_coef_pair_kernel(AdjStageArg
 
 // out[m] = c_self lam[m] + addend[m] + sum_o plane_o[m - o];
 // acc[m] = (acc_init ? 0 : acc[m]) + c_n lam[m] when acc is given.
-template <typename T, int DIM>
+// ZG: some axis is zero-gradient (sources outside the grid skipped, clamped
+// sources added on the edge cells).
+template <typename T, int DIM, bool ZG>
 __global__ void __launch_bounds__(256) stage_adj_gather_kernel(AdjGatherArgs a) {
     const Geo g = a.g;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -392,21 +419,52 @@ __global__ void __launch_bounds__(256) stage_adj_gather_kernel(AdjGatherArgs a) 
     const T* __restrict__ cm = (const T*)a.coef + (i + sy * j + sz * kl);  // plane 0 at cell m
     const T lam = ((const T*)a.lam)[m];
     T sum = cm[0];
-#pragma unroll
-    for (int q = 0; q < 6; ++q) {
-        const int o = stage_off(q);
-        sum += cm[(1 + q) * P + (wrap(i - o, g.nx) - i)];
-    }
-#pragma unroll
-    for (int q = 0; q < 6; ++q) {
-        const int o = stage_off(q);
-        sum += cm[(7 + q) * P + (long long)(wrap(j - o, g.ny) - j) * sy];
-    }
-    if (DIM == 3) {
+    if (!ZG) {
 #pragma unroll
         for (int q = 0; q < 6; ++q) {
             const int o = stage_off(q);
-            sum += cm[(13 + q) * P - (long long)o * sz];  // source plane kl - o of the slab
+            sum += cm[(1 + q) * P + (wrap(i - o, g.nx) - i)];
+        }
+#pragma unroll
+        for (int q = 0; q < 6; ++q) {
+            const int o = stage_off(q);
+            sum += cm[(7 + q) * P + (long long)(wrap(j - o, g.ny) - j) * sy];
+        }
+        if (DIM == 3) {
+#pragma unroll
+            for (int q = 0; q < 6; ++q) {
+                const int o = stage_off(q);
+                sum += cm[(13 + q) * P - (long long)o * sz];  // source plane kl - o of the slab
+            }
+        }
+    } else {
+        const int at[3] = {i, j, k};
+        const int n[3] = {g.nx, g.ny, g.nz};
+        const int bc[3] = {g.bcx, g.bcy, g.bcz};
+        const long long str[3] = {1, sy, sz};
+#pragma unroll
+        for (int ax = 0; ax < DIM; ++ax) {
+            const bool per = bc[ax] == LSGB_BC_PERIODIC;
+#pragma unroll
+            for (int q = 0; q < 6; ++q) {
+                const int o = stage_off(q);
+                const long long pl = (long long)(1 + 6 * ax + q) * P;
+                // z: the slab buffer is indexed by unwrapped plane, and its planes
+                // outside a clamped axis hold zeros
+                int src = at[ax] - o;
+                if (per && ax < 2) src = wrap(src, n[ax]);
+                if (per || ax == 2 || (src >= 0 && src < n[ax])) sum += cm[pl + (long long)(src - at[ax]) * str[ax]];
+            }
+            if (!per && (at[ax] == 0 || at[ax] == n[ax] - 1)) {
+#pragma unroll
+                for (int q = 0; q < 6; ++q) {
+                    const int o = stage_off(q);
+                    const long long pl = (long long)(1 + 6 * ax + q) * P;
+                    int lo, hi;
+                    clamped_sources(at[ax], o, n[ax], lo, hi);
+                    for (int cc = lo; cc <= hi; ++cc) sum += cm[pl + (long long)(cc - at[ax]) * str[ax]];
+                }
+            }
         }
     }
     T out = (T)a.c_self * lam + sum;
@@ -448,7 +506,8 @@ __global__ void __launch_bounds__(256) reinit_adj_coef_kernel(AdjReinitArgs a) {
     for (int q = 0; q < 2 * DIM; ++q) {
         int ox, oy, oz;
         nb_off(q, ox, oy, oz);
-        nb[q] = ix.at(wrap(i + ox, g.nx), wrap(j + oy, g.ny), wrap(k + oz, g.nz));
+        nb[q] = ix.at(map_axis(i + ox, g.nx, g.bcx), map_axis(j + oy, g.ny, g.bcy),
+                      DIM == 3 ? map_axis(k + oz, g.nz, g.bcz) : 0);
     }
     const R phi = phin[c], ph0 = phi0[c];
     R pn[6], p0[6];
@@ -535,7 +594,9 @@ __global__ void __launch_bounds__(256) reinit_adj_coef_kernel(AdjReinitArgs a) {
 // mu_out[m] = sum_o plane_o[m - o]  (o over centre and the 2 DIM neighbours)
 // lam0[m]   = (first ? 0 : lam0[m]) + sum_o plane_{7+o}[m - o]
 // last:      mu_out[m] += lam0[m]   (phi^0 = phi0)
-template <typename T, int DIM>
+// ZG: on a clamped axis a source outside the grid is skipped, and the edge
+// cell also takes its own plane of the offset that points out of the grid.
+template <typename T, int DIM, bool ZG>
 __global__ void __launch_bounds__(256) reinit_adj_gather_kernel(AdjReinitGatherArgs a) {
     const Geo g = a.g;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -552,9 +613,26 @@ __global__ void __launch_bounds__(256) reinit_adj_gather_kernel(AdjReinitGatherA
         int ox, oy, oz;
         nb_off(q, ox, oy, oz);
         // plane q of cell c holds d F_c / d phi_{c + o}: cell m receives it from c = m - o
-        const long long c = ix.at(wrap(i - ox, g.nx), wrap(j - oy, g.ny), wrap(k - oz, g.nz));
-        s += coef[(long long)(1 + q) * P + c];
-        s0 += coef[(long long)(8 + q) * P + c];
+        if (!ZG) {
+            const long long c = ix.at(wrap(i - ox, g.nx), wrap(j - oy, g.ny), wrap(k - oz, g.nz));
+            s += coef[(long long)(1 + q) * P + c];
+            s0 += coef[(long long)(8 + q) * P + c];
+        } else {
+            const int ax = q >> 1, o = (q & 1) ? 1 : -1;
+            const int at = ax == 0 ? i : (ax == 1 ? j : k);
+            const int n = ax == 0 ? g.nx : (ax == 1 ? g.ny : g.nz);
+            const bool per = (ax == 0 ? g.bcx : (ax == 1 ? g.bcy : g.bcz)) == LSGB_BC_PERIODIC;
+            const int src = per ? wrap(at - o, n) : at - o;
+            if (per || (src >= 0 && src < n)) {
+                const long long c = ix.at(ax == 0 ? src : i, ax == 1 ? src : j, ax == 2 ? src : k);
+                s += coef[(long long)(1 + q) * P + c];
+                s0 += coef[(long long)(8 + q) * P + c];
+            }
+            if (!per && ((o < 0 && at == 0) || (o > 0 && at == n - 1))) {
+                s += coef[(long long)(1 + q) * P + m];
+                s0 += coef[(long long)(8 + q) * P + m];
+            }
+        }
     }
     T* lam0 = (T*)a.lam0;
     const T l0 = (a.first ? (T)0 : lam0[m]) + s0;
@@ -606,6 +684,10 @@ __global__ void __launch_bounds__(RED_THREADS) sum_partials_kernel(const double*
     if (threadIdx.x == 0) out[0] = red[0];
 }
 
+bool zero_gradient(const Geo& g) {
+    return g.bcx != LSGB_BC_PERIODIC || g.bcy != LSGB_BC_PERIODIC || (g.dim == 3 && g.bcz != LSGB_BC_PERIODIC);
+}
+
 dim3 cell_block(const Geo& g) { return g.dim == 3 ? dim3(32, 4, 2) : dim3(32, 8, 1); }
 dim3 cell_grid(const Geo& g, dim3 b) {
     return dim3((g.nx + b.x - 1) / b.x, (g.ny + b.y - 1) / b.y, g.dim == 3 ? (g.nz + b.z - 1) / b.z : 1);
@@ -627,10 +709,12 @@ cudaError_t launch_stage_adj(const AdjStageArgs& c, const AdjGatherArgs& gth, cu
             stage_adj_coef_kernel<T, 3><<<gc, b, 0, st>>>(c);
         }
         const dim3 gg(gr.x, gr.y, (unsigned)((gth.zn + b.z - 1) / b.z));
-        stage_adj_gather_kernel<T, 3><<<gg, b, 0, st>>>(gth);
+        if (zero_gradient(c.g)) stage_adj_gather_kernel<T, 3, true><<<gg, b, 0, st>>>(gth);
+        else stage_adj_gather_kernel<T, 3, false><<<gg, b, 0, st>>>(gth);
     } else {
         stage_adj_coef_kernel<T, 2><<<gr, b, 0, st>>>(c);
-        stage_adj_gather_kernel<T, 2><<<gr, b, 0, st>>>(gth);
+        if (zero_gradient(c.g)) stage_adj_gather_kernel<T, 2, true><<<gr, b, 0, st>>>(gth);
+        else stage_adj_gather_kernel<T, 2, false><<<gr, b, 0, st>>>(gth);
     }
     count_launches(2);
     return cudaGetLastError();
@@ -641,10 +725,12 @@ cudaError_t launch_reinit_adj(const AdjReinitArgs& c, const AdjReinitGatherArgs&
     const dim3 b = cell_block(c.g), gr = cell_grid(c.g, b);
     if (c.g.dim == 3) {
         reinit_adj_coef_kernel<T, 3><<<gr, b, 0, st>>>(c);
-        reinit_adj_gather_kernel<T, 3><<<gr, b, 0, st>>>(gth);
+        if (zero_gradient(c.g)) reinit_adj_gather_kernel<T, 3, true><<<gr, b, 0, st>>>(gth);
+        else reinit_adj_gather_kernel<T, 3, false><<<gr, b, 0, st>>>(gth);
     } else {
         reinit_adj_coef_kernel<T, 2><<<gr, b, 0, st>>>(c);
-        reinit_adj_gather_kernel<T, 2><<<gr, b, 0, st>>>(gth);
+        if (zero_gradient(c.g)) reinit_adj_gather_kernel<T, 2, true><<<gr, b, 0, st>>>(gth);
+        else reinit_adj_gather_kernel<T, 2, false><<<gr, b, 0, st>>>(gth);
     }
     count_launches(2);
     return cudaGetLastError();

@@ -1912,9 +1912,6 @@ extern "C" int lsgb_adjoint_create(lsgb_solver* s, int checkpoint_interval, lsgb
     LSGB_TRY(solver_ok(s));
     if (!out) return fail(LSGB_ERR_INVALID, "out is NULL");
     if (checkpoint_interval < 1) return fail(LSGB_ERR_INVALID, "checkpoint_interval must be >= 1");
-    if (s->g.bcx != LSGB_BC_PERIODIC || s->g.bcy != LSGB_BC_PERIODIC ||
-        (s->g.dim == 3 && s->g.bcz != LSGB_BC_PERIODIC))
-        return fail(LSGB_ERR_UNSUPPORTED, "the adjoint supports periodic boundaries on every axis");
     lsgb_adjoint* a = new lsgb_adjoint();
     a->s = s;
     a->ckpt = checkpoint_interval;

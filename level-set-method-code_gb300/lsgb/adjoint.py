@@ -64,9 +64,10 @@ def sl_field(n, seed: int) -> np.ndarray:
 
 
 def workload(n: int = 192, steps: int = 300, dim: int = 3, cfl: float = 0.5, reinit_interval: int = 10,
-             reinit_iterations: int = 2, reinit: bool = True):
+             reinit_iterations: int = 2, reinit: bool = True, bc=None):
     """(params, G0, u, v, w, sl, sl_target) of the adjoint workload; fields in
-    the compact layout, FP64 host arrays."""
+    the compact layout, FP64 host arrays.  bc: boundary per axis ("periodic"
+    or "zero_gradient", x first; default periodic everywhere)."""
     if dim == 3:
         wl = syn.sphere_config(CONFIG, n, 16, 0.15)
     else:
@@ -82,8 +83,10 @@ def workload(n: int = 192, steps: int = 300, dim: int = 3, cfl: float = 0.5, rei
     sl_t = sl_field(grid, syn.seed_for(CONFIG, 200))
     speed = np.abs(u) + np.abs(v) + (np.abs(w) if dim == 3 else 0.0)
     dt = cfl * (1.0 / n) / (float(speed.max()) + float(max(sl.max(), sl_t.max())))
+    bcs = {"bc_" + a: b for a, b in zip("xyz", bc or ())}
     p = lsgb.params(dim, n, n, n if dim == 3 else 1, dx=1.0 / n, dy=1.0 / n, dz=1.0 / n, s_l=0.15, dt=dt,
-                    enable_reinit=reinit, reinit_interval=reinit_interval, reinit_iterations=reinit_iterations)
+                    enable_reinit=reinit, reinit_interval=reinit_interval, reinit_iterations=reinit_iterations,
+                    **bcs)
     return p, G, u, v, w, sl, sl_t
 
 

@@ -4,9 +4,10 @@ Checks, with the tolerances stated per test:
   * FP64 adjoint vs central finite differences of the FP64 forward along
     smooth random directions in S_L, G0 and u (relative step 1e-6; the
     frozen upwind / Godunov / constraint choices do not flip at that step):
-    relative error <= 1e-5;
+    relative error <= 1e-5, with periodic and zero-gradient axes;
   * the same directional derivative from finite differences of the oracle's
-    forward (the CPU restatement of the reference) on the ghosted layout;
+    forward (the CPU restatement of the reference) on the ghosted layout,
+    3D periodic and 2D with the reference's zero-gradient y;
   * gradients are bit-identical for every checkpoint interval;
   * the FP32 adjoint against the FP64 adjoint: relative L2 <= 1e-3;
   * the torch autograd Function gives the native gradients.
@@ -17,11 +18,17 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def small(lsgb_mod, dim):
+def small(lsgb_mod, dim, bc=None):
     from lsgb import adjoint as adj
     n, steps = (20, 12) if dim == 3 else (40, 15)
-    p, G0, u, v, w, sl, sl_t = adj.workload(n, steps, dim=dim, reinit_interval=5)
+    p, G0, u, v, w, sl, sl_t = adj.workload(n, steps, dim=dim, reinit_interval=5, bc=bc)
     return adj, p, steps, G0, u, v, w, sl, sl_t
+
+
+ZG = "zero_gradient"
+# (dim, boundary per axis): periodic everywhere; the reference 2D solver's
+# default (periodic x, zero-gradient y); a 3D mix with clamped x and z
+FD_CASES = [(3, None), (2, None), (2, ("periodic", ZG)), (3, (ZG, "periodic", ZG))]
 
 
 def loss_of(prob, G0, u, sl, steps):
@@ -29,9 +36,9 @@ def loss_of(prob, G0, u, sl, steps):
     return prob.loss(sl, steps)
 
 
-@pytest.mark.parametrize("dim", [3, 2])
-def test_adjoint_matches_fd_f64(cuda, lsgb_mod, dim):
-    adj, p, steps, G0, u, v, w, sl, sl_t = small(lsgb_mod, dim)
+@pytest.mark.parametrize("dim,bc", FD_CASES, ids=["3d", "2d", "2d-zgy", "3d-zgxz"])
+def test_adjoint_matches_fd_f64(cuda, lsgb_mod, dim, bc):
+    adj, p, steps, G0, u, v, w, sl, sl_t = small(lsgb_mod, dim, bc)
     prob = adj.Problem(p, G0, u, v, w, "f64", checkpoint=4)
     try:
         prob.target(sl_t, steps)
@@ -58,7 +65,7 @@ def test_adjoint_matches_fd_f64(cuda, lsgb_mod, dim):
     finally:
         prob.close()
     for name, fd, ad in checks:
-        print(f"dim={dim} {name}: fd={fd:.10e} adjoint={ad:.10e} rel={abs(fd - ad) / abs(fd):.2e}")
+        print(f"dim={dim} bc={bc} {name}: fd={fd:.10e} adjoint={ad:.10e} rel={abs(fd - ad) / abs(fd):.2e}")
         assert abs(fd - ad) <= 1e-5 * abs(fd), (name, fd, ad)
 
 
@@ -88,6 +95,43 @@ def test_adjoint_matches_fd_of_oracle(cuda, lsgb_mod, port):
         fd = (oracle_loss(sl + h * d, gt) - oracle_loss(sl - h * d, gt)) / (2 * h)
         ad = float(np.sum(g_sl * d))
         print(f"oracle fd={fd:.10e} adjoint={ad:.10e}")
+        assert abs(fd - ad) <= 1e-5 * abs(fd)
+
+
+def test_adjoint_matches_fd_of_oracle_2d_zero_gradient_y(cuda, lsgb_mod, port):
+    """The reference 2D solver's boundaries (periodic x, zero-gradient y;
+    Local_code/level-set_MPI_2D/include/boundary.h:217): the adjoint's
+    directional derivative against finite differences of the oracle's 2D
+    forward with HCR-2 on (relative error <= 1e-5)."""
+    from oracle import Problem as OProblem
+    adj, p, steps, G0, u, v, w, sl, sl_t = small(lsgb_mod, 2, ("periodic", ZG))
+    n = p.nx
+    pb = OProblem(n, n, dim=2, dt=p.dt, s_l=p.s_l, enable_reinit=True, reinit_interval=5, reinit_iterations=2,
+                  periodic_y=False)
+
+    def gh(a):  # ghosted copy: y edge-padded, x wrapped
+        return np.ascontiguousarray(np.pad(np.pad(a, ((3, 3), (0, 0)), mode="edge"), ((0, 0), (3, 3)), mode="wrap"))
+
+    eps, dv = 1.5 / n, 1.0 / n ** 2
+
+    def oracle_loss(s_field, G_target):
+        out = port.run(pb, steps, gh(G0), gh(u), gh(v), sl=gh(s_field))[3:-3, 3:-3]
+        h, ht = 0.5 * (1 - np.tanh(out / eps)), 0.5 * (1 - np.tanh(G_target / eps))
+        return 0.5 * np.sum((h - ht) ** 2) * dv
+
+    prob = adj.Problem(p, G0, u, v, w, "f64", checkpoint=4)
+    try:
+        gt = prob.target(sl_t, steps)
+        _, g_sl = prob.gradient(sl, steps)
+    finally:
+        prob.close()
+    for q in range(2):
+        d = adj.fourier_field(sl.shape[::-1], 61 + q)
+        d /= np.linalg.norm(d)
+        h = 1e-6 * np.linalg.norm(sl)
+        fd = (oracle_loss(sl + h * d, gt) - oracle_loss(sl - h * d, gt)) / (2 * h)
+        ad = float(np.sum(g_sl * d))
+        print(f"oracle 2D zero-gradient y: fd={fd:.10e} adjoint={ad:.10e}")
         assert abs(fd - ad) <= 1e-5 * abs(fd)
 
 
@@ -145,10 +189,11 @@ def test_torch_rollout_gradients(cuda, lsgb_mod):
     assert tu.grad is not None and tv.grad is None
 
 
-@pytest.mark.parametrize("n", [(21, 18, 15), (16, 16, 9)])
-def test_f32_adjoint_odd_and_ragged_grids(cuda, lsgb_mod, n):
+@pytest.mark.parametrize("n,bc", [((21, 18, 15), "periodic"), ((16, 16, 9), "periodic"), ((21, 18, 15), ZG)])
+def test_f32_adjoint_odd_and_ragged_grids(cuda, lsgb_mod, n, bc):
     """FP32 plane-pair coefficient pass on grids with an odd nz and ragged
-    tiles, against the FP64 adjoint (relative L2 <= 1e-3)."""
+    tiles, periodic and zero-gradient on every axis, against the FP64 adjoint
+    (relative L2 <= 1e-3)."""
     from lsgb import adjoint as adj
     rng = np.random.default_rng(sum(n))
     shape = n[::-1]
@@ -158,7 +203,7 @@ def test_f32_adjoint_odd_and_ragged_grids(cuda, lsgb_mod, n):
     sl = 0.15 + 0.05 * adj.fourier_field(n, 3)
     seed = rng.standard_normal(shape) * (np.abs(G0) < 0.2)
     p = lsgb_mod.params(3, *n, dx=1 / n[0], dy=1 / n[1], dz=1 / n[2], s_l=0.15, dt=2e-3, enable_reinit=True,
-                        reinit_interval=4, reinit_iterations=2)
+                        reinit_interval=4, reinit_iterations=2, bc_x=bc, bc_y=bc, bc_z=bc)
     out = {}
     for prec in ("f64", "f32"):
         with lsgb_mod.Solver(p, prec) as s:
@@ -175,9 +220,12 @@ def test_f32_adjoint_odd_and_ragged_grids(cuda, lsgb_mod, n):
 
 
 @pytest.mark.parametrize("prec", ["f64", "f32"])
-def test_gradient_independent_of_z_slab(cuda, lsgb_mod, prec):
+@pytest.mark.parametrize("bcz", ["periodic", ZG])
+def test_gradient_independent_of_z_slab(cuda, lsgb_mod, prec, bcz):
     """The stage transpose runs in z slabs (coefficients L2-resident between
-    its two passes); every slab size gives the same gradients bit for bit."""
+    its two passes); every slab size gives the same gradients bit for bit,
+    with a periodic z axis and with a clamped one (whose slab planes outside
+    the grid hold no cell)."""
     from lsgb import adjoint as adj
     n = (40, 36, 30)
     shape = n[::-1]
@@ -187,7 +235,7 @@ def test_gradient_independent_of_z_slab(cuda, lsgb_mod, prec):
     sl = np.ascontiguousarray(0.15 + 0.05 * adj.fourier_field(n, 4))
     seed = np.ascontiguousarray(np.random.default_rng(9).standard_normal(shape) * (np.abs(G0) < 0.15))
     p = lsgb_mod.params(3, *n, dx=1 / n[0], dy=1 / n[1], dz=1 / n[2], s_l=0.15, dt=2e-3, enable_reinit=True,
-                        reinit_interval=4, reinit_iterations=2)
+                        reinit_interval=4, reinit_iterations=2, bc_z=bcz)
     res = []
     for slab in (0, 30, 7, 1):
         with lsgb_mod.Solver(p, prec) as s:
