@@ -350,7 +350,11 @@ LSGB_API int lsgb_adjoint_set_grads(lsgb_adjoint* a, int mask);
  * and more launches.  Any slab gives bit-identical gradients. */
 LSGB_API int lsgb_adjoint_set_slab(lsgb_adjoint* a, int planes);
 /* Advance the solver n_steps steps (same results as lsgb_solver_advance),
- * recording checkpoints; the solver ends at G_T. */
+ * recording checkpoints; the solver ends at G_T.  With live deformation
+ * velocity (lsgb_solver_set_velocity_deformation_live) the checkpoints also
+ * keep the vortex time, and the backward evaluates the vortex at every step's
+ * time; dL/du, dL/dv, dL/dw are then the gradients with respect to a steady
+ * field added to the vortex at every step (the per-step sensitivities summed). */
 LSGB_API int lsgb_adjoint_forward(lsgb_adjoint* a, int n_steps);
 /* Target field for the smoothed-Heaviside mismatch
  *   L = 1/2 sum_cells (H(G_T) - H(G_target))^2 dV,  H(g) = (1 - tanh(g / eps)) / 2. */

@@ -491,17 +491,22 @@ int ensure_defo_tables(lsgb_solver* s) {
 
 float defo_time_factor(double t, double T) { return (float)std::cos(3.14159265358979323846 * t / T); }
 
-// Write the vortex at time t into the stored velocity arrays.
-int fill_deformation(lsgb_solver* s, double t, double T) {
+// Write the vortex at time t into (u, v, w) on stream st.
+int fill_deformation_into(lsgb_solver* s, double t, double T, void* u, void* v, void* w, cudaStream_t st) {
     if (s->prec == LSGB_PREC_F64) {
-        LSGB_CUDA(launch_deformation_f64(s->g, s->p.dx, s->p.dy, s->p.dz, t, T, (double*)s->u, (double*)s->v,
-                                         (double*)s->w, s->st));
+        LSGB_CUDA(launch_deformation_f64(s->g, s->p.dx, s->p.dy, s->p.dz, t, T, (double*)u, (double*)v, (double*)w,
+                                         st));
     } else {
         LSGB_TRY(ensure_defo_tables(s));
-        LSGB_CUDA(launch_deformation_f32(s->g, s->defo_f32, defo_time_factor(t, T), (float*)s->u, (float*)s->v,
-                                         (float*)s->w, s->st));
+        LSGB_CUDA(launch_deformation_f32(s->g, s->defo_f32, defo_time_factor(t, T), (float*)u, (float*)v, (float*)w,
+                                         st));
     }
     return LSGB_OK;
+}
+
+// Write the vortex at time t into the stored velocity arrays.
+int fill_deformation(lsgb_solver* s, double t, double T) {
+    return fill_deformation_into(s, t, T, s->u, s->v, s->w, s->st);
 }
 
 // Live vortex evaluated inside the FP32 3D stage kernel (no u, v, w traffic).
@@ -1695,6 +1700,13 @@ struct lsgb_adjoint {
     void* lam[4] = {nullptr, nullptr, nullptr, nullptr};  // lambda buffers (solver precision)
     double* grad[4] = {nullptr, nullptr, nullptr, nullptr};  // dL/dS_L, dL/du, dL/dv, dL/dw
     double* target = nullptr;  // FP64 compact target
+    // live deformation velocity during the recorded forward: the vortex time
+    // at every checkpoint, and the fields the recompute (vel[0..2], recording
+    // stream) and the reverse sweep (vel[3..5], solver stream) refill per step
+    bool live = false;
+    double live_T = 1.0;
+    std::vector<double> ckpt_t;
+    char* vel = nullptr;
 };
 
 namespace {
@@ -1705,6 +1717,7 @@ struct TapeStep {
     int gn, g1, g2;
     int r0;      // first HCR-2 slot, -1 when no reinitialisation follows the step
     int out;
+    double t;    // vortex time of the step (live velocity)
 };
 
 bool reinit_after(const lsgb_params& p, int step) {
@@ -1728,6 +1741,23 @@ std::vector<TapeStep> tape_plan(const lsgb_params& p, int t0, int t1, int* slots
     *slots = cur + 1;
     return v;
 }
+
+// The tape plan of checkpoint segment seg, with the vortex time of every
+// step accumulated as the forward did (t += dt after each step).
+std::vector<TapeStep> segment_plan(const lsgb_adjoint* a, int seg, int* slots) {
+    const lsgb_solver* s = a->s;
+    const int t0 = a->step0 + seg * a->ckpt, t1 = std::min(t0 + a->ckpt, a->step0 + a->n_steps);
+    std::vector<TapeStep> plan = tape_plan(s->p, t0, t1, slots);
+    double t = a->live ? a->ckpt_t[seg] : 0.0;
+    for (TapeStep& r : plan) {
+        r.t = t;
+        t += s->p.dt;
+    }
+    return plan;
+}
+
+// velocity field q (0..2) of set b (0 = recompute, 1 = reverse sweep)
+void* live_vel(lsgb_adjoint* a, int b, int q) { return a->vel + (size_t)(3 * b + q) * a->slot; }
 
 int adj_ok(const lsgb_adjoint* a) {
     if (!a || !a->s) return fail(LSGB_ERR_INVALID, "adjoint handle is NULL");
@@ -1759,6 +1789,11 @@ int adj_record(lsgb_adjoint* a, const std::vector<TapeStep>& plan) {
     r.dtau = s->p.reinit_dtau;
     r.beta = s->p.reinit_beta;
     for (const TapeStep& t : plan) {
+        if (a->live) {
+            LSGB_TRY(fill_deformation_into(s, t.t, a->live_T, live_vel(a, 0, 0), live_vel(a, 0, 1), live_vel(a, 0, 2),
+                                           s->st));
+            st.u = live_vel(a, 0, 0); st.v = live_vel(a, 0, 1); st.w = live_vel(a, 0, 2);
+        }
         st.Gn = tslot(a, t.gn);
         st.Gin = tslot(a, t.gn); st.Gout = tslot(a, t.g1); st.stage = 1;
         LSGB_TRY(launch_stage(s, st));
@@ -1825,6 +1860,11 @@ int adj_reverse_step(lsgb_adjoint* a, const TapeStep& t, void** L) {
     std::memset(&c, 0, sizeof(c));
     c.g = g;
     c.u = s->u; c.v = s->v; c.w = s->w; c.sl = s->sl;
+    if (a->live) {
+        LSGB_TRY(fill_deformation_into(s, t.t, a->live_T, live_vel(a, 1, 0), live_vel(a, 1, 1), live_vel(a, 1, 2),
+                                       s->st));
+        c.u = live_vel(a, 1, 0); c.v = live_vel(a, 1, 1); c.w = live_vel(a, 1, 2);
+    }
     c.s_l = s->p.s_l;
     c.eps = s->p.epsilon;
     c.dx = s->p.dx;
@@ -1951,7 +1991,7 @@ extern "C" int lsgb_adjoint_destroy(lsgb_adjoint* a) {
     if (a->s && a->s->st) cudaStreamSynchronize(a->s->st);
     if (a->rs) cudaStreamSynchronize(a->rs);
     void* ptrs[] = {a->tape_buf[0], a->tape_buf[1], a->ckpts, a->coef, a->lam[0], a->lam[1], a->lam[2],
-                    a->lam[3], a->grad[0], a->grad[1], a->grad[2], a->grad[3], a->target};
+                    a->lam[3], a->grad[0], a->grad[1], a->grad[2], a->grad[3], a->target, a->vel};
     for (void* q : ptrs)
         if (q) cudaFree(q);
     for (int b = 0; b < 2; ++b) {
@@ -1989,8 +2029,11 @@ extern "C" int lsgb_adjoint_forward(lsgb_adjoint* a, int n_steps) {
     lsgb_solver* s = a->s;
     if (n_steps < 1) return fail(LSGB_ERR_INVALID, "n_steps must be >= 1");
     if (!s->have_G || !s->have_vel) return fail(LSGB_ERR_STATE, "fields not set");
-    if (s->vel_live) return fail(LSGB_ERR_UNSUPPORTED, "the adjoint needs a fixed velocity field (live velocity is on)");
     const int nseg = (n_steps + a->ckpt - 1) / a->ckpt;
+    if (s->vel_live && !a->vel) {
+        LSGB_CUDA(cudaStreamSynchronize(s->st));
+        LSGB_TRY(adj_alloc((void**)&a->vel, 6 * a->slot, "live velocity fields"));
+    }
     if (nseg > a->ckpt_slots) {
         LSGB_CUDA(cudaStreamSynchronize(s->st));
         if (a->ckpts) cudaFree(a->ckpts);
@@ -2001,7 +2044,11 @@ extern "C" int lsgb_adjoint_forward(lsgb_adjoint* a, int n_steps) {
     }
     a->step0 = s->step;
     a->have_fwd = a->have_seed = a->have_grad = false;
+    a->live = s->vel_live;
+    a->live_T = s->vel_T;
+    a->ckpt_t.assign(nseg, 0.0);
     for (int seg = 0; seg < nseg; ++seg) {
+        a->ckpt_t[seg] = s->vel_t;
         LSGB_CUDA(cudaMemcpyAsync(a->ckpts + (size_t)seg * a->slot, s->G, nbytes(s), cudaMemcpyDeviceToDevice, s->st));
         const int n = std::min(a->ckpt, n_steps - seg * a->ckpt);
         LSGB_TRY(lsgb_solver_advance(s, n));
@@ -2100,9 +2147,8 @@ extern "C" int lsgb_adjoint_backward(lsgb_adjoint* a, const double* dL_dGT, int 
     // Segment seg's tape: its checkpoint re-advanced with the forward kernels
     // on stream st into tape buffer b.
     auto record = [&](int seg, int b, cudaStream_t st) -> int {
-        const int t0 = a->step0 + seg * a->ckpt, t1 = std::min(t0 + a->ckpt, a->step0 + a->n_steps);
         int slots = 0;
-        const std::vector<TapeStep> plan = tape_plan(s->p, t0, t1, &slots);
+        const std::vector<TapeStep> plan = segment_plan(a, seg, &slots);
         a->tape = a->tape_buf[b];
         cudaStream_t own = s->st;
         s->st = st;
@@ -2138,9 +2184,8 @@ extern "C" int lsgb_adjoint_backward(lsgb_adjoint* a, const double* dL_dGT, int 
         } else {
             LSGB_TRY(record(seg, 0, s->st));
         }
-        const int t0 = a->step0 + seg * a->ckpt, t1 = std::min(t0 + a->ckpt, a->step0 + a->n_steps);
         int slots = 0;
-        const std::vector<TapeStep> plan = tape_plan(s->p, t0, t1, &slots);
+        const std::vector<TapeStep> plan = segment_plan(a, seg, &slots);
         a->tape = a->tape_buf[cur];
         for (int q = (int)plan.size() - 1; q >= 0; --q) {
             if (s->prec == LSGB_PREC_F64) LSGB_TRY(adj_reverse_step<double>(a, plan[q], &L));

@@ -10,6 +10,8 @@ Checks, with the tolerances stated per test:
     3D periodic and 2D with the reference's zero-gradient y;
   * gradients are bit-identical for every checkpoint interval;
   * the FP32 adjoint against the FP64 adjoint: relative L2 <= 1e-3;
+  * live deformation velocity: FD of the live forward, checkpoint
+    independence and FP32 vs FP64;
   * the torch autograd Function gives the native gradients.
 """
 import numpy as np
@@ -133,6 +135,83 @@ def test_adjoint_matches_fd_of_oracle_2d_zero_gradient_y(cuda, lsgb_mod, port):
         ad = float(np.sum(g_sl * d))
         print(f"oracle 2D zero-gradient y: fd={fd:.10e} adjoint={ad:.10e}")
         assert abs(fd - ad) <= 1e-5 * abs(fd)
+
+
+def _live_setup(lsgb_mod, prec):
+    """20^3 sphere in the reference's live deformation vortex (time factor
+    cos(pi t / T), T = 0.5, from t = 0.05), HCR-2 every 5 steps."""
+    from lsgb import adjoint as adj
+    n, steps = 20, 12
+    _, G0, _, _, _, sl, sl_t = adj.workload(n, steps, reinit_interval=5)
+    p = lsgb_mod.params(3, n, n, n, dx=1 / n, dy=1 / n, dz=1 / n, s_l=0.15, dt=0.5 / n / 2.2, enable_reinit=True,
+                        reinit_interval=5, reinit_iterations=2)
+    return adj, p, steps, G0, sl, sl_t
+
+
+def _live_run(s, a, G0, sl, steps, record=False):
+    s.set_fields(G0, layout="compact")
+    s.set_sl_field(sl, layout="compact")
+    s.set_velocity_deformation_live(0.05, 0.5)
+    s.step = 0
+    if record:
+        a.forward(steps)
+    else:
+        s.advance(steps)
+
+
+def test_adjoint_live_deformation_velocity_fd(cuda, lsgb_mod):
+    """Live velocity (the vortex re-evaluated every step): FP64 adjoint vs
+    central FD of the live FP64 forward in S_L and G0 (relative <= 1e-5)."""
+    adj, p, steps, G0, sl, sl_t = _live_setup(lsgb_mod, "f64")
+    with lsgb_mod.Solver(p, "f64") as s, lsgb_mod.Adjoint(s, 5) as a:
+        _live_run(s, a, G0, sl_t, steps)
+        a.set_target(s.get_G(layout="compact"), 1.5 * p.dx, layout="compact")
+
+        def loss(G, f):
+            _live_run(s, a, G, f, steps)
+            return a.loss()
+
+        _live_run(s, a, G0, sl, steps, record=True)
+        L = a.loss(seed=True)
+        a.backward()
+        g_sl, g_G0, g_u = a.grad("sl"), a.grad("G0"), a.grad("u")
+        assert L > 0 and np.isfinite(g_u).all() and np.abs(g_u).max() > 0
+        checks = []
+        for q in range(2):
+            d = adj.fourier_field(sl.shape[::-1], 71 + q)
+            d /= np.linalg.norm(d)
+            h = 1e-6 * np.linalg.norm(sl)
+            checks.append(("sl", (loss(G0, sl + h * d) - loss(G0, sl - h * d)) / (2 * h), float(np.sum(g_sl * d))))
+        d = adj.fourier_field(sl.shape[::-1], 81)
+        d /= np.linalg.norm(d)
+        h = 1e-6 * np.linalg.norm(G0)
+        checks.append(("G0", (loss(G0 + h * d, sl) - loss(G0 - h * d, sl)) / (2 * h), float(np.sum(g_G0 * d))))
+    for name, fd, ad in checks:
+        print(f"live {name}: fd={fd:.10e} adjoint={ad:.10e} rel={abs(fd - ad) / abs(fd):.2e}")
+        assert abs(fd - ad) <= 1e-5 * abs(fd), (name, fd, ad)
+
+
+def test_adjoint_live_velocity_checkpoints_and_f32(cuda, lsgb_mod):
+    """Live velocity: gradients bit-identical for checkpoint intervals 1, 5
+    and 50 (the vortex time is carried across segments and the recording
+    and reverse streams refill their own fields), and the FP32 adjoint (whose
+    forward forms the vortex inside the stage kernel) within 1e-3 relative
+    L2 of the FP64 one."""
+    adj, p, steps, G0, sl, sl_t = _live_setup(lsgb_mod, "f64")
+    seed = np.ascontiguousarray(np.random.default_rng(5).standard_normal(G0.shape) * (np.abs(G0) < 0.2))
+    out = {}
+    for prec, ck in (("f64", 1), ("f64", 5), ("f64", 50), ("f32", 5)):
+        with lsgb_mod.Solver(p, prec) as s, lsgb_mod.Adjoint(s, ck) as a:
+            _live_run(s, a, G0, sl, steps, record=True)
+            a.backward(seed, layout="compact")
+            out[(prec, ck)] = (a.grad("sl"), a.grad("G0"), a.grad("w"))
+    for ck in (1, 50):
+        for g, g0 in zip(out[("f64", ck)], out[("f64", 5)]):
+            assert np.array_equal(g, g0)
+    for g32, g64 in zip(out[("f32", 5)], out[("f64", 5)]):
+        rel = np.linalg.norm(g32 - g64) / np.linalg.norm(g64)
+        print(f"live f32 vs f64 rel L2 {rel:.3e}")
+        assert rel <= 1e-3
 
 
 def test_gradient_independent_of_checkpoint_interval(cuda, lsgb_mod):
