@@ -388,8 +388,12 @@ LSGB_API int lsgb_solver_set_velocity_deformation(lsgb_solver* s, double t, doub
  * Either way the fields equal a per-step lsgb_solver_set_velocity_deformation
  * loop bit for bit.  Calls that read u, v, w (lsgb_solver_max_speed,
  * lsgb_solver_get_field) see the vortex at the current time.  Setting
- * velocity arrays ends live mode; batches and the adjoint reject handles in
- * it (LSGB_ERR_UNSUPPORTED). */
+ * velocity arrays ends live mode.  Batches advance live handles too: the
+ * host evaluates every step's time (FP64) or time factor (FP32) of an
+ * lsgb_batch_advance call as above into a device table, and the batch's
+ * launches (captured graphs included) refill u, v, w from it, indexed by a
+ * device-side step cursor -- the same bits as the handle advanced alone.
+ * The adjoint follows live handles (lsgb_adjoint_forward). */
 LSGB_API int lsgb_solver_set_velocity_deformation_live(lsgb_solver* s, double t, double T);
 /* The live-mode time (the t of the next step). */
 LSGB_API int lsgb_solver_get_time(const lsgb_solver* s, double* t);

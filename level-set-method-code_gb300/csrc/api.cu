@@ -348,6 +348,9 @@ struct lsgb_solver {
     bool vel_live = false;
     double vel_t = 0.0, vel_T = 1.0;
     float* defo_f32 = nullptr;  // FP32 factor tables of the vortex (built once)
+    // set while a batch advances a live instance: the vortex time (FP64) or
+    // time factor (FP32) of each step comes from the batch's device table
+    LiveAt batch_live;
     int tile = 0;  // tile-shape choice handed to the stage kernels (0 = default)
     int drop_copies = 0;  // test hook (lsgb_solver_debug_drop_copies)
     // set when a kernel gave up with bulk copies still in flight into its
@@ -491,27 +494,30 @@ int ensure_defo_tables(lsgb_solver* s) {
 
 float defo_time_factor(double t, double T) { return (float)std::cos(3.14159265358979323846 * t / T); }
 
-// Write the vortex at time t into (u, v, w) on stream st.
-int fill_deformation_into(lsgb_solver* s, double t, double T, void* u, void* v, void* w, cudaStream_t st) {
+// Write the vortex at time t (or at the time the device table of at names)
+// into (u, v, w) on stream st.
+int fill_deformation_into(lsgb_solver* s, double t, double T, void* u, void* v, void* w, cudaStream_t st,
+                          LiveAt at = LiveAt()) {
     if (s->prec == LSGB_PREC_F64) {
         LSGB_CUDA(launch_deformation_f64(s->g, s->p.dx, s->p.dy, s->p.dz, t, T, (double*)u, (double*)v, (double*)w,
-                                         st));
+                                         st, at));
     } else {
         LSGB_TRY(ensure_defo_tables(s));
         LSGB_CUDA(launch_deformation_f32(s->g, s->defo_f32, defo_time_factor(t, T), (float*)u, (float*)v, (float*)w,
-                                         st));
+                                         st, at));
     }
     return LSGB_OK;
 }
 
 // Write the vortex at time t into the stored velocity arrays.
 int fill_deformation(lsgb_solver* s, double t, double T) {
-    return fill_deformation_into(s, t, T, s->u, s->v, s->w, s->st);
+    return fill_deformation_into(s, t, T, s->u, s->v, s->w, s->st, s->batch_live);
 }
 
 // Live vortex evaluated inside the FP32 3D stage kernel (no u, v, w traffic).
+// (Not inside a batch: its launches refill the arrays from the device table.)
 bool live_fused(const lsgb_solver* s) {
-    return s->vel_live && s->prec == LSGB_PREC_F32 && stage3d_f32_fuses_deformation(s->g);
+    return s->vel_live && !s->batch_live.tab && s->prec == LSGB_PREC_F32 && stage3d_f32_fuses_deformation(s->g);
 }
 
 // Velocity operands of a stage launch: the stored arrays, or the fused vortex.
@@ -1126,6 +1132,17 @@ struct lsgb_batch {
     long long blk3 = 0, tiles2 = 0, rblk3 = 0, rblk2 = 0, cblk3 = 0, cblk2 = 0;
     int iters = 0;                    // HCR-2 pseudo-steps (uniform over the batch)
     std::vector<long long> sig;       // launch shapes the captured graph was made with
+    // live deformation velocity: per live instance a slot of live_cap entries
+    // (FP64 time or FP32 time factor of each step of one advance call), and
+    // the device cursor the launches index it from
+    std::vector<int> live;            // instance indices with live velocity
+    std::vector<long long> live_sig;  // live set + table the captured graph was made with
+    char* live_tab = nullptr;
+    int* live_base = nullptr;
+    size_t live_cap = 0;
+    char* live_h = nullptr;           // pinned staging of the table
+    size_t live_h_bytes = 0;
+    cudaEvent_t live_copied = nullptr;  // the last upload from live_h
 };
 
 namespace {
@@ -1165,6 +1182,7 @@ int batch_launch_steps(lsgb_batch* b, int n_steps) {
             lsgb_solver* s = b->inst[i];
             cudaStream_t own = s->st;
             s->st = b->lanes[i % b->lanes.size()];
+            s->batch_live.q = q;
             int rc = rk3_step(s);
             if (rc == LSGB_OK && s->p.enable_reinit && s->step > 0 && s->step % s->p.reinit_interval == 0)
                 rc = reinit(s);
@@ -1177,6 +1195,7 @@ int batch_launch_steps(lsgb_batch* b, int n_steps) {
         LSGB_CUDA(cudaEventRecord(b->lane_done[l], b->lanes[l]));
         LSGB_CUDA(cudaStreamWaitEvent(b->main, b->lane_done[l], 0));
     }
+    if (!b->live.empty()) LSGB_CUDA(launch_live_advance(b->live_base, n_steps, b->main));
     return LSGB_OK;
 }
 
@@ -1185,7 +1204,7 @@ int batch_launch_steps(lsgb_batch* b, int n_steps) {
 bool batch_grouped_ok(const lsgb_batch* b) {
     if (b->mode != LSGB_BATCH_GROUPED || b->prec != LSGB_PREC_F32 || b->inst.empty()) return false;
     for (const lsgb_solver* s : b->inst) {
-        if (s->g.cells() >= (1LL << 31) - 1 || s->vel_live) return false;
+        if (s->g.cells() >= (1LL << 31) - 1) return false;
         if (s->p.enable_reinit && s->p.reinit_iterations != b->inst[0]->p.reinit_iterations) return false;
     }
     return true;
@@ -1303,6 +1322,11 @@ int batch_launch_steps_grouped(lsgb_batch* b, int n_steps) {
     const int* o3 = (const int*)(d + b->oo3);
     const int* o2 = (const int*)(d + b->oo2);
     for (int q = 0; q < n_steps; ++q) {
+        for (int i : b->live) {  // live instances (3D): the vortex of this step into u, v, w
+            lsgb_solver* s = b->inst[i];
+            s->batch_live.q = q;
+            LSGB_TRY(fill_deformation_into(s, s->vel_t, s->vel_T, s->u, s->v, s->w, s3, s->batch_live));
+        }
         for (int stage = 1; stage <= 3; ++stage) {
             LSGB_CUDA(launch_stage3d_f32_group(d + b->off3, o3, n3, b->blk3, stage, s3));
             LSGB_CUDA(launch_stage2d_f32_group(d + b->off2, o2, n2, b->tiles2, stage, b->shape2, s2));
@@ -1324,7 +1348,80 @@ int batch_launch_steps_grouped(lsgb_batch* b, int n_steps) {
         LSGB_CUDA(cudaEventRecord(b->lane_done[1], s2));
         LSGB_CUDA(cudaStreamWaitEvent(b->main, b->lane_done[1], 0));
     }
+    if (!b->live.empty()) LSGB_CUDA(launch_live_advance(b->live_base, n_steps, b->main));
     return LSGB_OK;
+}
+
+// Live instances of an advance call of n_steps: their per-step vortex times
+// (FP64) or time factors (FP32), accumulated as lsgb_solver_advance does
+// (t += dt after every step) and evaluated with the same host function, go
+// into the device table; the launches read entry *live_base + q.  A grown
+// table drops the captured graph (its launches hold the table's address).
+int batch_live_begin(lsgb_batch* b, int n_steps) {
+    b->live.clear();
+    for (size_t i = 0; i < b->inst.size(); ++i)
+        if (b->inst[i]->vel_live) b->live.push_back((int)i);
+    if (b->live.empty()) {
+        if (!b->live_sig.empty()) batch_drop_graph(b);
+        b->live_sig.clear();
+        return LSGB_OK;
+    }
+    const size_t esz = b->prec == LSGB_PREC_F64 ? sizeof(double) : sizeof(float);
+    size_t cap = std::max<size_t>(b->live_cap, 64);
+    while (cap < (size_t)n_steps) cap *= 2;
+    const size_t bytes = cap * esz * b->live.size();
+    if (!b->live_base) {
+        cudaError_t e = cudaMalloc((void**)&b->live_base, 256);
+        if (e != cudaSuccess) { b->live_base = nullptr; return fail(LSGB_ERR_ALLOC, "batch live cursor: %s", cudaGetErrorString(e)); }
+    }
+    if (!b->live_copied) LSGB_CUDA(cudaEventCreateWithFlags(&b->live_copied, cudaEventDisableTiming));
+    LSGB_CUDA(cudaEventSynchronize(b->live_copied));  // live_h is free again
+    if (cap != b->live_cap || bytes > b->live_h_bytes) {
+        LSGB_CUDA(cudaStreamSynchronize(b->main));
+        if (b->live_tab) cudaFree(b->live_tab);
+        if (b->live_h) cudaFreeHost(b->live_h);
+        b->live_tab = nullptr;
+        b->live_h = nullptr;
+        b->live_cap = b->live_h_bytes = 0;
+        cudaError_t e = cudaMalloc((void**)&b->live_tab, bytes);
+        if (e != cudaSuccess) { b->live_tab = nullptr; return fail(LSGB_ERR_ALLOC, "batch live table: %s", cudaGetErrorString(e)); }
+        e = cudaMallocHost((void**)&b->live_h, bytes);
+        if (e != cudaSuccess) { b->live_h = nullptr; return fail(LSGB_ERR_ALLOC, "batch live staging: %s", cudaGetErrorString(e)); }
+        b->live_cap = cap;
+        b->live_h_bytes = bytes;
+    }
+    std::vector<long long> sig = {(long long)(uintptr_t)b->live_tab, (long long)cap};
+    for (int i : b->live) sig.push_back(i);
+    if (sig != b->live_sig) batch_drop_graph(b);
+    b->live_sig = sig;
+    for (size_t r = 0; r < b->live.size(); ++r) {
+        lsgb_solver* s = b->inst[b->live[r]];
+        char* slot = b->live_h + r * cap * esz;
+        double t = s->vel_t;
+        for (int n = 0; n < n_steps; ++n) {
+            if (esz == sizeof(double)) ((double*)slot)[n] = t;
+            else ((float*)slot)[n] = defo_time_factor(t, s->vel_T);
+            t += s->p.dt;
+        }
+        s->batch_live.tab = b->live_tab + r * cap * esz;
+        s->batch_live.base = b->live_base;
+        s->batch_live.q = 0;
+    }
+    LSGB_CUDA(cudaMemcpyAsync(b->live_tab, b->live_h, cap * esz * b->live.size(), cudaMemcpyHostToDevice, b->main));
+    LSGB_CUDA(cudaEventRecord(b->live_copied, b->main));
+    LSGB_CUDA(cudaMemsetAsync(b->live_base, 0, sizeof(int), b->main));
+    return LSGB_OK;
+}
+
+// After an advance call: the live instances' clocks move on by n_steps
+// steps and they leave the batch's table.
+void batch_live_end(lsgb_batch* b, int n_steps, bool advanced) {
+    for (int i : b->live) {
+        lsgb_solver* s = b->inst[i];
+        if (advanced)
+            for (int n = 0; n < n_steps; ++n) s->vel_t += s->p.dt;
+        s->batch_live = LiveAt();
+    }
 }
 
 }  // namespace
@@ -1360,6 +1457,10 @@ extern "C" int lsgb_batch_destroy(lsgb_batch* b) {
     if (b->main) cudaStreamSynchronize(b->main);
     batch_drop_graph(b);
     if (b->d_tab) cudaFree(b->d_tab);
+    if (b->live_tab) cudaFree(b->live_tab);
+    if (b->live_base) cudaFree(b->live_base);
+    if (b->live_h) cudaFreeHost(b->live_h);
+    if (b->live_copied) cudaEventDestroy(b->live_copied);
     for (lsgb_solver* s : b->inst) lsgb_solver_destroy(s);
     for (cudaStream_t l : b->lanes) cudaStreamDestroy(l);
     for (cudaEvent_t ev : b->lane_done) cudaEventDestroy(ev);
@@ -1520,8 +1621,9 @@ int batch_autotune_grouped(lsgb_batch* b, int reps) {
 // and long chunks win by their smaller halo overhead.)
 extern "C" int lsgb_batch_autotune(lsgb_batch* b, int reps) {
     LSGB_TRY(batch_ok(b));
+    // live instances are timed on the vortex at their current time
     for (lsgb_solver* s : b->inst)
-        if (s->vel_live) return fail(LSGB_ERR_UNSUPPORTED, "an instance has live velocity (replayed graphs need fixed fields)");
+        if (s->vel_live) LSGB_TRY(materialize_velocity(s));
     for (lsgb_solver* s : b->inst) LSGB_TRY(lsgb_solver_autotune(s, reps, nullptr, nullptr));
     batch_drop_graph(b);
     if (b->prec != LSGB_PREC_F32 || b->inst.empty()) return LSGB_OK;
@@ -1559,17 +1661,23 @@ extern "C" int lsgb_batch_advance(lsgb_batch* b, int n_steps) {
     LSGB_TRY(batch_ok(b));
     if (n_steps < 0) return fail(LSGB_ERR_INVALID, "n_steps < 0");
     if (b->inst.empty() || n_steps == 0) return LSGB_OK;
-    for (lsgb_solver* s : b->inst) {
+    for (lsgb_solver* s : b->inst)
         if (!s->have_G || !s->have_vel) return fail(LSGB_ERR_STATE, "an instance has no fields");
-        if (s->vel_live) return fail(LSGB_ERR_UNSUPPORTED, "an instance has live velocity (replayed graphs need fixed fields)");
-    }
     int step, interval, reinit_on;
     LSGB_TRY(batch_uniform(b, &step, &interval, &reinit_on));
+    // live instances read each step's vortex time from a device table
+    struct LiveScope {
+        lsgb_batch* b;
+        int n;
+        bool ok = false;
+        ~LiveScope() { batch_live_end(b, n, ok); }
+    } live_scope{b, n_steps};
     // order the batch after any work queued on the instances' own streams
     for (lsgb_solver* s : b->inst) {
         LSGB_CUDA(cudaEventRecord(b->done, s->st));
         LSGB_CUDA(cudaStreamWaitEvent(b->main, b->done, 0));
     }
+    LSGB_TRY(batch_live_begin(b, n_steps));
     // Steps before the first period boundary run as direct launches.  A
     // period starts at a step s with s % interval == 1 (the reinit then runs
     // after its last step), so its launch sequence is the same every time and
@@ -1632,6 +1740,7 @@ extern "C" int lsgb_batch_advance(lsgb_batch* b, int n_steps) {
         }
     }
     if (remaining > 0) LSGB_TRY(direct(remaining));
+    live_scope.ok = true;
     // later calls on an instance's own stream see the batch's results
     LSGB_CUDA(cudaEventRecord(b->done, b->main));
     for (lsgb_solver* s : b->inst) LSGB_CUDA(cudaStreamWaitEvent(s->st, b->done, 0));

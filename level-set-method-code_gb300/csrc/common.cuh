@@ -207,13 +207,23 @@ cudaError_t launch_synth(const Geo& g, const lsgb_synth& d, double dx, double dy
 // Deformation vortex (synth.cu).  FP64: the reference's per-cell products at
 // time t.  FP32: time-independent factor tables (deformation_table_floats
 // floats, built once per grid) and the field at tf = cos(pi t / T).
+// LiveAt: when tab is set, the time (FP64, double t) or time factor (FP32,
+// float tf) is read on the device from tab[*base + q] instead -- a batch's
+// per-step table, with base advanced on the device between graph replays.
+struct LiveAt {
+    const void* tab = nullptr;
+    const int* base = nullptr;
+    int q = 0;
+};
 cudaError_t launch_deformation_f64(const Geo& g, double dx, double dy, double dz, double t, double Tp,
-                                   double* u, double* v, double* w, cudaStream_t st);
+                                   double* u, double* v, double* w, cudaStream_t st, LiveAt at = LiveAt());
 size_t deformation_table_floats(const Geo& g);
 cudaError_t launch_deformation_tables_f32(const Geo& g, double dx, double dy, double dz, float* tab,
                                           cudaStream_t st);
 cudaError_t launch_deformation_f32(const Geo& g, const float* tab, float tf, float* u, float* v, float* w,
-                                   cudaStream_t st);
+                                   cudaStream_t st, LiveAt at = LiveAt());
+// *base += n (one thread): a batch's live-table cursor after a launch sequence
+cudaError_t launch_live_advance(int* base, int n, cudaStream_t st);
 
 // Views into the FP32 factor tables: per axis [sin^2(pi x_i)], [sin(2 pi x_i)],
 // n + 1 entries each (the last 0, so a plane pair may read one past nz).

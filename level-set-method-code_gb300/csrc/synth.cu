@@ -95,8 +95,9 @@ __global__ void scale3_kernel(long long n, double s, double* u, double* v, doubl
 // FP64: tab = [sin(pi x_i)][sin(2 pi x_i)] [.. y ..] [.. z ..] [cos(pi t / T)]
 // per call, and each cell forms the reference's products in its order:
 // exactly the values of evaluating the sines at every cell.
+// at.tab set: the time is at.tab[*at.base + at.q] (a batch's per-step table).
 __global__ void deformation_factors_f64_kernel(Geo g, double dx, double dy, double dz, double t, double Tp,
-                                               double* __restrict__ tab) {
+                                               LiveAt at, double* __restrict__ tab) {
     const double pi = 3.14159265358979323846;
     const int n[3] = {g.nx, g.ny, g.nz};
     const double h[3] = {dx, dy, dz};
@@ -109,7 +110,10 @@ __global__ void deformation_factors_f64_kernel(Geo g, double dx, double dy, doub
         }
         base += 2 * n[a];
     }
-    if (blockIdx.x == 0 && threadIdx.x == 0) tab[base] = cos(pi * t / Tp);
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        const double tt = at.tab ? ((const double*)at.tab)[*at.base + at.q] : t;
+        tab[base] = cos(pi * tt / Tp);
+    }
 }
 
 // One thread per cell of a row segment; rows (j, k) strided over gridDim.y.
@@ -159,9 +163,11 @@ __global__ void deformation_tables_f32_kernel(Geo g, double dx, double dy, doubl
     }
 }
 
-__global__ void deformation_f32_kernel(Geo g, const float* __restrict__ tab, float tf, float* __restrict__ u,
-                                       float* __restrict__ v, float* __restrict__ w) {
+// at.tab set: tf = at.tab[*at.base + at.q] (a batch's per-step table).
+__global__ void deformation_f32_kernel(Geo g, const float* __restrict__ tab, float tf, LiveAt at,
+                                       float* __restrict__ u, float* __restrict__ v, float* __restrict__ w) {
     const DeformTables d = deform_tables(g, tab);
+    if (at.tab) tf = ((const float*)at.tab)[*at.base + at.q];
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= g.nx) return;
     const long long rows = (long long)g.ny * g.nz;
@@ -175,6 +181,8 @@ __global__ void deformation_f32_kernel(Geo g, const float* __restrict__ tab, flo
     }
 }
 
+__global__ void live_advance_kernel(int* base, int n) { *base += n; }
+
 dim3 deformation_grid(const Geo& g) {
     const long long rows = (long long)g.ny * g.nz;
     return dim3((g.nx + 127) / 128, (unsigned)(rows < 65535 ? rows : 65535));
@@ -183,17 +191,23 @@ dim3 deformation_grid(const Geo& g) {
 }  // namespace
 
 cudaError_t launch_deformation_f64(const Geo& g, double dx, double dy, double dz, double t, double Tp,
-                                   double* u, double* v, double* w, cudaStream_t st) {
+                                   double* u, double* v, double* w, cudaStream_t st, LiveAt at) {
     double* tab = nullptr;
     const size_t ntab = 2 * ((size_t)g.nx + g.ny + g.nz) + 1;
     cudaError_t e = cudaMallocAsync((void**)&tab, ntab * sizeof(double), st);
     if (e != cudaSuccess) return e;
-    deformation_factors_f64_kernel<<<8, 256, 0, st>>>(g, dx, dy, dz, t, Tp, tab);
+    deformation_factors_f64_kernel<<<8, 256, 0, st>>>(g, dx, dy, dz, t, Tp, at, tab);
     deformation_f64_kernel<<<deformation_grid(g), 128, 0, st>>>(g, tab, u, v, w);
     count_launches(2);
     e = cudaGetLastError();
     const cudaError_t f = cudaFreeAsync(tab, st);
     return e != cudaSuccess ? e : f;
+}
+
+cudaError_t launch_live_advance(int* base, int n, cudaStream_t st) {
+    live_advance_kernel<<<1, 1, 0, st>>>(base, n);
+    count_launches(1);
+    return cudaGetLastError();
 }
 
 size_t deformation_table_floats(const Geo& g) { return 2 * ((size_t)g.nx + g.ny + g.nz + 3); }
@@ -206,8 +220,8 @@ cudaError_t launch_deformation_tables_f32(const Geo& g, double dx, double dy, do
 }
 
 cudaError_t launch_deformation_f32(const Geo& g, const float* tab, float tf, float* u, float* v, float* w,
-                                   cudaStream_t st) {
-    deformation_f32_kernel<<<deformation_grid(g), 128, 0, st>>>(g, tab, tf, u, v, w);
+                                   cudaStream_t st, LiveAt at) {
+    deformation_f32_kernel<<<deformation_grid(g), 128, 0, st>>>(g, tab, tf, at, u, v, w);
     count_launches(1);
     return cudaGetLastError();
 }

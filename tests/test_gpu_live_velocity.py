@@ -58,7 +58,7 @@ def test_live_equals_per_step_loop(cuda, lsgb_mod, prec, n, bc):
     assert float(np.abs(live - sphere(n, tuple(1.0 / (q - 1) for q in n))).max()) > 1e-4  # the front moved
 
 
-def test_live_rejected_by_batch_accepted_by_adjoint(cuda, lsgb_mod):
+def test_live_accepted_by_adjoint(cuda, lsgb_mod):
     n = (32, 32, 32)
     with make(lsgb_mod, "f32", n, 0) as s:
         s.set_velocity_deformation_live(0.0, T)
@@ -67,17 +67,57 @@ def test_live_rejected_by_batch_accepted_by_adjoint(cuda, lsgb_mod):
             a.backward(np.ones((32, 32, 32)), layout="compact")
             assert np.isfinite(a.grad("sl")).all()
         assert abs(s.time() - 6 * s.params().dt) < 1e-12  # the forward advanced the vortex time
-    h = 1.0 / 31
-    with lsgb_mod.Batch("f32", lanes=2) as b:
-        p = lsgb_mod.params(3, *n, dx=h, dy=h, dz=h, dt=2e-3)
-        s = b.add(p)
-        G = sphere(n, (h, h, h))
-        zero = np.zeros_like(G)
-        s.set_fields(G, zero, zero, zero, layout="compact")
-        s.set_velocity_deformation_live(0.0, T)
-        with pytest.raises(lsgb_mod.LsgbError) as e:
-            b.advance(1)
-        assert e.value.code == lsgb_mod.ERR_UNSUPPORTED
-        s.set_velocity_deformation(0.0, T)  # arrays again: the batch runs
-        b.advance(1)
+
+
+# (grid, live, zero-gradient): FP32 grids with nx % 4 == 0 form the vortex
+# inside the stage kernel when run alone; in a batch every live instance
+# refills u, v, w from the batch's per-step time table
+BATCH_CASES = [((32, 28, 24), True, 0), ((37, 21, 30), True, 1), ((24, 24, 20), False, 0), ((36, 32, 18), True, 0)]
+
+
+def _batch_instance(lsgb, s, n, live, t0):
+    h = tuple(1.0 / (q - 1) for q in n)
+    G = sphere(n, h)
+    if live:
+        s.set_fields(G, layout="compact")
+        s.set_velocity_deformation_live(t0, T)
+    else:
+        s.set_fields(G, *(0.3 * np.ones_like(G) for _ in range(3)), layout="compact")
+
+
+def _params(lsgb, n, bc):
+    h = tuple(1.0 / (q - 1) for q in n)
+    return lsgb.params(3, *n, dx=h[0], dy=h[1], dz=h[2], dt=2e-3, s_l=0.05, enable_reinit=True,
+                       reinit_interval=3, reinit_iterations=2, bc_x=bc, bc_y=bc, bc_z=bc)
+
+
+@pytest.mark.parametrize("prec,mode", [("f32", "grouped"), ("f32", "lanes"), ("f64", "lanes")])
+def test_batch_live_equals_solver(cuda, lsgb_mod, prec, mode):
+    """Batched live instances (the vortex time of every step read from a
+    device table that replayed graphs index by a device-side cursor) equal
+    the same instances advanced alone in live mode, bit for bit, beside a
+    fixed-velocity instance; two advance calls (7 + 11 steps) cover the
+    direct head, the graph replays, the tail and the table's reuse."""
+    chunks = (7, 11)
+    alone = []
+    for q, (n, live, bc) in enumerate(BATCH_CASES):
+        with lsgb_mod.Solver(_params(lsgb_mod, n, bc), prec) as s:
+            _batch_instance(lsgb_mod, s, n, live, 0.1 * q)
+            for c in chunks:
+                s.advance(c)
+            alone.append((s.get_G(layout="compact"), s.time()))
+    with lsgb_mod.Batch(prec, lanes=3) as b:
+        b.set_mode(mode)
+        inst = []
+        for q, (n, live, bc) in enumerate(BATCH_CASES):
+            x = b.add(_params(lsgb_mod, n, bc))
+            _batch_instance(lsgb_mod, x, n, live, 0.1 * q)
+            inst.append(x)
+        for c in chunks:
+            b.advance(c)
         b.sync()
+        assert b.mode == mode
+        for x, (G, t), (n, live, bc) in zip(inst, alone, BATCH_CASES):
+            assert np.array_equal(x.get_G(layout="compact"), G), (n, live)
+            if live:
+                assert x.time() == t
