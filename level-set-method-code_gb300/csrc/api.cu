@@ -1050,6 +1050,20 @@ extern "C" int lsgb_solver_get_tile(const lsgb_solver* s, int* tile) {
     return LSGB_OK;
 }
 
+extern "C" int lsgb_debug_f64_div_check(long long n, unsigned long long seed, long long* mismatches) {
+    if (n < 0 || !mismatches) return fail(LSGB_ERR_INVALID, "n < 0 or mismatches is NULL");
+    unsigned long long* d = nullptr;
+    LSGB_CUDA(cudaMalloc((void**)&d, sizeof(unsigned long long)));
+    cudaError_t e = cudaMemset(d, 0, sizeof(unsigned long long));
+    if (e == cudaSuccess) e = launch_div_check(n, seed, d, nullptr);
+    unsigned long long h = 0;
+    if (e == cudaSuccess) e = cudaMemcpy(&h, d, sizeof(h), cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e != cudaSuccess) return fail(LSGB_ERR_CUDA, "division check: %s", cudaGetErrorString(e));
+    *mismatches = (long long)h;
+    return LSGB_OK;
+}
+
 extern "C" int lsgb_solver_debug_drop_copies(lsgb_solver* s, int on) {
     LSGB_TRY(solver_ok(s));
     s->drop_copies = on ? 1 : 0;

@@ -201,6 +201,10 @@ template <typename T>
 cudaError_t launch_nonfinite(const Geo& g, const Lay& lay, const T* G, double* partials,
                              double* out, cudaStream_t st);
 
+// Self-test of the FP64 kernels' division by a known reciprocal against IEEE
+// division: bad (device) counts mismatching results over n seeded pairs.
+cudaError_t launch_div_check(long long n, uint64_t seed, unsigned long long* bad, cudaStream_t st);
+
 // Synthetic fields: writes FP64 compact arrays G, u, v, w (w ignored in 2D).
 cudaError_t launch_synth(const Geo& g, const lsgb_synth& d, double dx, double dy, double dz,
                          double* G, double* u, double* v, double* w, cudaStream_t st);

@@ -1,15 +1,16 @@
 // f64_kernels.cu -- FP64 kernels that reproduce the reference's arithmetic.
 //
 // Compiled with --fmad=false: every a*b+c below stays a rounded multiply and a
-// rounded add, divisions and sqrt are IEEE round-to-nearest, and expressions
-// keep the reference's evaluation order.  With the same inputs the results
+// rounded add, divisions and sqrt are IEEE round-to-nearest (a quotient by a
+// known or shared divisor is formed as a corrected product, div_rn, which
+// gives the same bits), and expressions keep the reference's evaluation order.  With the same inputs the results
 // are bit-identical to the reference CPU solver
 // (Local_code/level-set_MPI_3D/include/{weno5,rk3,reinitialization}.h and the
 // 2D twins), which tests/test_gpu_parity.py checks.
 //
 // Kernel shapes: one thread per interior cell (blocks of 32 x 4 x 2 in 3D,
 // 32 x 8 in 2D).  FP64 on GB300 runs far below the HBM roof (the step is
-// bound by the FP64 pipe, ~60 divisions per cell and stage), so these kernels
+// bound by the FP64 pipe), so these kernels
 // favour exactness and simple addressing; the throughput path is the FP32 form
 // in f32_kernels.cu.
 #include "common.cuh"
@@ -18,6 +19,35 @@ namespace lsgb {
 namespace {
 
 constexpr double WENO_EPS = 1.0e-6;  // weno5.h:22
+constexpr double RCP6 = 1.0 / 6.0;   // RN(1/6)
+
+// a / b rounded to nearest, from y = RN(1/b): Markstein's theorem (P.
+// Markstein, "Computation of elementary functions on the IBM RISC System/6000
+// processor", IBM J. Res. Dev. 34(1), 1990; Muller et al., Handbook of
+// Floating-Point Arithmetic, the section on division with an FMA): when q
+// is within one ulp of a / b and y within half an ulp of 1 / b, the
+// remainder r = a - b q is exact with one FMA and RN(q + r y) = RN(a / b).
+// q = RN(a y) is within one ulp of a / b.  The theorem needs a, b, the
+// quotient and the remainder clear of underflow and overflow, so a outside
+// [2^-500, 2^501) (zeros too, whose sign the FMAs would not keep), or b
+// outside it, takes IEEE division.  Every result is
+// the IEEE quotient bit for bit, at one multiply and two FMAs where a
+// division costs a reciprocal approximation and several FMAs.
+__device__ __noinline__ double div_ieee(double a, double b) { return a / b; }
+
+// Biased exponent of x in [523, 1523], i.e. 2^-500 <= |x| < 2^501, tested on
+// the integer pipe (the FP64 pipe is the kernels' bottleneck).
+__device__ __forceinline__ bool mid_range(double x) {
+    const unsigned e = ((unsigned)__double2hiint(x) >> 20) & 0x7ffu;
+    return e - 523u <= 1000u;
+}
+
+__device__ __forceinline__ double div_rn(double a, double b, double y) {
+    if (!(mid_range(a) && mid_range(b))) return div_ieee(a, b);
+    const double q = __dmul_rn(a, y);
+    const double r = __fma_rn(-q, b, a);
+    return __fma_rn(r, y, q);
+}
 
 // Smoothness indicator of the triple (a, b, c) = (v[k], v[k+1], v[k+2]),
 // computeSmoothnessIndicators, weno5.h:28-37 (non-standard second term).
@@ -35,10 +65,11 @@ __device__ __forceinline__ double weno_left(double v0, double v1, double v2, dou
     double a1 = 0.6 / ((WENO_EPS + b1) * (WENO_EPS + b1));
     double a2 = 0.3 / ((WENO_EPS + b2) * (WENO_EPS + b2));
     double s = a0 + a1 + a2;
-    double w0 = a0 / s, w1 = a1 / s, w2 = a2 / s;
-    double p0 = (2.0 * v0 - 7.0 * v1 + 11.0 * v2) / 6.0;
-    double p1 = (-v1 + 5.0 * v2 + 2.0 * v3) / 6.0;
-    double p2 = (2.0 * v2 + 5.0 * v3 - v4) / 6.0;
+    const double rs = 1.0 / s;
+    double w0 = div_rn(a0, s, rs), w1 = div_rn(a1, s, rs), w2 = div_rn(a2, s, rs);
+    double p0 = div_rn(2.0 * v0 - 7.0 * v1 + 11.0 * v2, 6.0, RCP6);
+    double p1 = div_rn(-v1 + 5.0 * v2 + 2.0 * v3, 6.0, RCP6);
+    double p2 = div_rn(2.0 * v2 + 5.0 * v3 - v4, 6.0, RCP6);
     return w0 * p0 + w1 * p1 + w2 * p2;
 }
 
@@ -52,16 +83,17 @@ __device__ __forceinline__ double weno_right(double v0, double v1, double v2, do
     double a1 = 0.6 / ((WENO_EPS + b1) * (WENO_EPS + b1));
     double a2 = 0.1 / ((WENO_EPS + b2) * (WENO_EPS + b2));
     double s = a0 + a1 + a2;
-    double w0 = a0 / s, w1 = a1 / s, w2 = a2 / s;
-    double p0 = (11.0 * v2 - 7.0 * v3 + 2.0 * v4) / 6.0;
-    double p1 = (2.0 * v1 + 5.0 * v2 - v3) / 6.0;
-    double p2 = (-v0 + 5.0 * v1 + 2.0 * v2) / 6.0;
+    const double rs = 1.0 / s;
+    double w0 = div_rn(a0, s, rs), w1 = div_rn(a1, s, rs), w2 = div_rn(a2, s, rs);
+    double p0 = div_rn(11.0 * v2 - 7.0 * v3 + 2.0 * v4, 6.0, RCP6);
+    double p1 = div_rn(2.0 * v1 + 5.0 * v2 - v3, 6.0, RCP6);
+    double p2 = div_rn(-v0 + 5.0 * v1 + 2.0 * v2, 6.0, RCP6);
     return w0 * p0 + w1 * p1 + w2 * p2;
 }
 
 // weno5_dx_3d / _dy_3d / _dz_3d (weno5.h:90-196): s[0..6] = G[i-3..i+3]
-// along the axis; branch on vel >= 0 (weno5.h:99).
-__device__ __forceinline__ double weno_deriv(const double* s, double vel, double h) {
+// along the axis; branch on vel >= 0 (weno5.h:99).  rh = RN(1 / h).
+__device__ __forceinline__ double weno_deriv(const double* s, double vel, double h, double rh) {
     double gl, gr;
     if (vel >= 0.0) {
         gl = weno_left(s[0], s[1], s[2], s[3], s[4]);
@@ -70,7 +102,7 @@ __device__ __forceinline__ double weno_deriv(const double* s, double vel, double
         gl = weno_right(s[1], s[2], s[3], s[4], s[5]);
         gr = weno_right(s[2], s[3], s[4], s[5], s[6]);
     }
-    return (gr - gl) / h;
+    return div_rn(gr - gl, h, rh);
 }
 
 // Stencil reader: element offset of interior coordinate (i + d) etc.  In the
@@ -128,29 +160,31 @@ __global__ void __launch_bounds__(256) stage_f64_kernel(StageArgs a) {
     }
 
     double s_l = a.sl ? ((const double*)a.sl)[a.lay.off + id] : a.s_l;
-    double gx = 0.0, gy = 0.0, gz = 0.0, gm = 1.0;
+    double gx = 0.0, gy = 0.0, gz = 0.0, gm = 1.0, rgm = 1.0;
+    const double hx2 = 2.0 * a.dx, hy2 = 2.0 * a.dy, hz2 = 2.0 * a.dz;
     if (s_l > a.eps) {
-        gx = (sx[4] - sx[2]) / (2.0 * a.dx);
-        gy = (sy[4] - sy[2]) / (2.0 * a.dy);
+        gx = div_rn(sx[4] - sx[2], hx2, 1.0 / hx2);
+        gy = div_rn(sy[4] - sy[2], hy2, 1.0 / hy2);
         if (DIM == 3) {
-            gz = (sz[4] - sz[2]) / (2.0 * a.dz);
+            gz = div_rn(sz[4] - sz[2], hz2, 1.0 / hz2);
             gm = sqrt(gx * gx + gy * gy + gz * gz + a.eps);
         } else {
             gm = sqrt(gx * gx + gy * gy + a.eps);
         }
+        rgm = 1.0 / gm;
     }
-    const double ue = ((const double*)a.u)[a.lay.off + id] - s_l * gx / gm;
-    const double ve = ((const double*)a.v)[a.lay.off + id] - s_l * gy / gm;
+    const double ue = ((const double*)a.u)[a.lay.off + id] - div_rn(s_l * gx, gm, rgm);
+    const double ve = ((const double*)a.v)[a.lay.off + id] - div_rn(s_l * gy, gm, rgm);
     double rhs;
     if (DIM == 3) {
-        const double we = ((const double*)a.w)[a.lay.off + id] - s_l * gz / gm;
-        double dgx = weno_deriv(sx, ue, a.dx);
-        double dgy = weno_deriv(sy, ve, a.dy);
-        double dgz = weno_deriv(sz, we, a.dz);
+        const double we = ((const double*)a.w)[a.lay.off + id] - div_rn(s_l * gz, gm, rgm);
+        double dgx = weno_deriv(sx, ue, a.dx, 1.0 / a.dx);
+        double dgy = weno_deriv(sy, ve, a.dy, 1.0 / a.dy);
+        double dgz = weno_deriv(sz, we, a.dz, 1.0 / a.dz);
         rhs = -(ue * dgx + ve * dgy + we * dgz);
     } else {
-        double dgx = weno_deriv(sx, ue, a.dx);
-        double dgy = weno_deriv(sy, ve, a.dy);
+        double dgx = weno_deriv(sx, ue, a.dx, 1.0 / a.dx);
+        double dgy = weno_deriv(sy, ve, a.dy, 1.0 / a.dy);
         rhs = -(ue * dgx + ve * dgy);
     }
 
@@ -183,7 +217,8 @@ __global__ void __launch_bounds__(256) stage_f64_kernel(StageArgs a) {
 //   2. the list of (face, bias) reconstructions the tile's cells use, one
 //      entry per needed value, compacted by a block scan;
 //   3. the list evaluated densely, one entry per thread at a time (about 3.5
-//      reconstructions per cell in place of 6, each with 9 IEEE divisions);
+//      reconstructions per cell in place of 6, each with 4 IEEE divisions
+//      and 6 quotients by a known reciprocal);
 //   4. per cell, (face right - face left) / h per axis, the rhs and the stage
 //      combination, as stage_f64_kernel.
 // Every face value is the reference's weno5_left / weno5_right of the same
@@ -205,16 +240,18 @@ __device__ __forceinline__ double weno_either(double v0, double v1, double v2, d
     const double a1 = 0.6 / ((WENO_EPS + b1) * (WENO_EPS + b1));
     const double a2 = d2 / ((WENO_EPS + b2) * (WENO_EPS + b2));
     const double s = a0 + a1 + a2;
-    const double w0 = a0 / s, w1 = a1 / s, w2 = a2 / s;
+    // the three weights share one reciprocal; every quotient is still IEEE's
+    const double rs = 1.0 / s;
+    const double w0 = div_rn(a0, s, rs), w1 = div_rn(a1, s, rs), w2 = div_rn(a2, s, rs);
     // left (2 v0 - 7 v1) + 11 v2; right (11 v2 - 7 v3) + 2 v4
     const double t0 = 2.0 * m0, t2 = 11.0 * m2;
-    const double p0 = ((right ? t2 : t0) - 7.0 * m1 + (right ? t0 : t2)) / 6.0;
+    const double p0 = div_rn((right ? t2 : t0) - 7.0 * m1 + (right ? t0 : t2), 6.0, RCP6);
     // left (-v1 + 5 v2) + 2 v3; right (2 v1 + 5 v2) - v3
     const double n1 = -m1, u3 = 2.0 * m3;
-    const double p1 = ((right ? u3 : n1) + 5.0 * m2 + (right ? n1 : u3)) / 6.0;
+    const double p1 = div_rn((right ? u3 : n1) + 5.0 * m2 + (right ? n1 : u3), 6.0, RCP6);
     // left (2 v2 + 5 v3) - v4; right (-v0 + 5 v1) + 2 v2
     const double u2 = 2.0 * m2, n4 = -m4;
-    const double p2 = ((right ? n4 : u2) + 5.0 * m3 + (right ? u2 : n4)) / 6.0;
+    const double p2 = div_rn((right ? n4 : u2) + 5.0 * m3 + (right ? u2 : n4), 6.0, RCP6);
     return w0 * p0 + w1 * p1 + w2 * p2;
 }
 
@@ -303,7 +340,10 @@ __global__ void __launch_bounds__(256) stage_f64_faces(StageArgs a) {
     }
     __syncthreads();
 
-    // ---- 1. u_eff and the upwind bias of the own cells (stage_f64_kernel's operations)
+    // ---- 1. u_eff and the upwind bias of the own cells (stage_f64_kernel's
+    // operations; quotients by a known reciprocal, div_rn)
+    const double h2[3] = {2.0 * a.dx, 2.0 * a.dy, 2.0 * a.dz};
+    const double rh2[3] = {1.0 / h2[0], 1.0 / h2[1], 1.0 / h2[2]};
     double ue[T::CPT], ve[T::CPT], we[T::CPT];
 #pragma unroll
     for (int q = 0; q < T::CPT; ++q) {
@@ -316,20 +356,21 @@ __global__ void __launch_bounds__(256) stage_f64_faces(StageArgs a) {
             const double* P = Gs + ((cz + (DIM == 3 ? 3 : 0)) * T::SY + cy + 3) * T::SX + cx + 3;
             const long long id = (long long)k * sz + (long long)j * sy + i;
             const double s_l = a.sl ? ((const double*)a.sl)[a.lay.off + id] : a.s_l;
-            double gx = 0.0, gy = 0.0, gz = 0.0, gm = 1.0;
+            double gx = 0.0, gy = 0.0, gz = 0.0, gm = 1.0, rgm = 1.0;
             if (s_l > a.eps) {
-                gx = (P[1] - P[-1]) / (2.0 * a.dx);
-                gy = (P[T::SX] - P[-T::SX]) / (2.0 * a.dy);
+                gx = div_rn(P[1] - P[-1], h2[0], rh2[0]);
+                gy = div_rn(P[T::SX] - P[-T::SX], h2[1], rh2[1]);
                 if (DIM == 3) {
-                    gz = (P[T::SX * T::SY] - P[-T::SX * T::SY]) / (2.0 * a.dz);
+                    gz = div_rn(P[T::SX * T::SY] - P[-T::SX * T::SY], h2[2], rh2[2]);
                     gm = sqrt(gx * gx + gy * gy + gz * gz + a.eps);
                 } else {
                     gm = sqrt(gx * gx + gy * gy + a.eps);
                 }
+                rgm = 1.0 / gm;
             }
-            ue[q] = ((const double*)a.u)[a.lay.off + id] - s_l * gx / gm;
-            ve[q] = ((const double*)a.v)[a.lay.off + id] - s_l * gy / gm;
-            if (DIM == 3) we[q] = ((const double*)a.w)[a.lay.off + id] - s_l * gz / gm;
+            ue[q] = ((const double*)a.u)[a.lay.off + id] - div_rn(s_l * gx, gm, rgm);
+            ve[q] = ((const double*)a.v)[a.lay.off + id] - div_rn(s_l * gy, gm, rgm);
+            if (DIM == 3) we[q] = ((const double*)a.w)[a.lay.off + id] - div_rn(s_l * gz, gm, rgm);
             b = (ue[q] >= 0.0 ? 0 : 1) | (ve[q] >= 0.0 ? 0 : 2) | (DIM == 3 && !(we[q] >= 0.0) ? 4 : 0);
         }
         bias[c] = b;
@@ -386,6 +427,7 @@ __global__ void __launch_bounds__(256) stage_f64_faces(StageArgs a) {
 
     // ---- 4. derivatives, rhs, stage combination
     const double dt = a.dt;
+    const double rh[3] = {1.0 / a.dx, 1.0 / a.dy, 1.0 / a.dz};
 #pragma unroll
     for (int q = 0; q < T::CPT; ++q) {
         const int c = t + q * T::NT;
@@ -395,7 +437,8 @@ __global__ void __launch_bounds__(256) stage_f64_faces(StageArgs a) {
         const int b = bias[c];
         auto deriv = [&](int ax, double h) {
             const int r = (b >> ax) & 1;
-            return (fv[2 * face_id<DIM>(ax, cx, cy, cz, 1) + r] - fv[2 * face_id<DIM>(ax, cx, cy, cz, 0) + r]) / h;
+            return div_rn(fv[2 * face_id<DIM>(ax, cx, cy, cz, 1) + r] - fv[2 * face_id<DIM>(ax, cx, cy, cz, 0) + r], h,
+                          rh[ax]);
         };
         double rhs;
         if (DIM == 3) {
@@ -420,6 +463,57 @@ __global__ void __launch_bounds__(256) stage_f64_faces(StageArgs a) {
         }
         ((double*)a.Gout)[a.lay.off + id] = out;
     }
+}
+
+// div_rn against IEEE division on n seeded pairs: divisors are the solver's
+// (6, 2^-9, 1/192, 1/200, 2/512, sums of WENO weights) and random ones in
+// [2^-40, 2^40]; dividends are random in [2^-80, 2^80] with either sign,
+// exact multiples of the divisor, and values next to a rounding midpoint of
+// the quotient.  Mismatching bit patterns are counted.
+__device__ __forceinline__ uint64_t mix64(uint64_t x) {
+    x += 0x9e3779b97f4a7c15ULL;
+    x = (x ^ (x >> 30)) * 0xbf58476d1ce4e5b9ULL;
+    x = (x ^ (x >> 27)) * 0x94d049bb133111ebULL;
+    return x ^ (x >> 31);
+}
+
+__device__ __forceinline__ double rand_in(uint64_t bits, int emin, int emax) {
+    const int e = emin + (int)((bits >> 52) % (uint64_t)(emax - emin + 1));
+    return ldexp(1.0 + (double)(bits & ((1ULL << 52) - 1)) * 0x1p-52, e);
+}
+
+__global__ void div_check_kernel(long long n, uint64_t seed, unsigned long long* bad) {
+    unsigned long long local = 0;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
+        const uint64_t h0 = mix64(seed ^ (uint64_t)e), h1 = mix64(h0), h2 = mix64(h1), h3 = mix64(h2);
+        double b;
+        switch (h0 % 8) {
+            case 0: b = 6.0; break;
+            case 1: b = 0x1p-9; break;
+            case 2: b = 1.0 / 192.0; break;
+            case 3: b = 1.0 / 200.0; break;
+            case 4: b = 2.0 / 512.0; break;
+            case 5: b = rand_in(h1, -3, 40); break;  // WENO weight sums
+            default: b = rand_in(h1, -40, 40); break;
+        }
+        double a;
+        switch (h2 % 4) {
+            case 0: a = (double)(long long)(h3 % 2000001) - 1000000.0; a = a * b; break;  // exact quotients
+            case 1: {  // next to a rounding midpoint: RN(b (q + ulp(q) / 2)) moved by -8 .. 7 ulps
+                const double q = rand_in(h3, -20, 20);
+                a = __fma_rn(b, q, b * ldexp(0.5, ilogb(q) - 52));
+                a += (double)((int)(h3 >> 60) - 8) * ldexp(1.0, ilogb(a) - 52);
+                break;
+            }
+            default: a = rand_in(h3, -80, 80); break;
+        }
+        if (h2 & 16) a = -a;
+        if (h2 & 32) b = -b;
+        const double y = 1.0 / b;
+        const double r = div_rn(a, b, y), ref = a / b;
+        if (__double_as_longlong(r) != __double_as_longlong(ref)) local++;
+    }
+    if (local) atomicAdd(bad, local);
 }
 
 // Godunov first-order |grad phi|^2 term of one axis by sign(S),
@@ -476,9 +570,10 @@ __global__ void __launch_bounds__(256) reinit_f64_kernel(Geo g, Lay lay, const d
 
     const double S = ph0 / sqrt(ph0 * ph0 + dx * dx);  // smoothSign, reinitialization.h:24
     const bool pos = S > 0.0;
-    double gsq = godunov_axis((phi - pn[0]) / dx, (pn[1] - phi) / dx, pos)
-               + godunov_axis((phi - pn[2]) / dy, (pn[3] - phi) / dy, pos);
-    if (DIM == 3) gsq = gsq + godunov_axis((phi - pn[4]) / dz, (pn[5] - phi) / dz, pos);
+    const double rdx = 1.0 / dx, rdy = 1.0 / dy, rdz = 1.0 / dz;
+    double gsq = godunov_axis(div_rn(phi - pn[0], dx, rdx), div_rn(pn[1] - phi, dx, rdx), pos)
+               + godunov_axis(div_rn(phi - pn[2], dy, rdy), div_rn(pn[3] - phi, dy, rdy), pos);
+    if (DIM == 3) gsq = gsq + godunov_axis(div_rn(phi - pn[4], dz, rdz), div_rn(pn[5] - phi, dz, rdz), pos);
     const double term = -S * (sqrt(gsq) - 1.0);
 
     int flag;
@@ -503,7 +598,7 @@ __global__ void __launch_bounds__(256) reinit_f64_kernel(Geo g, Lay lay, const d
 #pragma unroll
             for (int q = 0; q < 2 * DIM; ++q)
                 if ((flag >> q) & 1) sum += pn[q];
-            forcing = beta * (rt * sum - phi) / dx;
+            forcing = div_rn(beta * (rt * sum - phi), dx, rdx);
         }
     }
     phinew_[lay.off + id] = phi + dtau * (term + forcing);
@@ -653,6 +748,12 @@ bool use_faces(const StageArgs& a) {
 }
 
 }  // namespace
+
+cudaError_t launch_div_check(long long n, uint64_t seed, unsigned long long* bad, cudaStream_t st) {
+    div_check_kernel<<<152 * 8, 256, 0, st>>>(n, seed, bad);
+    count_launches(1);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_stage_f64(const StageArgs& a, cudaStream_t st) {
     const bool gh = a.lay.ghosted != 0;
