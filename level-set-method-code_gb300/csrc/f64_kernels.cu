@@ -49,11 +49,26 @@ __device__ __forceinline__ double div_rn(double a, double b, double y) {
     return __fma_rn(r, y, q);
 }
 
+// x * 2^K, exact: for a normal x whose product stays normal, the exponent
+// field moves by K on the integer pipe; zeros, subnormals and the edges of
+// the range take the FP64 multiply (whose result is the same product).
+__device__ __noinline__ double mul_ieee(double x, double c) { return x * c; }
+
+template <int K>
+__device__ __forceinline__ double mul_pow2(double x) {
+    const int hi = __double2hiint(x);
+    const unsigned e = ((unsigned)hi >> 20) & 0x7ffu;
+    constexpr unsigned lo = K < 0 ? 1u - K : 1u, hi_e = K > 0 ? 0x7feu - K : 0x7feu;
+    if (e - lo > hi_e - lo) return mul_ieee(x, K > 0 ? (double)(1 << K) : 1.0 / (double)(1 << -K));
+    return __hiloint2double(hi + K * (1 << 20), __double2loint(x));
+}
+
 // Smoothness indicator of the triple (a, b, c) = (v[k], v[k+1], v[k+2]),
 // computeSmoothnessIndicators, weno5.h:28-37 (non-standard second term).
 __device__ __forceinline__ double sm_beta(double a, double b, double c) {
-    double d2 = c - 2.0 * b + a;
-    return (13.0 / 12.0) * d2 * d2 + 0.25 * (c - a) * (c - a);
+    double d2 = c - mul_pow2<1>(b) + a;
+    const double h = c - a;
+    return (13.0 / 12.0) * d2 * d2 + mul_pow2<-2>(h) * h;
 }
 
 // weno5_left, weno5.h:39-58: value at i+1/2 from G[i-2..i+2].
@@ -67,9 +82,9 @@ __device__ __forceinline__ double weno_left(double v0, double v1, double v2, dou
     double s = a0 + a1 + a2;
     const double rs = 1.0 / s;
     double w0 = div_rn(a0, s, rs), w1 = div_rn(a1, s, rs), w2 = div_rn(a2, s, rs);
-    double p0 = div_rn(2.0 * v0 - 7.0 * v1 + 11.0 * v2, 6.0, RCP6);
-    double p1 = div_rn(-v1 + 5.0 * v2 + 2.0 * v3, 6.0, RCP6);
-    double p2 = div_rn(2.0 * v2 + 5.0 * v3 - v4, 6.0, RCP6);
+    double p0 = div_rn(mul_pow2<1>(v0) - 7.0 * v1 + 11.0 * v2, 6.0, RCP6);
+    double p1 = div_rn(-v1 + 5.0 * v2 + mul_pow2<1>(v3), 6.0, RCP6);
+    double p2 = div_rn(mul_pow2<1>(v2) + 5.0 * v3 - v4, 6.0, RCP6);
     return w0 * p0 + w1 * p1 + w2 * p2;
 }
 
@@ -85,9 +100,9 @@ __device__ __forceinline__ double weno_right(double v0, double v1, double v2, do
     double s = a0 + a1 + a2;
     const double rs = 1.0 / s;
     double w0 = div_rn(a0, s, rs), w1 = div_rn(a1, s, rs), w2 = div_rn(a2, s, rs);
-    double p0 = div_rn(11.0 * v2 - 7.0 * v3 + 2.0 * v4, 6.0, RCP6);
-    double p1 = div_rn(2.0 * v1 + 5.0 * v2 - v3, 6.0, RCP6);
-    double p2 = div_rn(-v0 + 5.0 * v1 + 2.0 * v2, 6.0, RCP6);
+    double p0 = div_rn(11.0 * v2 - 7.0 * v3 + mul_pow2<1>(v4), 6.0, RCP6);
+    double p1 = div_rn(mul_pow2<1>(v1) + 5.0 * v2 - v3, 6.0, RCP6);
+    double p2 = div_rn(-v0 + 5.0 * v1 + mul_pow2<1>(v2), 6.0, RCP6);
     return w0 * p0 + w1 * p1 + w2 * p2;
 }
 
@@ -244,13 +259,13 @@ __device__ __forceinline__ double weno_either(double v0, double v1, double v2, d
     const double rs = 1.0 / s;
     const double w0 = div_rn(a0, s, rs), w1 = div_rn(a1, s, rs), w2 = div_rn(a2, s, rs);
     // left (2 v0 - 7 v1) + 11 v2; right (11 v2 - 7 v3) + 2 v4
-    const double t0 = 2.0 * m0, t2 = 11.0 * m2;
+    const double t0 = mul_pow2<1>(m0), t2 = 11.0 * m2;
     const double p0 = div_rn((right ? t2 : t0) - 7.0 * m1 + (right ? t0 : t2), 6.0, RCP6);
     // left (-v1 + 5 v2) + 2 v3; right (2 v1 + 5 v2) - v3
-    const double n1 = -m1, u3 = 2.0 * m3;
+    const double n1 = -m1, u3 = mul_pow2<1>(m3);
     const double p1 = div_rn((right ? u3 : n1) + 5.0 * m2 + (right ? n1 : u3), 6.0, RCP6);
     // left (2 v2 + 5 v3) - v4; right (-v0 + 5 v1) + 2 v2
-    const double u2 = 2.0 * m2, n4 = -m4;
+    const double u2 = mul_pow2<1>(m2), n4 = -m4;
     const double p2 = div_rn((right ? n4 : u2) + 5.0 * m3 + (right ? u2 : n4), 6.0, RCP6);
     return w0 * p0 + w1 * p1 + w2 * p2;
 }
