@@ -9,8 +9,10 @@
 // Every kernel takes n_inst instances stored back to back (stride = one
 // ghosted array); blockIdx.z is the instance.  The frequency-sweep workload
 // of the reference (one process per forcing frequency) runs as one launch
-// per stage over all frequencies.
+// per stage over all frequencies.  Quotients by a known or shared divisor
+// and products by powers of two use fp64_exact.cuh (the same bits).
 #include "common.cuh"
+#include "fp64_exact.cuh"
 
 namespace lsgb {
 namespace {
@@ -25,9 +27,9 @@ struct S2 {
 
 // beta, sample/weno5_rk3.cpp:11-14; std::pow(x, 2) is the rounded product x*x
 __device__ __forceinline__ double s_beta(double f0, double f1, double f2) {
-    const double a = f0 - 2.0 * f1 + f2;
-    const double b = f0 - 4.0 * f1 + 3.0 * f2;
-    return (13.0 / 12.0) * (a * a) + (1.0 / 4.0) * (b * b);
+    const double a = f0 - mul_pow2<1>(f1) + f2;
+    const double b = f0 - mul_pow2<2>(f1) + 3.0 * f2;
+    return (13.0 / 12.0) * (a * a) + mul_pow2<-2>(b * b);
 }
 
 // weno5_left, sample/weno5_rk3.cpp:17-32.  weno5_right (:35-50) called with
@@ -43,10 +45,11 @@ __device__ __forceinline__ double s_face(double v0, double v1, double v2, double
     const double a1 = 0.6 / ((SEPS + b1) * (SEPS + b1));
     const double a2 = 0.3 / ((SEPS + b2) * (SEPS + b2));
     const double sum = a0 + a1 + a2;
-    const double w0 = a0 / sum, w1 = a1 / sum, w2 = a2 / sum;
-    return w0 * (2.0 * v0 - 7.0 * v1 + 11.0 * v2) / 6.0
-         + w1 * (-v1 + 5.0 * v2 + 2.0 * v3) / 6.0
-         + w2 * (2.0 * v2 + 5.0 * v3 - v4) / 6.0;
+    const double rsum = 1.0 / sum;
+    const double w0 = div_rn(a0, sum, rsum), w1 = div_rn(a1, sum, rsum), w2 = div_rn(a2, sum, rsum);
+    return div_rn(w0 * (mul_pow2<1>(v0) - 7.0 * v1 + 11.0 * v2), 6.0, RCP6)
+         + div_rn(w1 * (-v1 + 5.0 * v2 + mul_pow2<1>(v3)), 6.0, RCP6)
+         + div_rn(w2 * (mul_pow2<1>(v2) + 5.0 * v3 - v4), 6.0, RCP6);
 }
 
 __device__ __forceinline__ double smax(double a, double b) { return (a < b) ? b : a; }  // std::max
@@ -56,8 +59,8 @@ __device__ __forceinline__ double smin(double a, double b) { return (b < a) ? b 
 // derivatives of the cell.
 __device__ __forceinline__ double llf_rhs(double Gdxm, double Gdxp, double Gdym, double Gdyp, double uu, double vv,
                                           double S_L) {
-    const double Gdx_mean = 0.5 * (Gdxm + Gdxp);
-    const double Gdy_mean = 0.5 * (Gdym + Gdyp);
+    const double Gdx_mean = mul_pow2<-1>(Gdxm + Gdxp);
+    const double Gdy_mean = mul_pow2<-1>(Gdym + Gdyp);
     const double transport = uu * Gdx_mean + vv * Gdy_mean;
     const double propagation = S_L * sqrt(Gdx_mean * Gdx_mean + Gdy_mean * Gdy_mean);
     const double nm = sqrt(Gdxm * Gdxm + Gdym * Gdym + 1e-14);
@@ -69,8 +72,8 @@ __device__ __forceinline__ double llf_rhs(double Gdxm, double Gdxp, double Gdym,
     const double s_yp = vv - S_L * Gdyp / np;
     const double alpha_y = smax(fabs(s_ym), fabs(s_yp));
     const double alpha = smax(alpha_x, alpha_y);
-    const double diss_x = alpha * (Gdxp - Gdxm) * 0.5;
-    const double diss_y = alpha * (Gdyp - Gdym) * 0.5;
+    const double diss_x = mul_pow2<-1>(alpha * (Gdxp - Gdxm));
+    const double diss_y = mul_pow2<-1>(alpha * (Gdyp - Gdym));
     const double H = transport - propagation - (diss_x + diss_y);
     return -H;
 }
@@ -149,8 +152,9 @@ __global__ void __launch_bounds__(256) sample_stage_kernel(S2 s, const double* _
     const int x = threadIdx.x, y = threadIdx.y;
     const int i = i0 + x, j = j0 + y;
     if (i > s.nx + 2 || j > s.ny + 2) return;
-    const double Gdxm = (fx[y][x + 1] - fx[y][x]) / dx, Gdxp = (fx[y][x + 2] - fx[y][x + 1]) / dx;
-    const double Gdym = (fy[y + 1][x] - fy[y][x]) / dy, Gdyp = (fy[y + 2][x] - fy[y + 1][x]) / dy;
+    const double rdx = 1.0 / dx, rdy = 1.0 / dy;
+    const double Gdxm = div_rn(fx[y][x + 1] - fx[y][x], dx, rdx), Gdxp = div_rn(fx[y][x + 2] - fx[y][x + 1], dx, rdx);
+    const double Gdym = div_rn(fy[y + 1][x] - fy[y][x], dy, rdy), Gdyp = div_rn(fy[y + 2][x] - fy[y + 1][x], dy, rdy);
     const long long c = s.at(j, i);
     double uu, vv;
     vel_at(V, s, q, c, uu, vv);
@@ -159,7 +163,7 @@ __global__ void __launch_bounds__(256) sample_stage_kernel(S2 s, const double* _
     double o;
     if (STAGE == 0) o = r;
     else if (STAGE == 1) o = Gn[e] + dt * r;
-    else if (STAGE == 2) o = 0.75 * Gn[e] + 0.25 * (tile[y + 3][x + 3] + dt * r);
+    else if (STAGE == 2) o = 0.75 * Gn[e] + mul_pow2<-2>(tile[y + 3][x + 3] + dt * r);
     else o = (1.0 / 3.0) * Gn[e] + (2.0 / 3.0) * (tile[y + 3][x + 3] + dt * r);
     out[e] = o;
 }
@@ -264,10 +268,11 @@ __global__ void __launch_bounds__(256) sample_reinit_kernel(S2 s, const double* 
     const double g0 = init[s.at(j, i)];
     const double sg = g0 / sqrt(g0 * g0 + dx * dx);
     const double c = phi[s.at(j, i)];
-    const double dGdx_pos = (c - phi[s.at(j, i - 1)]) / dx;
-    const double dGdx_neg = (phi[s.at(j, i + 1)] - c) / dx;
-    const double dGdy_pos = (c - phi[s.at(j - 1, i)]) / dy;
-    const double dGdy_neg = (phi[s.at(j + 1, i)] - c) / dy;
+    const double rdx = 1.0 / dx, rdy = 1.0 / dy;
+    const double dGdx_pos = div_rn(c - phi[s.at(j, i - 1)], dx, rdx);
+    const double dGdx_neg = div_rn(phi[s.at(j, i + 1)] - c, dx, rdx);
+    const double dGdy_pos = div_rn(c - phi[s.at(j - 1, i)], dy, rdy);
+    const double dGdy_neg = div_rn(phi[s.at(j + 1, i)] - c, dy, rdy);
     double grad;
     if (sg > 0.0) {
         const double px = smax(smax(dGdx_pos, 0.0), -smin(dGdx_neg, 0.0));
