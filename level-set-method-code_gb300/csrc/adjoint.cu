@@ -147,7 +147,9 @@ __device__ __forceinline__ void axis_grad(const R* s, R vel, R inv_h, R& D, R* d
 // -3, -2, -1, +1, +2, +3 (axis a uses planes 1 + 6a .. 6 + 6a).
 __device__ __forceinline__ int stage_off(int q) { return q < 3 ? q - 3 : q - 2; }
 
-template <typename T, int DIM>
+// ZG: some axis is zero-gradient (neighbours through map_axis); otherwise
+// every axis wraps.
+template <typename T, int DIM, bool ZG>
 __global__ void __launch_bounds__(256) stage_adj_coef_kernel(AdjStageArgs a) {
     const Geo g = a.g;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -158,13 +160,13 @@ __global__ void __launch_bounds__(256) stage_adj_coef_kernel(AdjStageArgs a) {
     const long long sy = g.nx, sz = (long long)g.nx * g.ny;
     const long long P = DIM == 3 ? (long long)(a.zn + 6) * sz : g.cells();
     T* cp = (T*)a.coef + (i + sy * j + sz * kl);  // plane 0 of this cell; plane o at cp + o P
-    if (DIM == 3 && g.bcz != LSGB_BC_PERIODIC && (ku < 0 || ku >= g.nz)) {
+    if (ZG && DIM == 3 && g.bcz != LSGB_BC_PERIODIC && (ku < 0 || ku >= g.nz)) {
         // a plane outside a clamped z axis: no cell, no coefficients
 #pragma unroll
         for (int o = 0; o < ADJ_PLANES; ++o) cp[o * P] = (T)0;
         return;
     }
-    const int k = DIM == 3 ? zmap(ku, g.nz, g.bcz) : 0;
+    const int k = DIM == 3 ? (ZG ? zmap(ku, g.nz, g.bcz) : wrapn(ku, g.nz)) : 0;
     const bool own = DIM == 2 || (ku >= a.z0 && ku < a.z0 + a.zn);  // parameter gradients
     typedef T R;
     const T* __restrict__ G = (const T*)a.Gin;
@@ -173,9 +175,14 @@ __global__ void __launch_bounds__(256) stage_adj_coef_kernel(AdjStageArgs a) {
     R s[3][7];
 #pragma unroll
     for (int d = -3; d <= 3; ++d) {
-        s[0][d + 3] = Gc[map_axis(i + d, g.nx, g.bcx) - i];
-        s[1][d + 3] = Gc[(long long)(map_axis(j + d, g.ny, g.bcy) - j) * sy];
-        if (DIM == 3) s[2][d + 3] = Gc[(long long)(map_axis(k + d, g.nz, g.bcz) - k) * sz];
+        const int xi = ZG ? map_axis(i + d, g.nx, g.bcx) : wrap(i + d, g.nx);
+        const int yj = ZG ? map_axis(j + d, g.ny, g.bcy) : wrap(j + d, g.ny);
+        s[0][d + 3] = Gc[xi - i];
+        s[1][d + 3] = Gc[(long long)(yj - j) * sy];
+        if (DIM == 3) {
+            const int zk = ZG ? map_axis(k + d, g.nz, g.bcz) : wrap(k + d, g.nz);
+            s[2][d + 3] = Gc[(long long)(zk - k) * sz];
+        }
     }
     const R S = a.sl ? ((const T*)a.sl)[c] : (R)a.s_l;
     const R ih[3] = {(R)(1.0 / a.dx), (R)(1.0 / a.dy), (R)(1.0 / a.dz)};
@@ -299,6 +306,7 @@ __device__ __forceinline__ void axis_grad2(const float2* s, float2 vel, float in
     D = (Y - X) * sg;
 }
 
+template <bool ZG>
 __global__ void __launch_bounds__(256, 2) stage_adj_coef_pair_kernel(AdjStageArgs a) {
     const Geo g = a.g;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -308,9 +316,9 @@ __global__ void __launch_bounds__(256, 2) stage_adj_coef_pair_kernel(AdjStageArg
     if (i >= g.nx || j >= g.ny || kl >= nl) return;
     const bool two = kl + 1 < nl;  // an odd slab leaves the last thread one plane
     const int ku = a.z0 - 3 + kl;
-    const int k = zmap(ku, g.nz, g.bcz), k1 = zmap(ku + 1, g.nz, g.bcz);
+    const int k = ZG ? zmap(ku, g.nz, g.bcz) : wrapn(ku, g.nz), k1 = ZG ? zmap(ku + 1, g.nz, g.bcz) : wrapn(ku + 1, g.nz);
     // planes outside a clamped z axis hold no cell: their coefficients are 0
-    const bool zper = g.bcz == LSGB_BC_PERIODIC;
+    const bool zper = !ZG || g.bcz == LSGB_BC_PERIODIC;
     const bool in0 = zper || (ku >= 0 && ku < g.nz), in1 = zper || (ku + 1 >= 0 && ku + 1 < g.nz);
     const bool own0 = ku >= a.z0 && ku < a.z0 + a.zn;
     const bool own1 = two && ku + 1 >= a.z0 && ku + 1 < a.z0 + a.zn;
@@ -322,14 +330,14 @@ __global__ void __launch_bounds__(256, 2) stage_adj_coef_pair_kernel(AdjStageArg
     float2 s[3][7];
 #pragma unroll
     for (int d = -3; d <= 3; ++d) {
-        const int xo = map_axis(i + d, g.nx, g.bcx) - i;
-        const long long yo = (long long)(map_axis(j + d, g.ny, g.bcy) - j) * sy;
+        const int xo = (ZG ? map_axis(i + d, g.nx, g.bcx) : wrap(i + d, g.nx)) - i;
+        const long long yo = (long long)((ZG ? map_axis(j + d, g.ny, g.bcy) : wrap(j + d, g.ny)) - j) * sy;
         s[0][d + 3] = make_float2(Gc[xo], G[c1 + xo]);
         s[1][d + 3] = make_float2(Gc[yo], G[c1 + yo]);
     }
     float zq[8];
 #pragma unroll
-    for (int d = 0; d < 8; ++d) zq[d] = G[i + sy * j + sz * zmap(ku - 3 + d, g.nz, g.bcz)];
+    for (int d = 0; d < 8; ++d) zq[d] = G[i + sy * j + sz * (ZG ? zmap(ku - 3 + d, g.nz, g.bcz) : wrapn(ku - 3 + d, g.nz))];
 #pragma unroll
     for (int d = 0; d < 7; ++d) s[2][d] = make_float2(zq[d], zq[d + 1]);
     const float* sl = (const float*)a.sl;
@@ -357,7 +365,8 @@ __global__ void __launch_bounds__(256, 2) stage_adj_coef_pair_kernel(AdjStageArg
 #pragma unroll
     for (int ax = 0; ax < 3; ++ax) dg = fma2(D[ax], gr[ax], dg);
     const float* lam = (const float*)a.lam;
-    const float2 wc = f2((float)a.cdt) * make_float2(in0 ? lam[c] : 0.0f, in1 ? lam[c1] : 0.0f);
+    const float2 wc = ZG ? f2((float)a.cdt) * make_float2(in0 ? lam[c] : 0.0f, in1 ? lam[c1] : 0.0f)
+                         : f2((float)a.cdt) * make_float2(lam[c], lam[c1]);
     const long long P = (long long)nl * sz;  // plane stride of the slab buffer
     float* cp0 = (float*)a.coef + (i + sy * j + sz * kl);
     float* cp1 = cp0 + sz;
@@ -489,7 +498,7 @@ __device__ __forceinline__ void nb_off(int q, int& ox, int& oy, int& oz) {
     else oz = sgn;
 }
 
-template <typename T, int DIM>
+template <typename T, int DIM, bool ZG>
 __global__ void __launch_bounds__(256) reinit_adj_coef_kernel(AdjReinitArgs a) {
     const Geo g = a.g;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -506,8 +515,11 @@ __global__ void __launch_bounds__(256) reinit_adj_coef_kernel(AdjReinitArgs a) {
     for (int q = 0; q < 2 * DIM; ++q) {
         int ox, oy, oz;
         nb_off(q, ox, oy, oz);
-        nb[q] = ix.at(map_axis(i + ox, g.nx, g.bcx), map_axis(j + oy, g.ny, g.bcy),
-                      DIM == 3 ? map_axis(k + oz, g.nz, g.bcz) : 0);
+        if (ZG)
+            nb[q] = ix.at(map_axis(i + ox, g.nx, g.bcx), map_axis(j + oy, g.ny, g.bcy),
+                          DIM == 3 ? map_axis(k + oz, g.nz, g.bcz) : 0);
+        else
+            nb[q] = ix.at(wrap(i + ox, g.nx), wrap(j + oy, g.ny), wrap(k + oz, g.nz));
     }
     const R phi = phin[c], ph0 = phi0[c];
     R pn[6], p0[6];
@@ -703,16 +715,19 @@ cudaError_t launch_stage_adj(const AdjStageArgs& c, const AdjGatherArgs& gth, cu
         if (std::is_same<T, float>::value) {
             // plane pairs: half the threads along z
             const dim3 gp(gr.x, gr.y, (unsigned)((nl + 2 * b.z - 1) / (2 * b.z)));
-            stage_adj_coef_pair_kernel<<<gp, b, 0, st>>>(c);
+            if (zero_gradient(c.g)) stage_adj_coef_pair_kernel<true><<<gp, b, 0, st>>>(c);
+            else stage_adj_coef_pair_kernel<false><<<gp, b, 0, st>>>(c);
         } else {
             const dim3 gc(gr.x, gr.y, (unsigned)((nl + b.z - 1) / b.z));
-            stage_adj_coef_kernel<T, 3><<<gc, b, 0, st>>>(c);
+            if (zero_gradient(c.g)) stage_adj_coef_kernel<T, 3, true><<<gc, b, 0, st>>>(c);
+            else stage_adj_coef_kernel<T, 3, false><<<gc, b, 0, st>>>(c);
         }
         const dim3 gg(gr.x, gr.y, (unsigned)((gth.zn + b.z - 1) / b.z));
         if (zero_gradient(c.g)) stage_adj_gather_kernel<T, 3, true><<<gg, b, 0, st>>>(gth);
         else stage_adj_gather_kernel<T, 3, false><<<gg, b, 0, st>>>(gth);
     } else {
-        stage_adj_coef_kernel<T, 2><<<gr, b, 0, st>>>(c);
+        if (zero_gradient(c.g)) stage_adj_coef_kernel<T, 2, true><<<gr, b, 0, st>>>(c);
+        else stage_adj_coef_kernel<T, 2, false><<<gr, b, 0, st>>>(c);
         if (zero_gradient(c.g)) stage_adj_gather_kernel<T, 2, true><<<gr, b, 0, st>>>(gth);
         else stage_adj_gather_kernel<T, 2, false><<<gr, b, 0, st>>>(gth);
     }
@@ -724,11 +739,13 @@ template <typename T>
 cudaError_t launch_reinit_adj(const AdjReinitArgs& c, const AdjReinitGatherArgs& gth, cudaStream_t st) {
     const dim3 b = cell_block(c.g), gr = cell_grid(c.g, b);
     if (c.g.dim == 3) {
-        reinit_adj_coef_kernel<T, 3><<<gr, b, 0, st>>>(c);
+        if (zero_gradient(c.g)) reinit_adj_coef_kernel<T, 3, true><<<gr, b, 0, st>>>(c);
+        else reinit_adj_coef_kernel<T, 3, false><<<gr, b, 0, st>>>(c);
         if (zero_gradient(c.g)) reinit_adj_gather_kernel<T, 3, true><<<gr, b, 0, st>>>(gth);
         else reinit_adj_gather_kernel<T, 3, false><<<gr, b, 0, st>>>(gth);
     } else {
-        reinit_adj_coef_kernel<T, 2><<<gr, b, 0, st>>>(c);
+        if (zero_gradient(c.g)) reinit_adj_coef_kernel<T, 2, true><<<gr, b, 0, st>>>(c);
+        else reinit_adj_coef_kernel<T, 2, false><<<gr, b, 0, st>>>(c);
         if (zero_gradient(c.g)) reinit_adj_gather_kernel<T, 2, true><<<gr, b, 0, st>>>(gth);
         else reinit_adj_gather_kernel<T, 2, false><<<gr, b, 0, st>>>(gth);
     }
