@@ -307,7 +307,7 @@ __device__ __forceinline__ void axis_grad2(const float2* s, float2 vel, float in
 }
 
 template <bool ZG>
-__global__ void __launch_bounds__(256, 2) stage_adj_coef_pair_kernel(AdjStageArgs a) {
+__global__ void __launch_bounds__(256, 3) stage_adj_coef_pair_kernel(AdjStageArgs a) {
     const Geo g = a.g;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
@@ -327,19 +327,20 @@ __global__ void __launch_bounds__(256, 2) stage_adj_coef_pair_kernel(AdjStageArg
     const long long c = i + sy * j + sz * k;
     const long long c1 = i + sy * j + sz * k1;
     const float* Gc = G + c;
-    float2 s[3][7];
-#pragma unroll
-    for (int d = -3; d <= 3; ++d) {
-        const int xo = (ZG ? map_axis(i + d, g.nx, g.bcx) : wrap(i + d, g.nx)) - i;
-        const long long yo = (long long)((ZG ? map_axis(j + d, g.ny, g.bcy) : wrap(j + d, g.ny)) - j) * sy;
-        s[0][d + 3] = make_float2(Gc[xo], G[c1 + xo]);
-        s[1][d + 3] = make_float2(Gc[yo], G[c1 + yo]);
-    }
+    // The central differences first (two samples per axis); then one axis
+    // at a time: its 7-point line, the WENO derivative and the four
+    // coefficients that do not involve the other axes, stored at once.  The
+    // +-1 offsets wait for dg (every axis's D), so only their partial values
+    // stay live.
     float zq[8];
 #pragma unroll
     for (int d = 0; d < 8; ++d) zq[d] = G[i + sy * j + sz * (ZG ? zmap(ku - 3 + d, g.nz, g.bcz) : wrapn(ku - 3 + d, g.nz))];
-#pragma unroll
-    for (int d = 0; d < 7; ++d) s[2][d] = make_float2(zq[d], zq[d + 1]);
+    auto sample = [&](int ax, int d) -> float2 {  // G at offset d (-3 .. 3) along axis ax, planes k and k+1
+        if (ax == 2) return make_float2(zq[d + 3], zq[d + 4]);
+        const long long o = ax == 0 ? (long long)((ZG ? map_axis(i + d, g.nx, g.bcx) : wrap(i + d, g.nx)) - i)
+                                    : (long long)((ZG ? map_axis(j + d, g.ny, g.bcy) : wrap(j + d, g.ny)) - j) * sy;
+        return make_float2(Gc[o], G[c1 + o]);
+    };
     const float* sl = (const float*)a.sl;
     const float2 S = sl ? make_float2(sl[c], sl[c1]) : f2((float)a.s_l);
     const float ih[3] = {(float)(1.0 / a.dx), (float)(1.0 / a.dy), (float)(1.0 / a.dz)};
@@ -348,46 +349,56 @@ __global__ void __launch_bounds__(256, 2) stage_adj_coef_pair_kernel(AdjStageArg
     float2 gr[3], q = f2(0.0f);
 #pragma unroll
     for (int ax = 0; ax < 3; ++ax) {
-        gr[ax] = (s[ax][4] - s[ax][2]) * f2(0.5f * ih[ax]);
+        gr[ax] = (sample(ax, 1) - sample(ax, -1)) * f2(0.5f * ih[ax]);
         gr[ax] = make_float2(actx ? gr[ax].x : 0.0f, acty ? gr[ax].y : 0.0f);
         q = fma2(gr[ax], gr[ax], q);
     }
     const float2 gm = make_float2(actx ? sqrtf(q.x + epsf) : 1.0f, acty ? sqrtf(q.y + epsf) : 1.0f);
     const float2 igm = rcp2(gm);
     const float* vel[3] = {(const float*)a.u, (const float*)a.v, (const float*)a.w};
-    float2 ue[3], D[3], dD[3][7];
-#pragma unroll
-    for (int ax = 0; ax < 3; ++ax) {
-        ue[ax] = make_float2(vel[ax][c], vel[ax][c1]) - S * gr[ax] * igm;
-        axis_grad2(s[ax], ue[ax], ih[ax], D[ax], dD[ax]);
-    }
-    float2 dg = f2(0.0f);
-#pragma unroll
-    for (int ax = 0; ax < 3; ++ax) dg = fma2(D[ax], gr[ax], dg);
     const float* lam = (const float*)a.lam;
     const float2 wc = ZG ? f2((float)a.cdt) * make_float2(in0 ? lam[c] : 0.0f, in1 ? lam[c1] : 0.0f)
                          : f2((float)a.cdt) * make_float2(lam[c], lam[c1]);
     const long long P = (long long)nl * sz;  // plane stride of the slab buffer
     float* cp0 = (float*)a.coef + (i + sy * j + sz * kl);
     float* cp1 = cp0 + sz;
-    float2 centre = f2(0.0f);
+    float2 D[3], vm1[3], vp1[3], centre = f2(0.0f);
+#pragma unroll
+    for (int ax = 0; ax < 3; ++ax) {
+        float2 line[7], dD[7];
+#pragma unroll
+        for (int d = -3; d <= 3; ++d) line[d + 3] = sample(ax, d);
+        const float2 ue = make_float2(vel[ax][c], vel[ax][c1]) - S * gr[ax] * igm;
+        axis_grad2(line, ue, ih[ax], D[ax], dD);
+        centre = centre - ue * dD[3];
+#pragma unroll
+        for (int q6 = 0; q6 < 6; ++q6) {
+            const int sidx = stage_off(q6) + 3;
+            const float2 v = -(ue * dD[sidx]);
+            if (sidx == 2) { vm1[ax] = v; continue; }
+            if (sidx == 4) { vp1[ax] = v; continue; }
+            const float2 o = wc * v;
+            const long long po = (long long)(1 + 6 * ax + q6) * P;
+            cp0[po] = o.x;
+            if (two) cp1[po] = o.y;
+        }
+    }
+    float2 dg = f2(0.0f);
+#pragma unroll
+    for (int ax = 0; ax < 3; ++ax) dg = fma2(D[ax], gr[ax], dg);
     const float2 igm2 = igm * igm;
 #pragma unroll
     for (int ax = 0; ax < 3; ++ax) {
         float2 dRg = S * igm * (D[ax] - dg * gr[ax] * igm2);
         dRg = make_float2(actx ? dRg.x : 0.0f, acty ? dRg.y : 0.0f);
         const float2 half = dRg * f2(0.5f * ih[ax]);
-        centre = centre - ue[ax] * dD[ax][3];
-#pragma unroll
-        for (int q6 = 0; q6 < 6; ++q6) {
-            const int sidx = stage_off(q6) + 3;
-            float2 v = -(ue[ax] * dD[ax][sidx]);
-            if (sidx == 4) v = v + half;
-            if (sidx == 2) v = v - half;
-            const float2 o = wc * v;
-            const long long po = (long long)(1 + 6 * ax + q6) * P;
-            cp0[po] = o.x;
-            if (two) cp1[po] = o.y;
+        const float2 om = wc * (vm1[ax] - half), op = wc * (vp1[ax] + half);
+        const long long pm = (long long)(1 + 6 * ax + 2) * P, pp = (long long)(1 + 6 * ax + 3) * P;
+        cp0[pm] = om.x;
+        cp0[pp] = op.x;
+        if (two) {
+            cp1[pm] = om.y;
+            cp1[pp] = op.y;
         }
     }
     const float2 oc = wc * centre;
