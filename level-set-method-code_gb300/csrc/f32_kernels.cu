@@ -51,24 +51,31 @@ __device__ __forceinline__ float reinit_cell_f32(float phi, float ph0, const flo
     // floats is never rounded to zero in FP64, so comparing signs in FP32
     // decides it identically; only flagged cells go on to FP64 arithmetic.
     flag = 0;
+    forced = false;
     // no crossing where phi0 and all its neighbours lie strictly on one side
-    // (most cells): the per-neighbour tests below would all fail there
+    // (most cells): the per-neighbour tests below would all fail there.  The
+    // tests run only in warps with a lane near the interface.
     float lo = p0[0], hi = p0[0];
 #pragma unroll
     for (int q = 1; q < 2 * DIM; ++q) {
         lo = fminf(lo, p0[q]);
         hi = fmaxf(hi, p0[q]);
     }
-    if (!((ph0 > 0.0f && lo > 0.0f) || (ph0 < 0.0f && hi < 0.0f))) {
+    const bool near = !((ph0 > 0.0f && lo > 0.0f) || (ph0 < 0.0f && hi < 0.0f));
+    // (the lanes of a warp that reach this point together: cells past the
+    // grid's edge never do)
+    if (__any_sync(__activemask(), near)) {
+        if (near) {
+#pragma unroll
+            for (int q = 0; q < 2 * DIM; ++q)
+                if ((ph0 < 0.0f && p0[q] > 0.0f) || (ph0 > 0.0f && p0[q] < 0.0f)) flag |= 1 << q;
+        }
+        bool stable = flag != 0 && (phi > 0.0f) == (ph0 > 0.0f);
 #pragma unroll
         for (int q = 0; q < 2 * DIM; ++q)
-            if ((ph0 < 0.0f && p0[q] > 0.0f) || (ph0 > 0.0f && p0[q] < 0.0f)) flag |= 1 << q;
+            if ((flag >> q) & 1) stable = stable && ((pn[q] > 0.0f) == (p0[q] > 0.0f));
+        forced = stable;
     }
-    bool stable = flag != 0 && (phi > 0.0f) == (ph0 > 0.0f);
-#pragma unroll
-    for (int q = 0; q < 2 * DIM; ++q)
-        if ((flag >> q) & 1) stable = stable && ((pn[q] > 0.0f) == (p0[q] > 0.0f));
-    forced = stable;
     return term;
 }
 
@@ -121,11 +128,15 @@ __device__ __forceinline__ void reinit_f32_body(const Geo& g, const float* __res
     __shared__ float q_phi[RT], q_ph0[RT], q_term[RT];
     __shared__ float q_pn[2 * DIM][RT], q_p0[2 * DIM][RT];
     const int t = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+    // (ordered before the queue's first use by the barrier of __syncthreads_or)
     if (t == 0) nq = 0;
-    __syncthreads();
+    bool forced = false;
     int i = bx * blockDim.x + threadIdx.x;
     int j = by * blockDim.y + threadIdx.y;
     int k = DIM == 3 ? bz * blockDim.z + threadIdx.z : 0;
+    IDX c_id = 0;  // a forced cell's values until it is queued
+    int c_flag = 0;
+    float c_phi = 0.0f, c_ph0 = 0.0f, c_term = 0.0f, c_pn[6], c_p0[6];
     if (i < g.nx && j < g.ny && k < g.nz) {
         const IDX sy = g.nx;
         const IDX sz = (IDX)g.nx * g.ny;
@@ -149,22 +160,35 @@ __device__ __forceinline__ void reinit_f32_body(const Geo& g, const float* __res
         }
         if (phi0_copy) phi0_copy[id] = ph0;
         int flag;
-        bool forced;
         const float term = reinit_cell_f32<DIM>(phi, ph0, pn, p0, inv_dx, inv_dy, inv_dz, dx2, flag, forced);
         if (forced) {
-            const int e = atomicAdd(&nq, 1);
-            q_id[e] = id;
-            q_flag[e] = flag;
-            q_phi[e] = phi;
-            q_ph0[e] = ph0;
-            q_term[e] = term;
+            c_id = id;
+            c_flag = flag;
+            c_phi = phi;
+            c_ph0 = ph0;
+            c_term = term;
 #pragma unroll
             for (int q = 0; q < 2 * DIM; ++q) {
-                q_pn[q][e] = pn[q];
-                q_p0[q][e] = p0[q];
+                c_pn[q] = pn[q];
+                c_p0[q] = p0[q];
             }
         } else {
             phinew[id] = fmaf(dtau_f, term, phi);
+        }
+    }
+    // most blocks hold no forced cell: one barrier and done
+    if (!__syncthreads_or(forced)) return;
+    if (forced) {
+        const int e = atomicAdd(&nq, 1);
+        q_id[e] = c_id;
+        q_flag[e] = c_flag;
+        q_phi[e] = c_phi;
+        q_ph0[e] = c_ph0;
+        q_term[e] = c_term;
+#pragma unroll
+        for (int q = 0; q < 2 * DIM; ++q) {
+            q_pn[q][e] = c_pn[q];
+            q_p0[q][e] = c_p0[q];
         }
     }
     __syncthreads();
