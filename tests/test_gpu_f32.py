@@ -4,7 +4,7 @@ The FP32 path is not bit-exact by design.  Tolerances (stated here, checked
 on every run):
   * smooth synthetic fields (the benchmark construction): after 20 RK3 steps
     with HCR-2 every 5, L_inf(G32 - G64) <= 2e-6 and, within 3 cells of the
-    front, <= 1e-3 * dx (the north-star bound on the zero-level-set error);
+    front, <= 1e-3 * dx (the FP32 form's bound on the zero-level-set error);
   * rough random fields (every upwind branch, non-smooth WENO weights):
     L_inf <= 5e-5 after 4 steps -- a kernel-logic check on ragged tiles,
     z-chunk seams, the 3-cell minimum and zero-gradient axes (y and z, or all
