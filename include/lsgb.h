@@ -271,10 +271,12 @@ LSGB_API int lsgb_solver_get_tile(const lsgb_solver* s, int* tile);
  * the flag.  The context stays usable.  Off by default; no other effect. */
 LSGB_API int lsgb_solver_debug_drop_copies(lsgb_solver* s, int on);
 /* Test hook: the FP64 kernels divide by a known divisor b as a one-multiply,
- * two-FMA correction of a * RN(1/b) (Markstein's theorem).  Compares that
- * quotient with IEEE division on n seeded pairs (the solver's divisors and
- * random ones; random, exact-multiple and near-midpoint dividends) and
- * writes the number of results that differ in any bit.  Synchronises. */
+ * two-FMA correction of a * RN(1/b) (Markstein's theorem), and multiply by
+ * 2, 4, 1/2, 1/4 as exponent shifts.  Compares those with IEEE division and
+ * multiplication on n seeded cases (the solver's divisors and random ones;
+ * random, exact-multiple and near-midpoint dividends; multiplicands over the
+ * whole exponent range) and writes the number of results that differ in any
+ * bit.  Synchronises. */
 LSGB_API int lsgb_debug_f64_div_check(long long n, unsigned long long seed, long long* mismatches);
 
 /* Autotuner: times one stage launch per candidate tile shape (reps launches

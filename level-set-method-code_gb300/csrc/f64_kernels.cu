@@ -442,7 +442,9 @@ __global__ void __launch_bounds__(256) stage_f64_faces(StageArgs a) {
 // (6, 2^-9, 1/192, 1/200, 2/512, sums of WENO weights) and random ones in
 // [2^-40, 2^40]; dividends are random in [2^-80, 2^80] with either sign,
 // exact multiples of the divisor, and values next to a rounding midpoint of
-// the quotient.  Mismatching bit patterns are counted.
+// the quotient.  Also mul_pow2 against the FP64 multiply on values over the
+// whole exponent range (subnormals, zeros and the largest finite values
+// included).  Mismatching bit patterns are counted.
 __device__ __forceinline__ uint64_t mix64(uint64_t x) {
     x += 0x9e3779b97f4a7c15ULL;
     x = (x ^ (x >> 30)) * 0xbf58476d1ce4e5b9ULL;
@@ -485,6 +487,17 @@ __global__ void div_check_kernel(long long n, uint64_t seed, unsigned long long*
         const double y = 1.0 / b;
         const double r = div_rn(a, b, y), ref = a / b;
         if (__double_as_longlong(r) != __double_as_longlong(ref)) local++;
+        // any bit pattern but NaN: every exponent field, either sign
+        const uint64_t h4 = mix64(h3);
+        double x = __longlong_as_double((long long)(h4 & 0xfffffffffffffULL) |
+                                        (long long)((h4 >> 52) % 0x7ffULL) << 52);
+        if (h4 & (1ULL << 63)) x = -x;
+        if ((h2 >> 8) % 64 == 0) x = (h4 & 1) ? 0.0 : -0.0;
+        const double pr[4] = {mul_pow2<1>(x), mul_pow2<2>(x), mul_pow2<-1>(x), mul_pow2<-2>(x)};
+        const double pe[4] = {x * 2.0, x * 4.0, x * 0.5, x * 0.25};
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+            if (__double_as_longlong(pr[q]) != __double_as_longlong(pe[q])) local++;
     }
     if (local) atomicAdd(bad, local);
 }
