@@ -1677,7 +1677,7 @@ extern "C" int lsgb_batch_advance(lsgb_batch* b, int n_steps) {
     if (b->inst.empty() || n_steps == 0) return LSGB_OK;
     for (lsgb_solver* s : b->inst)
         if (!s->have_G || !s->have_vel) return fail(LSGB_ERR_STATE, "an instance has no fields");
-    int step, interval, reinit_on;
+    int step = 0, interval = 1, reinit_on = 0;
     LSGB_TRY(batch_uniform(b, &step, &interval, &reinit_on));
     // live instances read each step's vortex time from a device table
     struct LiveScope {
