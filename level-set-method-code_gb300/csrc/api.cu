@@ -1348,8 +1348,10 @@ int batch_launch_steps_grouped(lsgb_batch* b, int n_steps) {
         const lsgb_solver* f = b->inst[0];
         if (f->p.enable_reinit && f->step > 0 && f->step % f->p.reinit_interval == 0 && b->iters > 0) {
             for (int it = 0; it < b->iters; ++it) {
-                LSGB_CUDA(launch_reinit_f32_group(d + b->offr3, (const int*)(d + b->oor3), n3, b->rblk3, 3, it, s3));
-                LSGB_CUDA(launch_reinit_f32_group(d + b->offr2, (const int*)(d + b->oor2), n2, b->rblk2, 2, it, s2));
+                LSGB_CUDA(launch_reinit_f32_group(d + b->offr3, (const int*)(d + b->oor3), n3, b->rblk3, 3, it,
+                                                  b->iters, s3));
+                LSGB_CUDA(launch_reinit_f32_group(d + b->offr2, (const int*)(d + b->oor2), n2, b->rblk2, 2, it,
+                                                  b->iters, s2));
             }
             LSGB_CUDA(launch_copy_back_group(d + b->offr3, (const int*)(d + b->ooc3), n3, b->cblk3, b->iters, s3));
             LSGB_CUDA(launch_copy_back_group(d + b->offr2, (const int*)(d + b->ooc2), n2, b->cblk2, b->iters, s2));

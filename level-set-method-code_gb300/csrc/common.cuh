@@ -150,16 +150,18 @@ size_t group2_desc_bytes();
 void group2_fill(const GroupInst* in, int n, int shape, void* host_table, std::vector<int>& owner);
 cudaError_t launch_stage2d_f32_group(const void* table, const int* owner, int n, long long tiles, int stage,
                                      int shape, cudaStream_t st);
-// HCR-2 pseudo-step `iter` (0-based) of every instance: iter 0 reads G, iter
-// m > 0 reads the buffer pseudo-step m-1 wrote (A for even m-1, B for odd);
-// iteration m writes A (m even) or B (m odd).  The copy back sets G to the
-// last pseudo-step's buffer (iters pseudo-steps ran).  All instances of one
-// table have the same dimensionality.
+// HCR-2 pseudo-step `iter` (0-based) of `iters` for every instance.  Even
+// count: the handle's copy-free roles (iter 0: G -> A keeping phi0 in B; odd
+// iters A -> G, even ones G -> A, phi0 from B), the result in G and no copy
+// back.  Odd count: iter 0 reads G, iter m > 0 reads the buffer pseudo-step
+// m-1 wrote (A for even m-1, B for odd), iteration m writes A (m even) or B
+// (m odd), and the copy back sets G to the last one's buffer.  All instances
+// of one table have the same dimensionality.
 size_t groupr_desc_bytes();
 void groupr_fill(const GroupInst* in, int n, void* host_table, std::vector<int>& owner,
                  std::vector<int>& copy_owner);
 cudaError_t launch_reinit_f32_group(const void* table, const int* owner, int n, long long blocks, int dim, int iter,
-                                    cudaStream_t st);
+                                    int iters, cudaStream_t st);
 cudaError_t launch_copy_back_group(const void* table, const int* copy_owner, int n, long long copy_blocks, int iters,
                                    cudaStream_t st);
 

@@ -115,8 +115,9 @@ constexpr int RT = 256;  // threads of a pseudo-step block
 // holds one forced cell no longer runs the FP64 sequence for all 32 lanes.
 // SAME: phin and phi0 are one array (the first pseudo-step of a
 // reinitialisation), so each neighbour is loaded once.  phi0_copy (nullable)
-// receives phi0 at every cell.
-template <int DIM, typename IDX, bool SAME = false>
+// receives phi0 at every cell.  LOOP: the caller runs the body for several
+// cell blocks in turn, so the forced-cell queue ends with a barrier.
+template <int DIM, typename IDX, bool SAME = false, bool LOOP = false>
 __device__ __forceinline__ void reinit_f32_body(const Geo& g, const float* __restrict__ phin,
                                                 const float* __restrict__ phi0, float* __restrict__ phinew,
                                                 float inv_dx, float inv_dy, float inv_dz, float dx2, float dtau_f,
@@ -201,6 +202,7 @@ __device__ __forceinline__ void reinit_f32_body(const Geo& g, const float* __res
         }
         phinew[q_id[e]] = reinit_forced_f64<DIM>(q_phi[e], q_ph0[e], q_term[e], q_flag[e], pn, p0, dx, dtau, beta);
     }
+    if (LOOP) __syncthreads();  // the queue is free again for the next cell block
 }
 
 template <int DIM, typename IDX, bool SAME>
@@ -222,27 +224,53 @@ struct GroupR {
     float *G, *A, *B;
     float inv_dx, inv_dy, inv_dz, dx2, dtau_f;
     double dx, dtau, beta;
-    int gx, gy, blk0, cblk0;
+    int gx, gy, gz, blk0, cblk0;
 };
+
+// Cell blocks a grouped pseudo-step block works through, consecutive along
+// the last axis (z in 3D, y in 2D): one descriptor fetch for all of them.
+constexpr int RZL = 4;
 
 constexpr int CPB = 4096;  // floats per block of the copy back
 
-// Grouped HCR-2 pseudo-step `iter` of every instance (same dimensionality);
-// block b belongs to instance owner[b].
+// Grouped HCR-2 pseudo-step `iter` of `iters` for every instance (same
+// dimensionality); block b belongs to instance owner[b] and works through
+// RZL cell blocks along the last axis.  Buffer roles: with an even count
+// (copy_free) they are the handle's -- iteration 0 reads G as both fields,
+// writes A and keeps phi0 in B; odd iterations A -> G and even ones G -> A,
+// phi0 from B, so the result lands in G.  With an odd count phi0 stays in G,
+// the iterations ping-pong A / B and copy_back_group moves the result.
 template <int DIM, bool FIRST>
 __global__ void __launch_bounds__(RT) reinit_f32_group(const GroupR* __restrict__ ins, const int* __restrict__ owner,
-                                                       int iter) {
+                                                       int iter, int copy_free) {
     const GroupR* d = ins + owner[blockIdx.x];
     int l = (int)blockIdx.x - d->blk0;
     const int bx = l % d->gx;
     l /= d->gx;
-    const int by = l % d->gy;
-    const int bz = l / d->gy;
-    // iteration 0 (FIRST) reads G as both fields
-    float* out = iter & 1 ? d->B : d->A;
-    const float* in = FIRST ? d->G : ((iter - 1) & 1 ? d->B : d->A);
-    reinit_f32_body<DIM, int, FIRST>(d->g, in, d->G, out, d->inv_dx, d->inv_dy, d->inv_dz, d->dx2, d->dtau_f,
-                                     d->dx, d->dtau, d->beta, bx, by, bz);
+    const int last = DIM == 3 ? d->gz : d->gy;  // cell blocks along the last axis
+    const int by0 = DIM == 3 ? l % d->gy : l * RZL;
+    const int bz0 = DIM == 3 ? (l / d->gy) * RZL : 0;
+    const Geo g = d->g;
+    float* out;
+    const float* in;
+    const float* p0;
+    float* p0_copy = nullptr;
+    if (copy_free) {
+        out = iter & 1 ? d->G : d->A;
+        in = FIRST ? d->G : (iter & 1 ? d->A : d->G);
+        p0 = FIRST ? d->G : d->B;
+        if (FIRST) p0_copy = d->B;
+    } else {
+        out = iter & 1 ? d->B : d->A;
+        in = FIRST ? d->G : ((iter - 1) & 1 ? d->B : d->A);
+        p0 = d->G;
+    }
+    for (int q = 0; q < RZL; ++q) {
+        const int by = DIM == 3 ? by0 : by0 + q, bz = DIM == 3 ? bz0 + q : 0;
+        if ((DIM == 3 ? bz : by) >= last) break;  // the same for the whole block
+        reinit_f32_body<DIM, int, FIRST, true>(g, in, p0, out, d->inv_dx, d->inv_dy, d->inv_dz, d->dx2, d->dtau_f,
+                                               d->dx, d->dtau, d->beta, bx, by, bz, p0_copy);
+    }
 }
 
 // G <- the buffer the last of `iters` pseudo-steps wrote, every instance.
@@ -320,9 +348,13 @@ void groupr_fill(const GroupInst* in, int n, void* host_table, std::vector<int>&
         const dim3 b = cell_block(a.g), gr = cell_grid(a.g, b);
         e.gx = (int)gr.x;
         e.gy = (int)gr.y;
+        e.gz = (int)gr.z;
         e.blk0 = (int)blk;
         e.cblk0 = (int)cblk;
-        const long long nb = (long long)gr.x * gr.y * gr.z, nc = (a.g.cells() + CPB - 1) / CPB;
+        // blocks of RZL cell blocks along the last axis
+        const long long nb = a.g.dim == 3 ? (long long)gr.x * gr.y * ((gr.z + RZL - 1) / RZL)
+                                          : (long long)gr.x * ((gr.y + RZL - 1) / RZL);
+        const long long nc = (a.g.cells() + CPB - 1) / CPB;
         blk += nb;
         cblk += nc;
         owner.insert(owner.end(), (size_t)nb, q);
@@ -332,17 +364,18 @@ void groupr_fill(const GroupInst* in, int n, void* host_table, std::vector<int>&
 }
 
 cudaError_t launch_reinit_f32_group(const void* table, const int* owner, int n, long long blocks, int dim, int iter,
-                                    cudaStream_t st) {
+                                    int iters, cudaStream_t st) {
     if (n <= 0 || blocks <= 0) return cudaSuccess;
     if (blocks > 0x7fffffffLL) return cudaErrorInvalidValue;
     const GroupR* d = (const GroupR*)table;
     const unsigned nb = (unsigned)blocks;
+    const int cf = iters % 2 == 0;
     if (dim == 3) {
-        if (iter == 0) reinit_f32_group<3, true><<<nb, dim3(32, 4, 2), 0, st>>>(d, owner, iter);
-        else reinit_f32_group<3, false><<<nb, dim3(32, 4, 2), 0, st>>>(d, owner, iter);
+        if (iter == 0) reinit_f32_group<3, true><<<nb, dim3(32, 4, 2), 0, st>>>(d, owner, iter, cf);
+        else reinit_f32_group<3, false><<<nb, dim3(32, 4, 2), 0, st>>>(d, owner, iter, cf);
     } else {
-        if (iter == 0) reinit_f32_group<2, true><<<nb, dim3(32, 8, 1), 0, st>>>(d, owner, iter);
-        else reinit_f32_group<2, false><<<nb, dim3(32, 8, 1), 0, st>>>(d, owner, iter);
+        if (iter == 0) reinit_f32_group<2, true><<<nb, dim3(32, 8, 1), 0, st>>>(d, owner, iter, cf);
+        else reinit_f32_group<2, false><<<nb, dim3(32, 8, 1), 0, st>>>(d, owner, iter, cf);
     }
     count_launches(1);
     return cudaGetLastError();
@@ -350,7 +383,8 @@ cudaError_t launch_reinit_f32_group(const void* table, const int* owner, int n, 
 
 cudaError_t launch_copy_back_group(const void* table, const int* copy_owner, int n, long long copy_blocks, int iters,
                                    cudaStream_t st) {
-    if (n <= 0 || copy_blocks <= 0 || iters <= 0) return cudaSuccess;
+    // an even count leaves the result in G (reinit_f32_group's buffer roles)
+    if (n <= 0 || copy_blocks <= 0 || iters <= 0 || iters % 2 == 0) return cudaSuccess;
     if (copy_blocks > 0x7fffffffLL) return cudaErrorInvalidValue;
     copy_back_group<<<(unsigned)copy_blocks, 256, 0, st>>>((const GroupR*)table, copy_owner, iters);
     count_launches(1);

@@ -14,7 +14,7 @@ SIZES = [(2, (40, 40, 1)), (2, (67, 53, 1)), (2, (130, 96, 1)), (3, (20, 20, 20)
          (3, (33, 17, 40)), (3, (48, 40, 70)), (2, (64, 64, 1)), (3, (32, 32, 32))]
 
 
-def instance(lsgb, syn, dim, n, idx, precision):
+def instance(lsgb, syn, dim, n, idx, precision, iters=2):
     rng = np.random.default_rng(4000 + idx)
     if dim == 3:
         wl = syn.sphere_config(4, n[0], 8, float(rng.uniform(0.05, 0.3)), instance=idx,
@@ -29,18 +29,21 @@ def instance(lsgb, syn, dim, n, idx, precision):
     dt = syn.cfl_dt(wl, u, v, w, 0.5)
     nz = n[2] if dim == 3 else 1
     p = lsgb.params(dim, n[0], n[1], nz, dx=1 / n[0], dy=1 / n[1], dz=1 / nz if dim == 3 else 1 / n[0],
-                    s_l=wl.s_l, dt=dt, enable_reinit=True, reinit_interval=5, reinit_iterations=2)
+                    s_l=wl.s_l, dt=dt, enable_reinit=True, reinit_interval=5, reinit_iterations=iters)
     return p, (G, u, v, w)
 
 
-@pytest.mark.parametrize("precision,mode", [("f32", "grouped"), ("f32", "lanes"), ("f64", "lanes")])
-def test_batch_matches_single_runs(cuda, lsgb_mod, precision, mode):
-    """Grouped form: one launch per RK3 stage (and per pseudo-step, and the
-    copy back) for all 3D instances and one for all 2D ones, so a captured
-    period of 5 steps + HCR-2 (2 pseudo-steps) holds 5 x 6 + 2 x 2 + 2 = 36
-    kernels whatever the number of instances."""
+@pytest.mark.parametrize("precision,mode,iters", [("f32", "grouped", 2), ("f32", "grouped", 3), ("f32", "lanes", 2),
+                                                  ("f64", "lanes", 2)])
+def test_batch_matches_single_runs(cuda, lsgb_mod, precision, mode, iters):
+    """Grouped form: one launch per RK3 stage and per pseudo-step for all 3D
+    instances and one for all 2D ones, plus a copy back per dimensionality
+    when the pseudo-step count is odd (an even count ends in G), so a
+    captured period of 5 steps + HCR-2 holds 5 x 6 + 2 x 2 = 34 kernels with
+    2 pseudo-steps and 5 x 6 + 3 x 2 + 2 = 38 with 3, whatever the number of
+    instances."""
     from lsgb import synthetic as syn
-    cases = [instance(lsgb_mod, syn, d, n, i, precision) for i, (d, n) in enumerate(SIZES)]
+    cases = [instance(lsgb_mod, syn, d, n, i, precision, iters) for i, (d, n) in enumerate(SIZES)]
     steps = 12  # step 0 direct, a captured period, a replayed period, one direct step
     with lsgb_mod.Batch(precision, lanes=4) as b:
         b.set_mode(mode)
@@ -58,7 +61,7 @@ def test_batch_matches_single_runs(cuda, lsgb_mod, precision, mode):
         assert all(s.step == steps for s in b.instances)
     assert replays == 2 and kernels > 0
     if mode == "grouped":
-        assert kernels == 36
+        assert kernels == 5 * 6 + iters * 2 + (2 if iters % 2 else 0)
     for (p, f), g, tile in zip(cases, got, tiles):
         with lsgb_mod.Solver(p, precision) as s:
             s.set_fields(*f)
