@@ -182,14 +182,14 @@ __global__ void __launch_bounds__(256) stage_f64_kernel(StageArgs a) {
 // and cell i+1's left face are the same reconstruction of the same five
 // values when both cells are upwinded the same way, so the value is shared;
 // a face between cells of opposite upwind directions needs both biases.  A
-// CTA owns a tile of cells (3D 32 x 8 x 2, 2D 32 x 16; block 32 x 8, two
-// cells per thread) and works in four phases over the tile staged with its
+// CTA owns a tile of cells (3D 32 x 8 x 3, 2D 32 x 16; block 32 x 8, three
+// or two cells per thread) and works in four phases over the tile staged with its
 // 3-cell halo in shared memory:
 //   1. u_eff of every cell (the reference's operations), its upwind bias per
 //      axis into shared memory;
 //   2. the list of (face, bias) reconstructions the tile's cells use, one
 //      entry per needed value, compacted by a block scan;
-//   3. the list evaluated densely, one entry per thread at a time (about 3.5
+//   3. the list evaluated densely, one entry per thread at a time (about 3.4
 //      reconstructions per cell in place of 6, each with 4 IEEE divisions
 //      and 6 quotients by a known reciprocal);
 //   4. per cell, (face right - face left) / h per axis, the rhs and the stage
@@ -230,7 +230,7 @@ __device__ __forceinline__ double weno_either(double v0, double v1, double v2, d
 
 template <int DIM>
 struct FaceTile {
-    static constexpr int TX = 32, TY = DIM == 3 ? 8 : 16, TZ = DIM == 3 ? 2 : 1;
+    static constexpr int TX = 32, TY = DIM == 3 ? 8 : 16, TZ = DIM == 3 ? 3 : 1;
     static constexpr int NT = 256, CPT = TX * TY * TZ / NT;  // threads, cells per thread
     static constexpr int SX = TX + 6, SY = TY + 6, SZ = DIM == 3 ? TZ + 6 : 1;
     static constexpr int NFX = (TX + 1) * TY * TZ, NFY = TX * (TY + 1) * TZ;
