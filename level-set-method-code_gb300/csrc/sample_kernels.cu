@@ -78,11 +78,11 @@ __device__ __forceinline__ double llf_rhs(double Gdxm, double Gdxp, double Gdym,
     return -H;
 }
 
-// Stage tile: 32 x 8 interior cells.  The G tile with its 3-cell halo is
-// staged in shared memory; every face value F(i+1/2) the tile needs is
-// computed once (34 x 8 x-faces, 32 x 10 y-faces) and read by the two
-// cells that share it.
-constexpr int STX = 32, STY = 8;
+// Stage tile: 32 x 16 interior cells (one per thread).  The G tile with its
+// 3-cell halo is staged in shared memory; every face value F(i+1/2) the tile
+// needs is computed once (34 x 16 x-faces, 32 x 18 y-faces: 2.19 per cell)
+// and read by the two cells that share it.
+constexpr int STX = 32, STY = 16;
 constexpr int SW = STX + 6, SH = STY + 6;
 constexpr int NFXS = (STX + 2) * STY, NFYS = STX * (STY + 2);
 
@@ -113,7 +113,7 @@ __device__ __forceinline__ void vel_at(const Vel& V, const S2& s, int q, long lo
 //   STAGE 3: out = 1/3 Gn + 2/3 (Gin + dt L(Gin))  (out == Gn allowed)
 // STAGE 0: out = L(Gin), the drop-in compute_geqn_rhs.
 template <int STAGE>
-__global__ void __launch_bounds__(256) sample_stage_kernel(S2 s, const double* __restrict__ Gin_,
+__global__ void __launch_bounds__(STX * STY) sample_stage_kernel(S2 s, const double* __restrict__ Gin_,
                                                            const double* Gn, double* out, Vel V, double dx,
                                                            double dy, double dt, double S_L) {
     __shared__ double tile[SH][SW];
