@@ -647,35 +647,40 @@ def run_ours(args, dist: Dist):
         # copies): it varies by box and sets the end-to-end figure's copy time
         link = {}
         probe = torch.empty(shape, dtype=torch.float64, device="cuda")
+
+        def copy_rate(dst, src):
+            e = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+            e[0].record(stream)
+            dst.copy_(src, non_blocking=True)
+            e[1].record(stream)
+            e[1].synchronize()
+            return probe.numel() * 8 / (e[0].elapsed_time(e[1]) * 1e-3) / 1e9
+
         with torch.cuda.stream(stream):
             for name, dst, src in (("h2d_gbs", probe, host[0]), ("d2h_gbs", host[4], probe)):
-                rates = []
-                for _ in range(3):
-                    e = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
-                    e[0].record(stream)
-                    dst.copy_(src, non_blocking=True)
-                    e[1].record(stream)
-                    e[1].synchronize()
-                    rates.append(probe.numel() * 8 / (e[0].elapsed_time(e[1]) * 1e-3) / 1e9)
+                rates = [copy_rate(dst, src) for _ in range(3)]
                 link[name] = statistics.median(rates)
                 link[name + "_samples"] = rates
+            # every input array once (separate pinned allocations: G, u, v, w)
+            link["h2d_gbs_per_array"] = [copy_rate(probe, src) for src in host[:4]]
         del probe
         torch.cuda.synchronize()
         dist.barrier()
-        ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(args.e2e_steps + 1)]
         with torch.cuda.stream(stream):
             ev[0].record(stream)
-            for _ in range(args.e2e_steps):
+            for q in range(args.e2e_steps):
                 s32.run_host(host[0].numpy(), host[1].numpy(), host[2].numpy(), host[3].numpy(),
                              args.e2e_rk_steps, host[4].numpy())
-            ev[1].record(stream)
+                ev[q + 1].record(stream)
         torch.cuda.synchronize()
-        e2e_ms = dist.max(ev[0].elapsed_time(ev[1]))
+        e2e_ms = dist.max(ev[0].elapsed_time(ev[-1]))
+        per_call = [ev[q].elapsed_time(ev[q + 1]) for q in range(args.e2e_steps)]
         e2e = {"value": dist.world * cells * args.e2e_rk_steps * args.e2e_steps / (e2e_ms * 1e-3) / 1e9,
                "unit": "Gcell-updates/s", "h2d_bytes_per_step": 4 * shape[0] ** 3 * 8,
                "d2h_bytes_per_step": shape[0] ** 3 * 8,
                "call": "lsgb_solver_run_host (ghosted FP64 host arrays G,u,v,w in, G out)",
-               "rk3_steps_per_call": args.e2e_rk_steps, "host_link": link}
+               "rk3_steps_per_call": args.e2e_rk_steps, "ms_per_call": per_call, "host_link": link}
         del host
 
     # --- plain FP64 form beside it, and the FP32-vs-FP64 error after the same steps ---
