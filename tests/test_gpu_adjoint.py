@@ -246,6 +246,27 @@ def test_f32_adjoint_close_to_f64(cuda, lsgb_mod):
     assert rel <= 1e-3
 
 
+@pytest.mark.parametrize("bc", [None, ("periodic", ZG)], ids=["periodic", "zgy"])
+def test_f32_adjoint_close_to_f64_2d(cuda, lsgb_mod, bc):
+    """The 2D FP32 adjoint (one cell per thread, the zero-gradient gather on
+    the reference's default boundaries) against the FP64 one: relative L2
+    <= 1e-3 for dL/dS_L and dL/dG0."""
+    adj, p, steps, G0, u, v, w, sl, sl_t = small(lsgb_mod, 2, bc)
+    out = {}
+    for prec in ("f64", "f32"):
+        prob = adj.Problem(p, G0, u, v, w, prec, checkpoint=6)
+        try:
+            prob.target(sl_t, steps)
+            _, g = prob.gradient(sl, steps)
+            out[prec] = (g, prob.a.grad("G0"))
+        finally:
+            prob.close()
+    for g32, g64 in zip(out["f32"], out["f64"]):
+        rel = np.linalg.norm(g32 - g64) / np.linalg.norm(g64)
+        print(f"2D {bc}: f32 vs f64 adjoint rel L2 {rel:.3e}")
+        assert rel <= 1e-3
+
+
 def test_torch_rollout_gradients(cuda, lsgb_mod):
     import torch
     adj, p, steps, G0, u, v, w, sl, sl_t = small(lsgb_mod, 3)
