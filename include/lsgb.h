@@ -295,8 +295,9 @@ LSGB_API int lsgb_solver_autotune(lsgb_solver* s, int reps, int* best_tile, floa
  * one instance per process, e.g. the sweep of sample/submit_all.sh:9-11).
  * Two forms of the graph:
  *   LSGB_BATCH_GROUPED (default; FP32, every instance < 2^31 cells, one HCR-2
- *     pseudo-step count): one kernel launch per RK3 stage, per pseudo-step
- *     and for the copy back, for all 3D instances, and one for all 2D ones;
+ *     pseudo-step count): one kernel launch per RK3 stage and per
+ *     pseudo-step (and, for an odd pseudo-step count, for the copy back)
+ *     for all 3D instances, and one for all 2D ones;
  *     the kernels walk a block / tile list that spans the instances, with
  *     each instance's fields and coefficients in a descriptor table;
  *   LSGB_BATCH_LANES (FP64 batches, or on request): each instance's own
